@@ -1,0 +1,337 @@
+#!/usr/bin/env python
+"""Benchmark: FP64 SSP-RK3 steps of the Flame3D finite-difference RHS on one GB300.
+
+Workload (the configuration the headline metric is quoted on): Sod shock tube on a
+perturbed curvilinear grid, 256 x 64 x 64 interior cells (264 x 72 x 72 with ghosts),
+x = xi + 0.02 sin(2 pi eta) sin(2 pi zeta) and cyclic, metrics and J computed from these
+coordinates on the device, hybrid UP7/WENO7/WENO5/NND2 with the shock sensor,
+characteristic-wise reconstruction, Steger-Warming splitting, inviscid, zero-gradient x and
+periodic y, z. A step is one SSP-RK3 time step = 3 RHS evaluations; the metric counts
+interior cells x RHS evaluations per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the C++ restatement
+in oracle/, OpenMP over all host cores) on the same workload; Julia is not available to
+run the reference's own code. Under torchrun each rank runs an independent replica (the
+path is single-GPU by design: no sharding, no collectives); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mcell-RHS/s FP64 vs mixed at stated L-inf err; adjoint/forward step time"
+UNIT = "Mcell-RHS/s"
+WORKLOAD = dict(nx=256, ny=64, nz=64)
+NG = 4
+
+# Algorithmic (compulsory) bytes per interior cell of each kernel of one stage, FP64:
+# what the kernel must read and write at least once given its interface.
+#   sweep (first, OUT_SET): Q 6 + c 1 + metric row 3 + A/|A| 3 + |A| 1 + phi 1 read, acc 5 write
+#   sweep (second, OUT_ADD): the same reads + acc 5 read + acc 5 write
+#   sweep (last, OUT_STAGE): the same reads + acc 5 + U 5 + Un 5 (stages 2,3) + J 1 read, U 5 write
+#   prim_ghost_fill: U 5 read, Q 6 write;  sound_speed: T (or p, rho) read, c write;
+#   shock_sensor: p read, phi write
+KERNEL_BYTES_PER_CELL = {
+    "sweep_xi": 8 * (15 + 5),
+    "sweep_eta": 8 * (15 + 10),
+    "sweep_zeta": 8 * (15 + 16 + 5),
+    "prim_ghost_fill": 8 * (5 + 6),
+    "sound_speed": 8 * 2,
+    "shock_sensor": 8 * 2,
+    "viscous_flux": 8 * (6 + 10 + 12),
+}
+# one RK3 step of the whole RHS: 3 x (U + 9 metrics + J read, U written) + 2 x Un read
+STEP_BYTES_PER_CELL = 3 * 160 + 2 * 40
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float) -> dict:
+        rows = [r for t, r in self.rows if t0 <= t <= t1] or [r for _, r in self.rows]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample(target_s: float = 12.0, max_steps: int = 8) -> dict:
+    """The oracle (C++ restatement of the reference algorithm, OpenMP on every host core) on
+    the same workload: one untimed step, then whole RK3 steps until about target_s."""
+    import numpy as np
+
+    from flame3d_mhd_gb300 import cases
+    from oracle import oracle as orc
+    threads = orc.set_threads(os.cpu_count() or 1)
+    c = cases.sod(**WORKLOAD)
+    P = c["params"]
+    m, J, Q, U = orc.prepare(P, c["Q"], c["x"], c["y"], c["z"])
+    Un = np.zeros_like(U)
+    s = orc.PersistentSolver(P, m, J)
+    s.rk3(1, c["dt"], U, Un, Q)
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps and (time.perf_counter() - t0) < target_s:
+        s.rk3(1, c["dt"], U, Un, Q)
+        steps += 1
+    dt = time.perf_counter() - t0
+    s.close()
+    cells = WORKLOAD["nx"] * WORKLOAD["ny"] * WORKLOAD["nz"]
+    return {"value": cells * 3 * steps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} SSP-RK3 steps ({3 * steps} RHS) of the {WORKLOAD['nx']}x{WORKLOAD['ny']}x"
+                      f"{WORKLOAD['nz']} workload after 1 untimed step, {dt:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    from flame3d_mhd_gb300 import cases
+    from oracle import oracle as orc
+    threads = orc.set_threads(os.cpu_count() or 1)
+    c = cases.sod(**WORKLOAD)
+    P = c["params"]
+    m, J, Q, U = orc.prepare(P, c["Q"], c["x"], c["y"], c["z"])
+    Un = np.zeros_like(U)
+    s = orc.PersistentSolver(P, m, J)
+    s.rk3(max(args.warmup, 1), c["dt"], U, Un, Q)
+    t0 = time.perf_counter()
+    s.rk3(args.steps, c["dt"], U, Un, Q)
+    dt = time.perf_counter() - t0
+    s.close()
+    cells = WORKLOAD["nx"] * WORKLOAD["ny"] * WORKLOAD["nz"]
+    value = cells * 3 * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sod_curvilinear_256x64x64_hybrid_char_SW_inviscid", **WORKLOAD,
+                   "parallelism": "openmp", "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} SSP-RK3 steps of the full workload after {max(args.warmup, 1)} "
+                                   f"untimed; C++ restatement of the reference formulas (Julia absent)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from flame3d_mhd_gb300 import build as fbuild
+    fbuild.build()
+    from flame3d_mhd_gb300 import cases
+    from flame3d_mhd_gb300.solver import Flame3D
+
+    c = cases.sod(**WORKLOAD)
+    P = c["params"]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    s = Flame3D(P)
+    ms, J = s.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
+    s.set_metrics(ms, J)
+    Q = dev(c["Q"])
+    U, Un = s.field(5), s.field(5)
+    s.prim2c(U, Q)
+    s.fillGhost(Q, U)
+    Q0, U0 = Q.clone(), U.clone()
+    dt = c["dt"]
+    cells = P.nx * P.ny * P.nz
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    stream = torch.cuda.Stream()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            s.time_step(U, Un, Q, dt, 1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        tw0 = time.time()
+        e0.record(stream)
+        s.time_step(U, Un, Q, dt, args.steps)
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        tw1 = time.time()
+    sampler.stop()
+    ms_total = e0.elapsed_time(e1)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = ws * cells * 3 * args.steps / (ms_total / 1e3) / 1e6
+    ok = s.check_finite(U)
+
+    # per-kernel device times of single steps (events between launches, outside the timed loop)
+    prof = {}
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            for k, (t_ms, n) in s.profile_step(U, Un, Q, dt).items():
+                a = prof.setdefault(k, [0.0, 0])
+                a[0] += t_ms
+                a[1] += n
+    launches_per_step = sum(n for _, n in prof.values()) // 3
+    total_ms = sum(t for t, _ in prof.values())
+    top = max(prof, key=lambda k: prof[k][0])
+    top_avg_ms = prof[top][0] / prof[top][1]
+    peaks = load_peaks()
+    alg = KERNEL_BYTES_PER_CELL[top] * cells
+    achieved = alg / (top_avg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": top,
+                "peak_source": peaks["source"],
+                "alg_bytes_per_launch": alg, "avg_launch_ms": top_avg_ms,
+                "shares": {k: round(v[0] / total_ms, 4) for k, v in sorted(prof.items())}}
+    step_gbs = STEP_BYTES_PER_CELL * cells / (ms_step / 1e3) / 1e9
+
+    # end to end through the public API with host buffers: H2D of U and Q, one step, D2H of U
+    U_h = U0.cpu().pin_memory()
+    Q_h = Q0.cpu().pin_memory()
+    U_out = torch.empty_like(U_h).pin_memory()
+    e2e_steps = max(3, min(args.steps, 20))
+    with torch.cuda.stream(stream):
+        for it in range(e2e_steps + 1):
+            if it == 1:
+                stream.synchronize()
+                f0 = torch.cuda.Event(enable_timing=True)
+                f1 = torch.cuda.Event(enable_timing=True)
+                f0.record(stream)
+            U.copy_(U_h, non_blocking=True)
+            Q.copy_(Q_h, non_blocking=True)
+            s.time_step(U, Un, Q, dt, 1)
+            U_out.copy_(U, non_blocking=True)
+        f1.record(stream)
+        f1.synchronize()
+    e2e_ms = f0.elapsed_time(f1) / e2e_steps
+    e2e_value = ws * cells * 3 / (e2e_ms / 1e3) / 1e6
+    nbytes = U.numel() * 8
+
+    clocks = sampler.summary(tw0, tw1)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "sod_curvilinear_256x64x64_hybrid_char_SW_inviscid", **WORKLOAD,
+                   "precision": "fp64", "step": "one SSP-RK3 step (3 RHS)", "parallelism": f"replicas{ws}",
+                   "l2": "inputs larger than L2 (state + metrics + scratch ~0.5 GB)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes + Q.numel() * 8,
+                "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
+                "per_step": "H2D of U and Q from pinned host memory, one RK3 step, D2H of U"},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": roofline,
+        "roofline_step": {"bound": "hbm", "achieved": step_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                          "frac": step_gbs / peaks["hbm_gbs"], "alg_bytes_per_cell_step": STEP_BYTES_PER_CELL},
+        "mcell_updates_per_s": value / 3,
+        "clocks": clocks,
+        "state_finite": bool(ok),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

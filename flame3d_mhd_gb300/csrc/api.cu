@@ -1,0 +1,558 @@
+// api.cu — the extern "C" boundary of libflame3d_gpu.so (declared in include/flame3d_gpu.h).
+//
+// It replaces the @cuda launch sites of the reference's finite-difference path:
+// flowAdvance (solver.jl:19-189), the RK3 stage loop (solver.jl:416-444), exchange_ghost
+// (mpi.jl:2-103) and fillGhost (boundary.jl:151-156). Every entry point validates its
+// arguments, launches asynchronously on the caller's stream and returns a status code.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "f3d_kernels.cuh"
+
+using namespace f3d;
+
+// Per-launch event recording for f3d_profile_step.
+struct Prof {
+    static constexpr int kMax = 64;
+    cudaEvent_t ev[kMax];
+    int kind[kMax];
+    int n = 0;
+};
+
+struct f3d_ctx {
+    f3d_params params;
+    DevParams dp;
+    int device = 0;
+    std::string err;
+    const double* m[9] = {};
+    const double* J = nullptr;
+    bool metrics_set = false;
+    // scratch (one allocation)
+    void* slab = nullptr;
+    size_t slab_bytes = 0;
+    double* S[3] = {};
+    double* Ah[9] = {};
+    double* csnd = nullptr;
+    double* phi = nullptr;
+    double* acc = nullptr;
+    double* Fv[3] = {};
+    double* dscalar = nullptr;  // 8 bytes for reductions
+    Prof* prof = nullptr;
+    // CUDA graph of one RK3 step, keyed by its arguments
+    cudaGraphExec_t step_graph = nullptr;
+    const void* g_key[4] = {};
+    double g_dt = 0.0;
+};
+
+namespace {
+
+enum KernelKind { K_SOUND = 0, K_SENSOR, K_VISCOUS, K_SWEEP_X, K_SWEEP_Y, K_SWEEP_Z, K_PRIM_FILL, K_NKIND };
+const char* kKernelNames[K_NKIND] = {"sound_speed", "shock_sensor", "viscous_flux", "sweep_xi",
+                                     "sweep_eta", "sweep_zeta", "prim_ghost_fill"};
+
+void mark(f3d_ctx* ctx, int kind, cudaStream_t st) {
+    Prof* p = ctx->prof;
+    if (p && p->n < Prof::kMax) {
+        cudaEventRecord(p->ev[p->n], st);
+        p->kind[p->n++] = kind;
+    }
+}
+
+int fail(f3d_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_fail(f3d_ctx* ctx, cudaError_t e, const char* where) {
+    return fail(ctx, F3D_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define F3D_CUDA(ctx, call)                                              \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);      \
+    } while (0)
+
+bool aligned(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+int check_ptrs(f3d_ctx* ctx, std::initializer_list<const void*> ps) {
+    for (const void* p : ps) {
+        if (!p) return fail(ctx, F3D_ERR_ARG, "null array pointer");
+        if (!aligned(p)) return fail(ctx, F3D_ERR_ALIGN, "array pointer not 16-byte aligned");
+    }
+    return F3D_OK;
+}
+
+// Branch every face takes when the thresholds leave no choice for a sensor value in
+// [0, 3] (each directional term of schemes.jl:19-21 lies in [0,1] for positive p).
+int fixed_branch_of(const f3d_params& p) {
+    const double top = 4.0;
+    if (p.phi1 > top) return 0;
+    if (p.phi1 <= 0.0 && p.phi2 > top) return 1;
+    if (p.phi1 <= 0.0 && p.phi2 <= 0.0 && p.phi3 > top) return 2;
+    if (p.phi1 <= 0.0 && p.phi2 <= 0.0 && p.phi3 <= 0.0) return 3;
+    return -1;
+}
+
+int validate(const f3d_params& p, std::string& why) {
+    if (p.ng != NG) { why = "ng must be 4"; return F3D_ERR_ARG; }
+    if (p.nx < NG || p.ny < NG || p.nz < NG) { why = "each interior dimension must be >= 4"; return F3D_ERR_ARG; }
+    if ((long long)p.nx > (1 << 20) || (long long)p.ny > 65535 - 8 || (long long)p.nz > 65535 - 8) {
+        why = "grid too large for the launch shape"; return F3D_ERR_ARG;
+    }
+    const long long cells = (long long)(p.nx + 8) * (p.ny + 8) * (p.nz + 8);
+    if (cells > (1LL << 34)) { why = "grid too large"; return F3D_ERR_ARG; }
+    if (!(p.gamma > 1.0) || !(p.rg > 0.0) || !(p.pr > 0.0) || !(p.c_s >= 0.0) || !(p.t_s >= 0.0)) {
+        why = "gas constants out of range"; return F3D_ERR_ARG;
+    }
+    if (p.split_method < 0 || p.split_method > 3) { why = "unknown split_method"; return F3D_ERR_ARG; }
+    if (p.character != 0 && p.character != 1) { why = "character must be 0 or 1"; return F3D_ERR_ARG; }
+    if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
+    if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
+    if (p.precision == F3D_PREC_MIXED) { why = "mixed precision is not built in this library"; return F3D_ERR_UNSUPPORTED; }
+    int iso_dirs = 0;
+    for (int d = 0; d < 3; d++) {
+        const f3d_bc &lo = p.bc[2 * d], &hi = p.bc[2 * d + 1];
+        for (const f3d_bc* b : {&lo, &hi}) {
+            if (b->kind < 0 || b->kind > 4) { why = "unknown boundary kind"; return F3D_ERR_ARG; }
+            if (b->kind == F3D_BC_DIRICHLET && !(b->rho > 0.0 && b->p > 0.0)) {
+                why = "Dirichlet state needs rho > 0 and p > 0"; return F3D_ERR_ARG;
+            }
+            if (b->kind == F3D_BC_WALL_ISOTHERMAL && !(b->t_wall > 0.0)) {
+                why = "isothermal wall needs t_wall > 0"; return F3D_ERR_ARG;
+            }
+        }
+        if ((lo.kind == F3D_BC_PERIODIC) != (hi.kind == F3D_BC_PERIODIC)) {
+            why = "periodic boundaries must be paired on both faces of a direction"; return F3D_ERR_ARG;
+        }
+        if (lo.kind == F3D_BC_WALL_ISOTHERMAL || hi.kind == F3D_BC_WALL_ISOTHERMAL) iso_dirs++;
+    }
+    if (iso_dirs > 1) { why = "isothermal walls on more than one direction are not supported"; return F3D_ERR_UNSUPPORTED; }
+    return F3D_OK;
+}
+
+DevParams make_dev(const f3d_params& p) {
+    DevParams d;
+    std::memset(&d, 0, sizeof(d));
+    d.nx = p.nx; d.ny = p.ny; d.nz = p.nz;
+    d.nxt = p.nx + 2 * NG; d.nyt = p.ny + 2 * NG; d.nzt = p.nz + 2 * NG;
+    d.plane = (long long)d.nxt * d.nyt * d.nzt;
+    d.gamma = p.gamma; d.rg = p.rg;
+    d.cp = p.cp != 0.0 ? p.cp : p.rg * p.gamma / (p.gamma - 1.0);
+    d.c_s = p.c_s; d.t_s = p.t_s; d.pr = p.pr;
+    d.gm1 = p.gamma - 1.0;
+    d.grg = p.gamma * p.rg;
+    d.eps_clamp = p.clamp_eps != 0.0 ? p.clamp_eps : 1.1920928955078125e-07;
+    d.phi1 = p.phi1; d.phi2 = p.phi2; d.phi3 = p.phi3;
+    const double up7[7] = {-3.0 / 420, 25.0 / 420, -101.0 / 420, 319.0 / 420, 214.0 / 420, -38.0 / 420, 4.0 / 420};
+    const double cd6[7] = {0.0, 1.0 / 60, -2.0 / 15, 37.0 / 60, 37.0 / 60, -2.0 / 15, 1.0 / 60};
+    for (int m = 0; m < 7; m++) d.lin[m] = up7[m] * p.linear_phi + cd6[m] * (1.0 - p.linear_phi);
+    d.split = p.split_method; d.character = p.character; d.viscous = p.viscous;
+    d.fixed_branch = fixed_branch_of(p);
+    for (int f = 0; f < 6; f++) {
+        const f3d_bc& b = p.bc[f];
+        d.bc[f].kind = b.kind;
+        d.bc[f].rho = b.rho; d.bc[f].u = b.u; d.bc[f].v = b.v; d.bc[f].w = b.w; d.bc[f].p = b.p;
+        d.bc[f].T = b.kind == F3D_BC_DIRICHLET ? b.p / (b.rho * p.rg) : 0.0;
+        d.bc[f].t_wall = b.t_wall;
+    }
+    return d;
+}
+
+int check_ctx(f3d_ctx* ctx, bool need_metrics) {
+    if (!ctx) return F3D_ERR_ARG;
+    if (need_metrics && !ctx->metrics_set) return fail(ctx, F3D_ERR_STATE, "metrics not set (call f3d_set_metrics)");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, F3D_ERR_CUDA, "cudaSetDevice failed");
+    return F3D_OK;
+}
+
+SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, const double* phi) {
+    SweepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.P = ctx->dp;
+    a.Q = Q;
+    a.csnd = ctx->csnd;
+    for (int n = 0; n < 3; n++) {
+        a.A[n] = ctx->m[3 * dir + n];
+        a.Ah[n] = ctx->Ah[3 * dir + n];
+    }
+    a.S = ctx->S[dir];
+    a.phi = phi;
+    a.Fv = ctx->params.viscous ? ctx->Fv[dir] : nullptr;
+    a.J = ctx->J;
+    return a;
+}
+
+// Sensor, viscous fluxes and the three sweeps. mode_last is OUT_RHS or OUT_STAGE.
+int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStream_t st) {
+    const DevParams& P = ctx->dp;
+    F3D_CUDA(ctx, launch_sound(P, Q, ctx->csnd, st));
+    mark(ctx, K_SOUND, st);
+    const bool hybrid = P.fixed_branch < 0;
+    if (hybrid) {
+        F3D_CUDA(ctx, launch_sensor(P, Q, ctx->phi, st));
+        mark(ctx, K_SENSOR, st);
+    }
+    if (ctx->params.viscous) {
+        F3D_CUDA(ctx, launch_viscous(P, Q, ctx->m, ctx->J, ctx->Fv[0], ctx->Fv[1], ctx->Fv[2], st));
+        mark(ctx, K_VISCOUS, st);
+    }
+    for (int d = 0; d < 3; d++) {
+        SweepArgs a = sweep_args(ctx, d, Q, hybrid ? ctx->phi : nullptr);
+        a.acc = acc;
+        if (d == 0) a.out_mode = OUT_SET;
+        else if (d == 1) a.out_mode = OUT_ADD;
+        else {
+            a.out_mode = last.out_mode;
+            a.out = last.out;
+            a.U = last.U;
+            a.Un = last.Un;
+            a.dt = last.dt;
+            a.ca = last.ca;
+            a.cb = last.cb;
+            a.combine = last.combine;
+            a.stage1_copy = last.stage1_copy;
+        }
+        F3D_CUDA(ctx, launch_sweep(d, a, st));
+        mark(ctx, K_SWEEP_X + d, st);
+    }
+    return F3D_OK;
+}
+
+int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double* Q, cudaStream_t st) {
+    SweepArgs last;
+    std::memset(&last, 0, sizeof(last));
+    last.out_mode = OUT_STAGE;
+    last.U = U;
+    last.Un = Un;
+    last.dt = dt;
+    last.stage1_copy = stage == 1;
+    last.combine = stage != 1;
+    last.ca = stage == 2 ? 0.25 : 2.0 / 3.0;  // utils.jl:57-70 via solver.jl:433-435
+    last.cb = stage == 2 ? 0.75 : 1.0 / 3.0;
+    int rc = run_rhs(ctx, Q, ctx->acc, last, st);
+    if (rc) return rc;
+    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 0, st));
+    mark(ctx, K_PRIM_FILL, st);
+    return F3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int f3d_version(void) { return F3D_VERSION; }
+
+int f3d_default_params(int nx, int ny, int nz, f3d_params* p) {
+    if (!p) return F3D_ERR_ARG;
+    std::memset(p, 0, sizeof(*p));
+    p->nx = nx; p->ny = ny; p->nz = nz; p->ng = NG;
+    p->gamma = 1.4; p->rg = 287.0; p->cp = 0.0; p->c_s = 1.458e-6; p->t_s = 110.4; p->pr = 0.72;  // run.jl:8-13
+    p->phi1 = 0.05; p->phi2 = 1.0; p->phi3 = 10.0; p->linear_phi = 1.0;                          // run.jl:70-73
+    p->clamp_eps = 0.0;
+    p->split_method = F3D_SPLIT_SW; p->character = 1; p->viscous = 1;                            // run.jl:61,68,69
+    p->precision = F3D_PREC_FP64;
+    // boundary.jl: Dirichlet free stream inlet, zero-gradient outlet, adiabatic no-slip wall,
+    // Dirichlet far field, periodic span.
+    f3d_bc fs;
+    std::memset(&fs, 0, sizeof(fs));
+    fs.kind = F3D_BC_DIRICHLET; fs.rho = 1.0; fs.u = 0.5; fs.v = 0.0; fs.w = 0.0; fs.p = 1.0 / 1.4;
+    p->bc[0] = fs;
+    p->bc[1].kind = F3D_BC_ZERO_GRADIENT;
+    p->bc[2].kind = F3D_BC_WALL_ADIABATIC;
+    p->bc[3] = fs;
+    p->bc[4].kind = F3D_BC_PERIODIC;
+    p->bc[5].kind = F3D_BC_PERIODIC;
+    return F3D_OK;
+}
+
+int f3d_create(const f3d_params* p, f3d_ctx** out) {
+    if (!p || !out) return F3D_ERR_ARG;
+    *out = nullptr;
+    std::string why;
+    int rc = validate(*p, why);
+    if (rc) {
+        std::fprintf(stderr, "f3d_create: %s\n", why.c_str());
+        return rc;
+    }
+    f3d_ctx* ctx = new f3d_ctx();
+    ctx->params = *p;
+    ctx->dp = make_dev(*p);
+    if (cudaGetDevice(&ctx->device) != cudaSuccess) { delete ctx; return F3D_ERR_CUDA; }
+    const size_t nc = (size_t)ctx->dp.plane;
+    const size_t nv = (size_t)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
+    // S(3) + Ah(9) + csnd + phi + acc(5) + viscous(12) + scalar
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t b1 = up(nc * sizeof(double));
+    size_t total = b1 * (3 + 9 + 1 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * sizeof(double)) : 0) + 256;
+    cudaError_t e = cudaMalloc(&ctx->slab, total);
+    if (e != cudaSuccess) {
+        delete ctx;
+        std::fprintf(stderr, "f3d_create: cudaMalloc(%zu) failed: %s\n", total, cudaGetErrorString(e));
+        return F3D_ERR_CUDA;
+    }
+    ctx->slab_bytes = total;
+    char* q = (char*)ctx->slab;
+    for (int d = 0; d < 3; d++) { ctx->S[d] = (double*)q; q += b1; }
+    for (int n = 0; n < 9; n++) { ctx->Ah[n] = (double*)q; q += b1; }
+    ctx->csnd = (double*)q; q += b1;
+    ctx->phi = (double*)q; q += b1;
+    ctx->acc = (double*)q; q += 5 * b1;
+    if (p->viscous)
+        for (int d = 0; d < 3; d++) { ctx->Fv[d] = (double*)q; q += up(nv * 4 * sizeof(double)); }
+    ctx->dscalar = (double*)q;
+    // phi outside cells 1..Nt-2 is never written; keep it defined (CUDA.zeros in solver.jl:296)
+    if ((e = cudaMemset(ctx->phi, 0, b1)) != cudaSuccess || (e = sweep_configure()) != cudaSuccess) {
+        cudaFree(ctx->slab);
+        delete ctx;
+        std::fprintf(stderr, "f3d_create: %s\n", cudaGetErrorString(e));
+        return F3D_ERR_CUDA;
+    }
+    *out = ctx;
+    return F3D_OK;
+}
+
+int f3d_destroy(f3d_ctx* ctx) {
+    if (!ctx) return F3D_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
+    cudaError_t e = cudaFree(ctx->slab);
+    delete ctx;
+    return e == cudaSuccess ? F3D_OK : F3D_ERR_CUDA;
+}
+
+const char* f3d_last_error(const f3d_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int f3d_scratch_bytes(const f3d_ctx* ctx, size_t* bytes) {
+    if (!ctx || !bytes) return F3D_ERR_ARG;
+    *bytes = ctx->slab_bytes;
+    return F3D_OK;
+}
+
+int f3d_set_metrics(f3d_ctx* ctx, const double* const metrics[9], const double* jac, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!metrics) return fail(ctx, F3D_ERR_ARG, "null metrics array");
+    if ((rc = check_ptrs(ctx, {metrics[0], metrics[1], metrics[2], metrics[3], metrics[4], metrics[5], metrics[6],
+                              metrics[7], metrics[8], jac})))
+        return rc;
+    for (int n = 0; n < 9; n++) ctx->m[n] = metrics[n];
+    ctx->J = jac;
+    F3D_CUDA(ctx, launch_metric_prep(ctx->dp, ctx->m, ctx->S, ctx->Ah, (cudaStream_t)stream));
+    ctx->metrics_set = true;
+    return F3D_OK;
+}
+
+int f3d_compute_metrics(f3d_ctx* ctx, const double* x, const double* y, const double* z, double* const metrics[9],
+                        double* jac, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!metrics) return fail(ctx, F3D_ERR_ARG, "null metrics array");
+    if ((rc = check_ptrs(ctx, {x, y, z, metrics[0], metrics[1], metrics[2], metrics[3], metrics[4], metrics[5],
+                              metrics[6], metrics[7], metrics[8], jac})))
+        return rc;
+    F3D_CUDA(ctx, launch_metrics(ctx->dp, x, y, z, metrics, jac, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_c2prim(f3d_ctx* ctx, const double* U, double* Q, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;
+    F3D_CUDA(ctx, launch_c2prim_interior(ctx->dp, U, Q, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_prim2c(f3d_ctx* ctx, const double* Q, double* U, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;
+    F3D_CUDA(ctx, launch_prim2c(ctx->dp, Q, U, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_lincomb(f3d_ctx* ctx, double* U, const double* Un, double a, double b, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Un}))) return rc;
+    F3D_CUDA(ctx, launch_lincomb(ctx->dp, U, Un, a, b, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_fill_ghosts(f3d_ctx* ctx, double* Q, double* U, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;
+    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 1, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_rhs(f3d_ctx* ctx, const double* Q, double* dUdt, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {Q, dUdt}))) return rc;
+    SweepArgs last;
+    std::memset(&last, 0, sizeof(last));
+    last.out_mode = OUT_RHS;
+    last.out = dUdt;
+    return run_rhs(ctx, Q, dUdt, last, (cudaStream_t)stream);
+}
+
+int f3d_rk3_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double* Q, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
+    if (stage < 1 || stage > 3) return fail(ctx, F3D_ERR_ARG, "stage must be 1, 2 or 3");
+    return run_stage(ctx, stage, dt, U, Un, Q, (cudaStream_t)stream);
+}
+
+int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, double* Q, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
+    if (nsteps < 0) return fail(ctx, F3D_ERR_ARG, "nsteps must be >= 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (st == nullptr) {  // the legacy stream cannot be captured: plain launches
+        for (int t = 0; t < nsteps; t++)
+            for (int s = 1; s <= 3; s++)
+                if ((rc = run_stage(ctx, s, dt, U, Un, Q, st))) return rc;
+        return F3D_OK;
+    }
+    const void* key[4] = {U, Un, Q, st};
+    bool hit = ctx->step_graph && ctx->g_dt == dt;
+    for (int n = 0; n < 4 && hit; n++) hit = ctx->g_key[n] == key[n];
+    if (!hit) {
+        if (ctx->step_graph) {
+            cudaGraphExecDestroy(ctx->step_graph);
+            ctx->step_graph = nullptr;
+        }
+        cudaGraph_t g;
+        F3D_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int src = F3D_OK;
+        for (int s = 1; s <= 3 && !src; s++) src = run_stage(ctx, s, dt, U, Un, Q, st);
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (src) return src;
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&ctx->step_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaGraphInstantiate");
+        for (int n = 0; n < 4; n++) ctx->g_key[n] = key[n];
+        ctx->g_dt = dt;
+    }
+    for (int t = 0; t < nsteps; t++) F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
+    return F3D_OK;
+}
+
+int f3d_kernel_count(void) { return K_NKIND; }
+
+const char* f3d_kernel_name(int kind) { return (kind >= 0 && kind < K_NKIND) ? kKernelNames[kind] : "unknown"; }
+
+int f3d_profile_step(f3d_ctx* ctx, double dt, double* U, double* Un, double* Q, f3d_stream stream, double* ms_out,
+                     int* launches_out) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
+    if (!ms_out || !launches_out) return fail(ctx, F3D_ERR_ARG, "null output arrays");
+    cudaStream_t st = (cudaStream_t)stream;
+    Prof prof;
+    for (int i = 0; i < Prof::kMax; i++) F3D_CUDA(ctx, cudaEventCreate(&prof.ev[i]));
+    ctx->prof = &prof;
+    mark(ctx, -1, st);
+    for (int s = 1; s <= 3 && !rc; s++) rc = run_stage(ctx, s, dt, U, Un, Q, st);
+    ctx->prof = nullptr;
+    cudaError_t e = cudaStreamSynchronize(st);
+    for (int k = 0; k < K_NKIND; k++) {
+        ms_out[k] = 0.0;
+        launches_out[k] = 0;
+    }
+    if (!rc && e == cudaSuccess) {
+        for (int i = 1; i < prof.n; i++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, prof.ev[i - 1], prof.ev[i]);
+            ms_out[prof.kind[i]] += ms;
+            launches_out[prof.kind[i]] += 1;
+        }
+    }
+    for (int i = 0; i < Prof::kMax; i++) cudaEventDestroy(prof.ev[i]);
+    if (rc) return rc;
+    return e == cudaSuccess ? F3D_OK : cuda_fail(ctx, e, "cudaStreamSynchronize");
+}
+
+int f3d_cfl_dt(f3d_ctx* ctx, const double* Q, double cfl, double* dt_out, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {Q}))) return rc;
+    if (!dt_out || !(cfl > 0.0)) return fail(ctx, F3D_ERR_ARG, "need cfl > 0 and dt_out");
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned long long inf = 0x7ff0000000000000ULL;
+    F3D_CUDA(ctx, cudaMemcpyAsync(ctx->dscalar, &inf, 8, cudaMemcpyHostToDevice, st));
+    F3D_CUDA(ctx, launch_cfl(ctx->dp, Q, ctx->m, ctx->J, cfl, (unsigned long long*)ctx->dscalar, st));
+    F3D_CUDA(ctx, cudaMemcpyAsync(dt_out, ctx->dscalar, 8, cudaMemcpyDeviceToHost, st));
+    F3D_CUDA(ctx, cudaStreamSynchronize(st));
+    return F3D_OK;
+}
+
+int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U}))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    int flag = 0;
+    F3D_CUDA(ctx, cudaMemsetAsync(ctx->dscalar, 0, 8, st));
+    F3D_CUDA(ctx, launch_check_finite(ctx->dp, U, (int*)ctx->dscalar, st));
+    F3D_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->dscalar, 4, cudaMemcpyDeviceToHost, st));
+    F3D_CUDA(ctx, cudaStreamSynchronize(st));
+    return flag ? fail(ctx, F3D_ERR_NONFINITE, "non-finite value in U") : F3D_OK;
+}
+
+int f3d_debug_sensor(f3d_ctx* ctx, const double* Q, double* phi, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {Q, phi}))) return rc;
+    F3D_CUDA(ctx, launch_sensor(ctx->dp, Q, phi, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_debug_split(f3d_ctx* ctx, int dir, const double* Q, double* Fp, double* Fm, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {Q, Fp, Fm}))) return rc;
+    if (dir < 0 || dir > 2) return fail(ctx, F3D_ERR_ARG, "dir must be 0, 1 or 2");
+    cudaStream_t st = (cudaStream_t)stream;
+    F3D_CUDA(ctx, launch_sound(ctx->dp, Q, ctx->csnd, st));
+    const double* A[3] = {ctx->m[3 * dir], ctx->m[3 * dir + 1], ctx->m[3 * dir + 2]};
+    const double* H[3] = {ctx->Ah[3 * dir], ctx->Ah[3 * dir + 1], ctx->Ah[3 * dir + 2]};
+    F3D_CUDA(ctx, launch_split_debug(ctx->dp, Q, ctx->csnd, A, H, ctx->S[dir], Fp, Fm, st));
+    return F3D_OK;
+}
+
+int f3d_debug_face_flux(f3d_ctx* ctx, int dir, const double* Q, const double* phi, double* F, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {Q, F}))) return rc;
+    if (dir < 0 || dir > 2) return fail(ctx, F3D_ERR_ARG, "dir must be 0, 1 or 2");
+    const bool hybrid = ctx->dp.fixed_branch < 0;
+    if (hybrid && !phi) return fail(ctx, F3D_ERR_ARG, "hybrid thresholds need phi");
+    cudaStream_t st = (cudaStream_t)stream;
+    F3D_CUDA(ctx, launch_sound(ctx->dp, Q, ctx->csnd, st));
+    SweepArgs a = sweep_args(ctx, dir, Q, hybrid ? phi : nullptr);
+    a.out_mode = OUT_FACES;
+    a.faces = F;
+    a.Fv = nullptr;
+    F3D_CUDA(ctx, launch_sweep(dir, a, st));
+    return F3D_OK;
+}
+
+int f3d_debug_viscous(f3d_ctx* ctx, const double* Q, double* Fvx, double* Fvy, double* Fvz, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {Q, Fvx, Fvy, Fvz}))) return rc;
+    F3D_CUDA(ctx, launch_viscous(ctx->dp, Q, ctx->m, ctx->J, Fvx, Fvy, Fvz, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_div(f3d_ctx* ctx, double* U, const double* Fx, const double* Fy, const double* Fz, const double* Fvx,
+            const double* Fvy, const double* Fvz, double dt, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U, Fx, Fy, Fz}))) return rc;
+    const bool visc = Fvx || Fvy || Fvz;
+    if (visc && (rc = check_ptrs(ctx, {Fvx, Fvy, Fvz}))) return rc;
+    F3D_CUDA(ctx, launch_div_ref(ctx->dp, U, Fx, Fy, Fz, visc ? Fvx : nullptr, Fvy, Fvz, ctx->J, dt,
+                                 (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_measure_pipes(double* fp64_tflops, double* fp32_tflops) {
+    if (!fp64_tflops || !fp32_tflops) return F3D_ERR_ARG;
+    return measure_pipes(fp64_tflops, fp32_tflops) == cudaSuccess ? F3D_OK : F3D_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,188 @@
+// f3d_flux.cuh — per-cell flux splitting and per-face reconstruction, templated on the
+// arithmetic type (double for the FP64 drop-in, float for the mixed-precision form).
+#pragma once
+#include "f3d_common.cuh"
+
+namespace f3d {
+
+// Flux-vector splitting of one cell (split.jl). q = (rho,u,v,w,p,T); A = the J^-1-scaled
+// metric row of the sweep direction; Ah = A/|A| (precomputed as A*(1/|A|), split.jl:28-32);
+// ss = |A|; c = sound speed (precomputed: sqrt(gamma Rg T) for SW, split.jl:22;
+// sqrt(gamma p/rho) for LF/VL/AUSM, split.jl:90,130,205).
+template <class R>
+__device__ __forceinline__ void split_cell(int method, R g, const R q[6], R c, R A1, R A2, R A3, R Ah1, R Ah2,
+                                           R Ah3, R ss, R fp[5], R fm[5]) {
+    const R rho = q[0], u = q[1], v = q[2], w = q[3], p = q[4];
+    const R half = R(0.5), one = R(1), two = R(2);
+    if (method == F3D_SPLIT_SW) {  // split.jl:2-68
+        R E1 = A1 * u + A2 * v + A3 * w;
+        R E2 = E1 - c * ss;
+        R E3 = E1 + c * ss;
+        R E1P = (E1 + fabs(E1)) * half, E2P = (E2 + fabs(E2)) * half, E3P = (E3 + fabs(E3)) * half;
+        R E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
+        R uc1 = u - c * Ah1, uc2 = u + c * Ah1;
+        R vc1 = v - c * Ah2, vc2 = v + c * Ah2;
+        R wc1 = w - c * Ah3, wc2 = w + c * Ah3;
+        R vvc1 = (uc1 * uc1 + vc1 * vc1 + wc1 * wc1) * half;
+        R vvc2 = (uc2 * uc2 + vc2 * vc2 + wc2 * wc2) * half;
+        R gm1 = g - one;
+        R vv = gm1 * (u * u + v * v + w * w);
+        R W2 = (R(3) - g) / (two * gm1) * (c * c);
+        R t1 = rho / (two * g);
+        R t2 = two * gm1;
+        R a1 = t2 * E1P, b1 = t2 * E1M;
+        fp[0] = t1 * (a1 + E2P + E3P);
+        fp[1] = t1 * (a1 * u + E2P * uc1 + E3P * uc2);
+        fp[2] = t1 * (a1 * v + E2P * vc1 + E3P * vc2);
+        fp[3] = t1 * (a1 * w + E2P * wc1 + E3P * wc2);
+        fp[4] = t1 * (E1P * vv + E2P * vvc1 + E3P * vvc2 + W2 * (E2P + E3P));
+        fm[0] = t1 * (b1 + E2M + E3M);
+        fm[1] = t1 * (b1 * u + E2M * uc1 + E3M * uc2);
+        fm[2] = t1 * (b1 * v + E2M * vc1 + E3M * vc2);
+        fm[3] = t1 * (b1 * w + E2M * wc1 + E3M * wc2);
+        fm[4] = t1 * (E1M * vv + E2M * vvc1 + E3M * vvc2 + W2 * (E2M + E3M));
+    } else if (method == F3D_SPLIT_LF) {  // split.jl:70-108
+        R un = A1 * u + A2 * v + A3 * w;
+        R l0 = fabs(un) + c * ss;
+        R E0 = p / (g - one) + half * rho * (u * u + v * v + w * w);
+        R ru = rho * u, rv = rho * v, rw = rho * w;
+        fp[0] = half * (rho * un + l0 * rho);
+        fp[1] = half * (ru * un + A1 * p + l0 * ru);
+        fp[2] = half * (rv * un + A2 * p + l0 * rv);
+        fp[3] = half * (rw * un + A3 * p + l0 * rw);
+        fp[4] = half * ((E0 + p) * un + l0 * E0);
+        fm[0] = half * (rho * un - l0 * rho);
+        fm[1] = half * (ru * un + A1 * p - l0 * ru);
+        fm[2] = half * (rv * un + A2 * p - l0 * rv);
+        fm[3] = half * (rw * un + A3 * p - l0 * rw);
+        fm[4] = half * ((E0 + p) * un - l0 * E0);
+    } else {  // VL split.jl:110-183, AUSM split.jl:185-255
+        R un = A1 * u + A2 * v + A3 * w;
+        R M = un / (c * ss);
+        R kin = u * u + v * v + w * w;
+        R f4;  // energy flux coefficient of the supersonic state
+        R h = R(0);
+        if (method == F3D_SPLIT_VL) {
+            R E0 = p / (g - one) + half * rho * kin;
+            f4 = (E0 + p) * un;
+        } else {
+            h = g * p / (rho * (g - one)) + half * kin;
+            f4 = rho * h * un;
+        }
+        if (M <= R(-1) || M >= R(1)) {
+            R full[5] = {rho * un, rho * u * un + A1 * p, rho * v * un + A2 * p, rho * w * un + A3 * p, f4};
+            const bool neg = M <= R(-1);
+            for (int n = 0; n < 5; n++) {
+                fp[n] = neg ? R(0) : full[n];
+                fm[n] = neg ? full[n] : R(0);
+            }
+        } else if (method == F3D_SPLIT_VL) {
+            R unn = un / ss;
+            R f1p = rho * c * R(0.25) * sq(M + one) * ss;
+            R f1m = -rho * c * R(0.25) * sq(M - one) * ss;
+            R t1 = (-unn + two * c) / (g * ss);
+            R t2 = (-unn - two * c) / (g * ss);
+            R t3 = one / (two * (g * g - one));
+            R t4 = half * (kin - unn * unn);
+            fp[0] = f1p;
+            fp[1] = f1p * (A1 * t1 + u);
+            fp[2] = f1p * (A2 * t1 + v);
+            fp[3] = f1p * (A3 * t1 + w);
+            fp[4] = f1p * (sq((g - one) * unn + two * c) * t3 + t4);
+            fm[0] = f1m;
+            fm[1] = f1m * (A1 * t2 + u);
+            fm[2] = f1m * (A2 * t2 + v);
+            fm[3] = f1m * (A3 * t2 + w);
+            fm[4] = f1m * (sq((g - one) * unn - two * c) * t3 + t4);
+        } else {
+            R f_p = R(0.25) * sq(M + one) * rho * c * ss;
+            R f_m = -R(0.25) * sq(M - one) * rho * c * ss;
+            R Pp = p * (R(0.25) * sq(M + one) * (two - M));
+            R Pm = p * (R(0.25) * sq(M - one) * (two + M));
+            fp[0] = f_p;
+            fp[1] = f_p * u + A1 * Pp;
+            fp[2] = f_p * v + A2 * Pp;
+            fp[3] = f_p * w + A3 * Pp;
+            fp[4] = f_p * h;
+            fm[0] = f_m;
+            fm[1] = f_m * u + A1 * Pm;
+            fm[2] = f_m * v + A2 * Pm;
+            fm[3] = f_m * w + A3 * Pm;
+            fm[4] = f_m * h;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Nonlinear weights. The reference normalises alpha_k = d_k / b_k, b_k = (eps + IS_k s)^2
+// with one division per alpha plus one for the sum (schemes.jl:178-185, 243-252). The
+// combine functions take the bases t_k = eps + IS_k s.
+// FP64 form: multiply numerator and denominator by prod_k b_k, leaving ONE division per
+// stencil side; with b_k in [eps^2, ~1e40] the products stay far inside the FP64 range.
+// FP32 form: scale by the smallest base, r_k = min_j t_j / t_k in (0,1], alpha_k = d_k r_k^2,
+// so every scaled alpha lies in [0, d_k] and the sum in [d_min, sum d_k]. This keeps the
+// eps = 1e-20 of WENO7 usable in FP32, where 1/(1e-20)^2 overflows (the reason the
+// reference promotes these alphas to FP64), and never forms a subnormal.
+
+__device__ __forceinline__ double weno5_combine(double t1, double t2, double t3, double v1, double v2, double v3) {
+    double b1 = t1 * t1, b2 = t2 * t2, b3 = t3 * t3;
+    double a1 = b2 * b3, a2 = 6.0 * b1 * b3, a3 = 3.0 * b1 * b2;
+    return (a1 * v1 + a2 * v2 + a3 * v3) / (a1 + a2 + a3);
+}
+__device__ __forceinline__ float weno5_combine(float t1, float t2, float t3, float v1, float v2, float v3) {
+    float m = fminf(t1, fminf(t2, t3));
+    float r1 = m / t1, r2 = m / t2, r3 = m / t3;
+    float a1 = r1 * r1, a2 = 6.f * r2 * r2, a3 = 3.f * r3 * r3;
+    return (a1 * v1 + a2 * v2 + a3 * v3) / (a1 + a2 + a3);
+}
+__device__ __forceinline__ double weno7_combine(double t1, double t2, double t3, double t4, double q1, double q2,
+                                                double q3, double q4) {
+    double b1 = t1 * t1, b2 = t2 * t2, b3 = t3 * t3, b4 = t4 * t4;
+    double p12 = b1 * b2, p34 = b3 * b4;
+    double a1 = b2 * p34, a2 = 12.0 * b1 * p34, a3 = 18.0 * p12 * b4, a4 = 4.0 * p12 * b3;
+    return (a1 * q1 + a2 * q2 + a3 * q3 + a4 * q4) / (a1 + a2 + a3 + a4);
+}
+__device__ __forceinline__ float weno7_combine(float t1, float t2, float t3, float t4, float q1, float q2, float q3,
+                                               float q4) {
+    float m = fminf(fminf(t1, t2), fminf(t3, t4));
+    float r1 = m / t1, r2 = m / t2, r3 = m / t3, r4 = m / t4;
+    float a1 = r1 * r1, a2 = 12.f * r2 * r2, a3 = 18.f * r3 * r3, a4 = 4.f * r4 * r4;
+    return (a1 * q1 + a2 * q2 + a3 * q3 + a4 * q4) / (a1 + a2 + a3 + a4);
+}
+
+// WENO5 of one side, schemes.jl:233-252: 6x the reconstructed value. V in upwind order.
+template <class R> __device__ __forceinline__ R weno5(R V1, R V2, R V3, R V4, R V5, R s0) {
+    const R e2 = R(1e-16);
+    R s11 = R(13) * sq(V1 - R(2) * V2 + V3) + R(3) * sq(V1 - R(4) * V2 + R(3) * V3);
+    R s22 = R(13) * sq(V2 - R(2) * V3 + V4) + R(3) * sq(V2 - V4);
+    R s33 = R(13) * sq(V3 - R(2) * V4 + V5) + R(3) * sq(R(3) * V3 - R(4) * V4 + V5);
+    R t1 = e2 + s11 * s0, t2 = e2 + s22 * s0, t3 = e2 + s33 * s0;
+    R v1 = R(2) * V1 - R(7) * V2 + R(11) * V3;
+    R v2 = -V2 + R(5) * V3 + R(2) * V4;
+    R v3 = R(2) * V3 + R(5) * V4 - V5;
+    return weno5_combine(t1, t2, t3, v1, v2, v3);
+}
+
+// WENO7 of one side, schemes.jl:153-185: 12x the reconstructed value.
+template <class R> __device__ __forceinline__ R weno7(R V1, R V2, R V3, R V4, R V5, R V6, R V7, R s0) {
+    R q1 = R(-3) * V1 + R(13) * V2 - R(23) * V3 + R(25) * V4;
+    R q2 = V2 - R(5) * V3 + R(13) * V4 + R(3) * V5;
+    R q3 = -V3 + R(7) * V4 + R(7) * V5 - V6;
+    R q4 = R(3) * V4 + R(13) * V5 - R(5) * V6 + V7;
+    R Is1 = V1 * (R(547) * V1 - R(3882) * V2 + R(4642) * V3 - R(1854) * V4) +
+            V2 * (R(7043) * V2 - R(17246) * V3 + R(7042) * V4) + V3 * (R(11003) * V3 - R(9402) * V4) +
+            V4 * (R(2107) * V4);
+    R Is2 = V2 * (R(267) * V2 - R(1642) * V3 + R(1602) * V4 - R(494) * V5) +
+            V3 * (R(2843) * V3 - R(5966) * V4 + R(1922) * V5) + V4 * (R(3443) * V4 - R(2522) * V5) +
+            V5 * (R(547) * V5);
+    R Is3 = V3 * (R(547) * V3 - R(2522) * V4 + R(1922) * V5 - R(494) * V6) +
+            V4 * (R(3443) * V4 - R(5966) * V5 + R(1602) * V6) + V5 * (R(2843) * V5 - R(1642) * V6) +
+            V6 * (R(267) * V6);
+    R Is4 = V4 * (R(2107) * V4 - R(9402) * V5 + R(7042) * V6 - R(1854) * V7) +
+            V5 * (R(11003) * V5 - R(17246) * V6 + R(4642) * V7) + V6 * (R(7043) * V6 - R(3882) * V7) +
+            V7 * (R(547) * V7);
+    const R e1 = R(1e-20);
+    return weno7_combine(e1 + Is1 * s0, e1 + Is2 * s0, e1 + Is3 * s0, e1 + Is4 * s0, q1, q2, q3, q4);
+}
+
+}  // namespace f3d

@@ -1,0 +1,69 @@
+// f3d_kernels.cuh — launch interfaces between the C-ABI layer (api.cu) and the kernels.
+#pragma once
+#include "f3d_common.cuh"
+#include "f3d_flux.cuh"
+
+namespace f3d {
+
+constexpr int SWEEP_THREADS = 256;
+
+enum OutMode { OUT_SET = 0, OUT_ADD = 1, OUT_RHS = 2, OUT_STAGE = 3, OUT_FACES = 4 };
+
+struct SweepArgs {
+    DevParams P;
+    const double* Q;      // primitive state (Nt^3 x 6), ghost-filled
+    const double* csnd;   // sound speed per cell for the split
+    const double* A[3];   // metric row of the sweep direction (J^-1 scaled)
+    const double* Ah[3];  // A * (1/|A|)
+    const double* S;      // |A|
+    const double* phi;    // shock sensor (only read when P.fixed_branch < 0)
+    const double* Fv;     // viscous flux of this direction ((Nt-4)^3 x 4) or null
+    const double* J;      // Jacobian
+    double* acc;          // RHS accumulator (U layout)
+    double* out;          // OUT_RHS destination (may alias acc)
+    double* U;            // OUT_STAGE state, updated in place
+    double* Un;           // OUT_STAGE stage-start copy
+    double* faces;        // OUT_FACES destination (Fx/Fy/Fz shape) or null
+    double dt, ca, cb;    // OUT_STAGE: U = ca*(U + dt J acc) + cb*Un when combine
+    int out_mode;
+    int combine;
+    int stage1_copy;      // OUT_STAGE of stage 1: Un = U before the update
+};
+
+cudaError_t sweep_configure();
+cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st);
+
+// pointwise / stencil kernels (k_pointwise.cu)
+// Q at every cell from the interior of U (c2Prim) or of Q itself (from_q), with the
+// ghost layers produced by the composed boundary rules. U ghosts are written when
+// U_ghost_out is not null. csnd (optional) receives the split's sound speed.
+cudaError_t launch_prim_fill(const DevParams& P, const double* U, double* Q, double* U_ghost_out, double* csnd,
+                             int from_q, cudaStream_t st);
+cudaError_t launch_c2prim_interior(const DevParams& P, const double* U, double* Q, cudaStream_t st);
+cudaError_t launch_prim2c(const DevParams& P, const double* Q, double* U, cudaStream_t st);
+cudaError_t launch_lincomb(const DevParams& P, double* U, const double* Un, double a, double b, cudaStream_t st);
+cudaError_t launch_sound(const DevParams& P, const double* Q, double* csnd, cudaStream_t st);
+cudaError_t launch_sensor(const DevParams& P, const double* Q, double* phi, cudaStream_t st);
+cudaError_t launch_metric_prep(const DevParams& P, const double* const m[9], double* S[3], double* Ah[9],
+                               cudaStream_t st);
+cudaError_t launch_split_debug(const DevParams& P, const double* Q, const double* csnd, const double* const A[3],
+                               const double* const Ah[3], const double* S, double* Fp, double* Fm, cudaStream_t st);
+cudaError_t launch_div_ref(const DevParams& P, double* U, const double* Fx, const double* Fy, const double* Fz,
+                           const double* Fvx, const double* Fvy, const double* Fvz, const double* J, double dt,
+                           cudaStream_t st);
+cudaError_t launch_check_finite(const DevParams& P, const double* U, int* flag, cudaStream_t st);
+cudaError_t launch_cfl(const DevParams& P, const double* Q, const double* const m[9], const double* J, double cfl,
+                       unsigned long long* dtbits, cudaStream_t st);
+
+// viscous fluxes (k_viscous.cu)
+cudaError_t launch_viscous(const DevParams& P, const double* Q, const double* const m[9], const double* J,
+                           double* Fvx, double* Fvy, double* Fvz, cudaStream_t st);
+
+// metrics from coordinates (k_metrics.cu)
+cudaError_t launch_metrics(const DevParams& P, const double* x, const double* y, const double* z,
+                           double* const m[9], double* J, cudaStream_t st);
+
+// pipe throughput probe (k_pointwise.cu)
+cudaError_t measure_pipes(double* fp64_tflops, double* fp32_tflops);
+
+}  // namespace f3d

@@ -1,0 +1,325 @@
+// k_sweep.cu — one direction of the inviscid RHS (plus that direction's viscous
+// divergence) as a tiled sweep.
+//
+// A block owns TL grid lines along the sweep direction d and TC consecutive interior
+// cells of each. Phase A splits the TC+8 cells the tile's stencils touch into Fp/Fm in
+// shared memory (fluxSplit_*, split.jl), once per cell. Phase B reconstructs the TC+1
+// faces of the tile, one thread per face, choosing UP7 / WENO7 / WENO5 / NND2 per face
+// from the shock sensor (advect_x/xc and their y, z permutations, schemes.jl:86-1643).
+// Phase C differences the face fluxes into the cells, adds the 4th-order central
+// divergence of the viscous flux of direction d (div.jl:14-39), and accumulates into the
+// RHS, or (last sweep) applies the Euler update and SSP-RK3 combination
+// (div.jl:40-48, utils.jl:57-70) in place.
+//
+// Shared-memory layout is [var][line][pos] for d = x (threads run along the line) and
+// [var][pos][line] for d = y, z (threads run across x-adjacent lines), so global loads
+// coalesce along i and shared loads are conflict-free in both cases.
+#include "f3d_kernels.cuh"
+
+namespace f3d {
+
+template <int DIR> struct Tile;
+template <> struct Tile<0> { static constexpr int TL = 8, TC = 64; };
+template <> struct Tile<1> { static constexpr int TL = 16, TC = 32; };
+template <> struct Tile<2> { static constexpr int TL = 16, TC = 32; };
+
+template <int DIR, class R> constexpr size_t sweep_smem_bytes(bool hybrid) {
+    return sizeof(R) * ((size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 8) * (10 + (hybrid ? 1 : 0)) +
+                        (size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 1) * 5);
+}
+
+// Face flux of one face from the split fluxes of the 8 cells around it, positions
+// p0..p0+7 of the line (face between positions p0+3 and p0+4). FP/FM(n, pos) read shared
+// memory. For characteristic mode the face state comes from global memory at the two
+// adjacent cells (cl, cr linear indices).
+template <bool CHAR, class R, class FPA, class FMA>
+__device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a, int br, int p0, R s0,
+                                          long long cl, long long cr, FPA FP, FMA FM, R out[5]) {
+    if (br == 0) {  // UP7, schemes.jl:119-142
+        const R c1 = R(P.lin[0]), c2 = R(P.lin[1]), c3 = R(P.lin[2]), c4 = R(P.lin[3]), c5 = R(P.lin[4]),
+                c6 = R(P.lin[5]), c7 = R(P.lin[6]);
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            R fp = c1 * FP(n, p0) + c2 * FP(n, p0 + 1) + c3 * FP(n, p0 + 2) + c4 * FP(n, p0 + 3) +
+                   c5 * FP(n, p0 + 4) + c6 * FP(n, p0 + 5) + c7 * FP(n, p0 + 6);
+            R fm = c1 * FM(n, p0 + 7) + c2 * FM(n, p0 + 6) + c3 * FM(n, p0 + 5) + c4 * FM(n, p0 + 4) +
+                   c5 * FM(n, p0 + 3) + c6 * FM(n, p0 + 2) + c7 * FM(n, p0 + 1);
+            out[n] = fp + fm;
+        }
+        return;
+    }
+    if (br == 3) {  // NND2, schemes.jl:277-286 (component-wise in both modes)
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            R fp = FP(n, p0 + 3) + R(0.5) * minmod(FP(n, p0 + 4) - FP(n, p0 + 3), FP(n, p0 + 3) - FP(n, p0 + 2));
+            R fm = FM(n, p0 + 4) - R(0.5) * minmod(FM(n, p0 + 5) - FM(n, p0 + 4), FM(n, p0 + 4) - FM(n, p0 + 3));
+            out[n] = fp + fm;
+        }
+        return;
+    }
+    const R tmp1 = R(1) / R(12), tmp2 = R(1) / R(6);
+    if (!CHAR) {  // component-wise WENO7 (schemes.jl:143-230) / WENO5 (:231-276)
+#pragma unroll 1
+        for (int n = 0; n < 5; n++) {
+            if (br == 1) {
+                R fp = weno7(FP(n, p0), FP(n, p0 + 1), FP(n, p0 + 2), FP(n, p0 + 3), FP(n, p0 + 4), FP(n, p0 + 5),
+                             FP(n, p0 + 6), s0);
+                R fm = weno7(FM(n, p0 + 7), FM(n, p0 + 6), FM(n, p0 + 5), FM(n, p0 + 4), FM(n, p0 + 3),
+                             FM(n, p0 + 2), FM(n, p0 + 1), s0);
+                out[n] = (fp + fm) * tmp1;
+            } else {
+                R fp = weno5(FP(n, p0 + 1), FP(n, p0 + 2), FP(n, p0 + 3), FP(n, p0 + 4), FP(n, p0 + 5), s0);
+                R fm = weno5(FM(n, p0 + 6), FM(n, p0 + 5), FM(n, p0 + 4), FM(n, p0 + 3), FM(n, p0 + 2), s0);
+                out[n] = (fp + fm) * tmp2;
+            }
+        }
+        return;
+    }
+    // characteristic-wise, schemes.jl:756-999: eigenvectors of the face from the arithmetic
+    // mean of u,v,w,T and of the metric row at the two adjacent cells.
+    const long long pl = P.plane;
+    const R u = R(0.5) * (R(a.Q[cr + pl]) + R(a.Q[cl + pl]));
+    const R v = R(0.5) * (R(a.Q[cr + 2 * pl]) + R(a.Q[cl + 2 * pl]));
+    const R w = R(0.5) * (R(a.Q[cr + 3 * pl]) + R(a.Q[cl + 3 * pl]));
+    const R T = R(0.5) * (R(a.Q[cr + 5 * pl]) + R(a.Q[cl + 5 * pl]));
+    const R A1 = (R(a.A[0][cr]) + R(a.A[0][cl])) * R(0.5);
+    const R A2 = (R(a.A[1][cr]) + R(a.A[1][cl])) * R(0.5);
+    const R A3 = (R(a.A[2][cr]) + R(a.A[2][cl])) * R(0.5);
+    const R nx = A1 * s0, ny = A2 * s0, nz = A3 * s0;
+    R lx, ly, lz;
+    if (fabs(nz) <= fabs(ny)) {
+        R ss = rsqrt(nx * nx + ny * ny);
+        lx = -ny * ss;
+        ly = nx * ss;
+        lz = R(0);
+    } else {
+        R ss = rsqrt(nx * nx + nz * nz);
+        lx = -nz * ss;
+        ly = R(0);
+        lz = nx * ss;
+    }
+    const R mx = ny * lz - nz * ly, my = nz * lx - nx * lz, mz = nx * ly - ny * lx;
+    const R qn = u * nx + v * ny + w * nz;
+    const R ql = u * lx + v * ly + w * lz;
+    const R qm = u * mx + v * my + w * mz;
+    const R q2 = R(0.5) * (u * u + v * v + w * w);
+    const R gT = R(P.grg) * T;
+    const R rc = rsqrt(gT);         // 1/c
+    const R c = gT * rc;            // c = sqrt(gamma Rg T)
+    const R c2 = R(0.5) * rc;       // 1/(2c)
+    const R K = R(P.gm1) * (rc * rc);  // (gamma-1)/c^2
+    const R K2 = K * R(0.5);
+    const R H = gT / R(P.gm1) + q2;    // 1/K + q2
+    R flux[5];
+#pragma unroll 1
+    for (int n = 0; n < 5; n++) {
+        R l0, l1, l2, l3, l4;  // row n of L
+        if (n == 0) { l0 = K2 * q2 + qn * c2; l1 = -(K2 * u + nx * c2); l2 = -(K2 * v + ny * c2); l3 = -(K2 * w + nz * c2); l4 = K2; }
+        else if (n == 1) { l0 = R(1) - K * q2; l1 = K * u; l2 = K * v; l3 = K * w; l4 = -K; }
+        else if (n == 2) { l0 = K2 * q2 - qn * c2; l1 = -(K2 * u - nx * c2); l2 = -(K2 * v - ny * c2); l3 = -(K2 * w - nz * c2); l4 = K2; }
+        else if (n == 3) { l0 = -ql; l1 = lx; l2 = ly; l3 = lz; l4 = R(0); }
+        else { l0 = -qm; l1 = mx; l2 = my; l3 = mz; l4 = R(0); }
+        auto projP = [&](int pos) {
+            return FP(0, pos) * l0 + FP(1, pos) * l1 + FP(2, pos) * l2 + FP(3, pos) * l3 + FP(4, pos) * l4;
+        };
+        auto projM = [&](int pos) {
+            return FM(0, pos) * l0 + FM(1, pos) * l1 + FM(2, pos) * l2 + FM(3, pos) * l3 + FM(4, pos) * l4;
+        };
+        if (br == 1) {
+            R fp = weno7(projP(p0), projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5),
+                         projP(p0 + 6), s0);
+            R fm = weno7(projM(p0 + 7), projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3), projM(p0 + 2),
+                         projM(p0 + 1), s0);
+            flux[n] = (fp + fm) * tmp1;
+        } else {
+            R fp = weno5(projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5), s0);
+            R fm = weno5(projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3), projM(p0 + 2), s0);
+            flux[n] = (fp + fm) * tmp2;
+        }
+    }
+    out[0] = flux[0] + flux[1] + flux[2];
+    out[1] = flux[0] * (u - c * nx) + flux[1] * u + flux[2] * (u + c * nx) + flux[3] * lx + flux[4] * mx;
+    out[2] = flux[0] * (v - c * ny) + flux[1] * v + flux[2] * (v + c * ny) + flux[3] * ly + flux[4] * my;
+    out[3] = flux[0] * (w - c * nz) + flux[1] * w + flux[2] * (w + c * nz) + flux[3] * lz + flux[4] * mz;
+    out[4] = flux[0] * (H - qn * c) + flux[1] * q2 + flux[2] * (H + qn * c) + flux[3] * ql + flux[4] * qm;
+}
+
+template <int DIR, bool CHAR>
+__global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
+    using R = double;
+    constexpr int TL = Tile<DIR>::TL, TC = Tile<DIR>::TC, NP = TC + 8, NF = TC + 1;
+    const DevParams& P = a.P;
+    const bool hybrid = P.fixed_branch < 0;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sFp = reinterpret_cast<R*>(smem_raw);
+    R* sFm = sFp + 5 * TL * NP;
+    R* sF = sFm + 5 * TL * NP;
+    R* sPhi = sF + 5 * TL * NF;
+
+    // tile geometry: interior start c0 along d, first line l0 and line count
+    const int Nd = DIR == 0 ? P.nx : (DIR == 1 ? P.ny : P.nz);
+    const int Nl = DIR == 0 ? P.ny : P.nx;
+    int c0, l0, other;
+    if (DIR == 0) { c0 = blockIdx.x * TC; l0 = blockIdx.y * TL; other = blockIdx.z; }
+    else { l0 = blockIdx.x * TL; c0 = blockIdx.y * TC; other = blockIdx.z; }
+    const int nc = min(TC, Nd - c0);
+    const int nl = min(TL, Nl - l0);
+    const long long stride = DIR == 0 ? 1 : (DIR == 1 ? (long long)P.nxt : (long long)P.nxt * P.nyt);
+    // linear index of (line l, full position along d = g)
+    auto cell = [&](int l, int g) -> long long {
+        if (DIR == 0) return lin3(P, g, l0 + l + NG, other + NG);
+        if (DIR == 1) return lin3(P, l0 + l + NG, g, other + NG);
+        return lin3(P, l0 + l + NG, other + NG, g);
+    };
+    auto sidx = [&](int l, int p) { return DIR == 0 ? l * NP + p : p * TL + l; };
+    auto fidx = [&](int l, int t) { return DIR == 0 ? l * NF + t : t * TL + l; };
+    const long long pl = P.plane;
+
+    // ---- Phase A: split every cell the tile's stencils reach (positions 0..nc+7, full
+    // index c0 + p along d).
+    for (int it = threadIdx.x; it < TL * NP; it += SWEEP_THREADS) {
+        int l, p;
+        if (DIR == 0) { l = it / NP; p = it - l * NP; } else { p = it / TL; l = it - p * TL; }
+        if (l >= nl || p >= nc + 8) continue;
+        const long long c = cell(l, c0 + p);
+        R q[6];
+#pragma unroll
+        for (int n = 0; n < 6; n++) q[n] = a.Q[c + n * pl];
+        R fp[5], fm[5];
+        split_cell<R>(P.split, R(P.gamma), q, a.csnd[c], a.A[0][c], a.A[1][c], a.A[2][c], a.Ah[0][c], a.Ah[1][c],
+                      a.Ah[2][c], a.S[c], fp, fm);
+        const int s = sidx(l, p);
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            sFp[n * TL * NP + s] = fp[n];
+            sFm[n * TL * NP + s] = fm[n];
+        }
+        if (hybrid) sPhi[s] = a.phi[c];
+    }
+    __syncthreads();
+
+    // ---- Phase B: faces t = 0..nc (face t lies between positions t+3 and t+4).
+    for (int it = threadIdx.x; it < TL * NF; it += SWEEP_THREADS) {
+        int l, t;
+        if (DIR == 0) { l = it / NF; t = it - l * NF; } else { t = it / TL; l = it - t * TL; }
+        if (l >= nl || t > nc) continue;
+        int br = P.fixed_branch;
+        if (hybrid) {  // Jameson sensor max over cells i-3..i+2, schemes.jl:112-117
+            R pm = sPhi[sidx(l, t + 1)];
+#pragma unroll
+            for (int o = 2; o <= 6; o++) pm = fmax(pm, sPhi[sidx(l, t + o)]);
+            br = pm < R(P.phi1) ? 0 : (pm < R(P.phi2) ? 1 : (pm < R(P.phi3) ? 2 : 3));
+            if (pm != pm) br = 3;  // NaN fails every comparison in the reference
+        }
+        const long long cl = cell(l, c0 + t + 3), cr = cl + stride;
+        R out[5];
+        R s0 = R(0);
+        if (br == 1 || br == 2) s0 = R(2) / (a.S[cl] + a.S[cr]);
+        auto FP = [&](int n, int p) { return sFp[n * TL * NP + sidx(l, p)]; };
+        auto FM = [&](int n, int p) { return sFm[n * TL * NP + sidx(l, p)]; };
+        face_flux<CHAR, R>(P, a, br, t, s0, cl, cr, FP, FM, out);
+        const int f = fidx(l, t);
+#pragma unroll
+        for (int n = 0; n < 5; n++) sF[n * TL * NF + f] = out[n];
+        if (a.faces) {  // face-flux output in the reference's Fx/Fy/Fz shape
+            const long long fx = P.nx + (DIR == 0), fy = P.ny + (DIR == 1), fz = P.nz + (DIR == 2);
+            long long fi, fj, fk;
+            if (DIR == 0) { fi = c0 + t; fj = l0 + l; fk = other; }
+            else if (DIR == 1) { fi = l0 + l; fj = c0 + t; fk = other; }
+            else { fi = l0 + l; fj = other; fk = c0 + t; }
+            const long long fo = fi + fx * (fj + fy * fk), nf = fx * fy * fz;
+#pragma unroll
+            for (int n = 0; n < 5; n++) a.faces[fo + n * nf] = out[n];
+        }
+    }
+    if (a.out_mode == OUT_FACES) return;
+    __syncthreads();
+
+    // ---- Phase C: cells t = 0..nc-1 (full position c0 + t + NG).
+    const int vxt = P.nxt - 4, vyt = P.nyt - 4, vzt = P.nzt - 4;
+    const long long vplane = (long long)vxt * vyt * vzt;
+    for (int it = threadIdx.x; it < TL * TC; it += SWEEP_THREADS) {
+        int l, t;
+        if (DIR == 0) { l = it / TC; t = it - l * TC; } else { t = it / TL; l = it - t * TL; }
+        if (l >= nl || t >= nc) continue;
+        const long long c = cell(l, c0 + t + NG);
+        R d[5];
+#pragma unroll
+        for (int n = 0; n < 5; n++) d[n] = sF[n * TL * NF + fidx(l, t)] - sF[n * TL * NF + fidx(l, t + 1)];
+        if (a.Fv) {
+            // Fv index = full index - 2 in every dimension (viscous.jl:119, div.jl:14-39)
+            long long vi, vj, vk;
+            const int g = c0 + t + NG - 2;
+            if (DIR == 0) { vi = g; vj = l0 + l + NG - 2; vk = other + NG - 2; }
+            else if (DIR == 1) { vi = l0 + l + NG - 2; vj = g; vk = other + NG - 2; }
+            else { vi = l0 + l + NG - 2; vj = other + NG - 2; vk = g; }
+            const long long vc = vi + (long long)vxt * (vj + (long long)vyt * vk);
+            const long long vs = DIR == 0 ? 1 : (DIR == 1 ? (long long)vxt : (long long)vxt * vyt);
+            const R k1 = R(1) / R(12), k2 = R(-2) / R(3);
+#pragma unroll
+            for (int n = 0; n < 4; n++) {
+                const R* F = a.Fv + n * vplane + vc;
+                d[n + 1] += k1 * (F[-2 * vs] - F[2 * vs]) + k2 * (F[-vs] - F[vs]);
+            }
+        }
+        if (a.out_mode == OUT_SET) {
+#pragma unroll
+            for (int n = 0; n < 5; n++) a.acc[c + n * pl] = d[n];
+        } else if (a.out_mode == OUT_ADD) {
+#pragma unroll
+            for (int n = 0; n < 5; n++) a.acc[c + n * pl] += d[n];
+        } else if (a.out_mode == OUT_RHS) {
+            const R Jc = a.J[c];
+#pragma unroll
+            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * (a.acc[c + n * pl] + d[n]);
+        } else {  // OUT_STAGE
+            const R Jact = a.J[c] * a.dt;
+#pragma unroll
+            for (int n = 0; n < 5; n++) {
+                const R u = a.U[c + n * pl];
+                if (a.stage1_copy) a.Un[c + n * pl] = u;
+                R un = u + (a.acc[c + n * pl] + d[n]) * Jact;
+                if (a.combine) un = un * a.ca + a.Un[c + n * pl] * a.cb;
+                a.U[c + n * pl] = un;
+            }
+        }
+    }
+}
+
+template <int DIR, bool CHAR> static cudaError_t configure_dir() {
+    return cudaFuncSetAttribute(k_sweep<DIR, CHAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sweep_smem_bytes<DIR, double>(true));
+}
+
+// Dynamic shared memory above 48 KB must be enabled per kernel before the first launch
+// (and outside stream capture): called from f3d_create.
+cudaError_t sweep_configure() {
+    cudaError_t e;
+    if ((e = configure_dir<0, false>()) != cudaSuccess) return e;
+    if ((e = configure_dir<0, true>()) != cudaSuccess) return e;
+    if ((e = configure_dir<1, false>()) != cudaSuccess) return e;
+    if ((e = configure_dir<1, true>()) != cudaSuccess) return e;
+    if ((e = configure_dir<2, false>()) != cudaSuccess) return e;
+    return configure_dir<2, true>();
+}
+
+template <int DIR, bool CHAR> static cudaError_t launch_dir(const SweepArgs& a, cudaStream_t st) {
+    constexpr int TL = Tile<DIR>::TL, TC = Tile<DIR>::TC;
+    const DevParams& P = a.P;
+    const size_t smem = sweep_smem_bytes<DIR, double>(true);
+    dim3 grid;
+    if (DIR == 0) grid = dim3(cdiv(P.nx, TC), cdiv(P.ny, TL), P.nz);
+    else if (DIR == 1) grid = dim3(cdiv(P.nx, TL), cdiv(P.ny, TC), P.nz);
+    else grid = dim3(cdiv(P.nx, TL), cdiv(P.nz, TC), P.ny);
+    k_sweep<DIR, CHAR><<<grid, SWEEP_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st) {
+    const bool ch = a.P.character != 0;
+    if (dir == 0) return ch ? launch_dir<0, true>(a, st) : launch_dir<0, false>(a, st);
+    if (dir == 1) return ch ? launch_dir<1, true>(a, st) : launch_dir<1, false>(a, st);
+    return ch ? launch_dir<2, true>(a, st) : launch_dir<2, false>(a, st);
+}
+
+}  // namespace f3d

@@ -1,0 +1,207 @@
+"""Host-side mirror of the reference's finite-difference solver interface over the C ABI.
+
+Method names and argument meaning follow the reference's Julia functions (solver.jl,
+utils.jl, boundary.jl, schemes.jl, div.jl): prim2c(U, Q), c2Prim(U, Q), linComb(U, Un, a, b),
+fillGhost(Q, U) (exchange_ghost + fillGhost), shockSensor(phi, Q), flowAdvance(Q),
+div(U, Fx, Fy, Fz, Fv_x, Fv_y, Fv_z, dt) and the RK3 loop of time_step. Arrays are torch
+float64 CUDA tensors whose memory is the reference's Julia layout: a tensor of shape
+(nvar, Nz+8, Ny+8, Nx+8) in C order is the Julia array (Nx+8, Ny+8, Nz+8, nvar).
+
+PyTorch only provides device memory and the stream here; every computation runs in the
+CUDA kernels of libflame3d_gpu.so, and a missing library or a non-CUDA tensor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import abi
+from .abi import F3DError, F3DParams
+
+NG = 4
+
+
+class Flame3D:
+    """One solver context (f3d_create) for a fixed grid and parameter set."""
+
+    def __init__(self, params: F3DParams, device: int | torch.device | None = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("Flame3D needs a CUDA device; there is no CPU path")
+        self.lib = abi.load()
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else
+                                   torch.device(device).index or 0)
+        self.params = params
+        self.nx, self.ny, self.nz = params.nx, params.ny, params.nz
+        self.shape3 = (self.nz + 2 * NG, self.ny + 2 * NG, self.nx + 2 * NG)
+        self.metrics = None
+        self.J = None
+        with torch.cuda.device(self.device):
+            h = C.c_void_p()
+            rc = self.lib.f3d_create(C.byref(params), C.byref(h))
+            if rc != abi.F3D_OK:
+                raise F3DError(rc, "f3d_create rejected the parameters (see stderr)")
+            self._h = h
+
+    # ---- plumbing -------------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != abi.F3D_OK:
+            raise F3DError(rc, self.lib.f3d_last_error(self._h).decode())
+
+    def _stream(self) -> C.c_void_p:
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _ptr(self, t: torch.Tensor | None, nvar: int | None = None) -> C.c_void_p | None:
+        if t is None:
+            return None
+        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+            raise TypeError("arrays must be contiguous float64 CUDA tensors")
+        if nvar is not None and tuple(t.shape) != (nvar, *self.shape3) and not (
+                nvar == 1 and tuple(t.shape) == self.shape3):
+            raise ValueError(f"expected shape {(nvar, *self.shape3)}, got {tuple(t.shape)}")
+        return C.c_void_p(t.data_ptr())
+
+    def field(self, nvar: int) -> torch.Tensor:
+        """Zero-initialised array in the reference layout with nvar variables."""
+        shape = self.shape3 if nvar == 1 else (nvar, *self.shape3)
+        return torch.zeros(shape, dtype=torch.float64, device=self.device)
+
+    def face_field(self, d: int) -> torch.Tensor:
+        """Zero array shaped like the reference's Fx / Fy / Fz (solver.jl:298-300)."""
+        n = [self.nz, self.ny, self.nx]
+        n[2 - d] += 1
+        return torch.zeros((5, *n), dtype=torch.float64, device=self.device)
+
+    def viscous_field(self) -> torch.Tensor:
+        """Zero array shaped like Fv_x / Fv_y / Fv_z (solver.jl:301-303)."""
+        return torch.zeros((4, self.nz + NG, self.ny + NG, self.nx + NG), dtype=torch.float64, device=self.device)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.f3d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def scratch_bytes(self) -> int:
+        b = C.c_size_t()
+        self._check(self.lib.f3d_scratch_bytes(self._h, C.byref(b)))
+        return b.value
+
+    # ---- geometry ---------------------------------------------------------------------
+    def set_metrics(self, metrics: list[torch.Tensor], J: torch.Tensor):
+        """Nine J^-1-scaled metrics in metrics.h5 order and J (solver.jl:238-288)."""
+        if len(metrics) != 9:
+            raise ValueError("need nine metric arrays")
+        arr = (C.c_void_p * 9)(*[self._ptr(m, 1) for m in metrics])
+        self._check(self.lib.f3d_set_metrics(self._h, arr, self._ptr(J, 1), self._stream()))
+        self.metrics, self.J = list(metrics), J  # keep the borrowed arrays alive
+
+    def compute_metrics(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor):
+        """Metrics and J from coordinates on the device (parse_mesh.jl:139-248)."""
+        ms = [self.field(1) for _ in range(9)]
+        J = self.field(1)
+        arr = (C.c_void_p * 9)(*[self._ptr(m, 1) for m in ms])
+        self._check(self.lib.f3d_compute_metrics(self._h, self._ptr(x, 1), self._ptr(y, 1), self._ptr(z, 1), arr,
+                                                 self._ptr(J, 1), self._stream()))
+        return ms, J
+
+    # ---- utils.jl / boundary.jl ----------------------------------------------------------
+    def prim2c(self, U: torch.Tensor, Q: torch.Tensor):
+        self._check(self.lib.f3d_prim2c(self._h, self._ptr(Q, 6), self._ptr(U, 5), self._stream()))
+
+    def c2Prim(self, U: torch.Tensor, Q: torch.Tensor):
+        self._check(self.lib.f3d_c2prim(self._h, self._ptr(U, 5), self._ptr(Q, 6), self._stream()))
+
+    def linComb(self, U: torch.Tensor, Un: torch.Tensor, a: float, b: float):
+        self._check(self.lib.f3d_lincomb(self._h, self._ptr(U, 5), self._ptr(Un, 5), a, b, self._stream()))
+
+    def fillGhost(self, Q: torch.Tensor, U: torch.Tensor):
+        """exchange_ghost (periodic, one GPU) followed by fillGhost for Q and U."""
+        self._check(self.lib.f3d_fill_ghosts(self._h, self._ptr(Q, 6), self._ptr(U, 5), self._stream()))
+
+    # ---- schemes.jl / split.jl / viscous.jl / div.jl --------------------------------------
+    def shockSensor(self, phi: torch.Tensor, Q: torch.Tensor):
+        self._check(self.lib.f3d_debug_sensor(self._h, self._ptr(Q, 6), self._ptr(phi, 1), self._stream()))
+
+    def fluxSplit(self, d: int, Q: torch.Tensor, Fp: torch.Tensor, Fm: torch.Tensor):
+        self._check(self.lib.f3d_debug_split(self._h, d, self._ptr(Q, 6), self._ptr(Fp, 5), self._ptr(Fm, 5),
+                                             self._stream()))
+
+    def advect(self, d: int, F: torch.Tensor, phi: torch.Tensor | None, Q: torch.Tensor):
+        """Face flux of direction d in the shape of Fx/Fy/Fz (advect_x/xc ... advect_z/zc)."""
+        self._check(self.lib.f3d_debug_face_flux(self._h, d, self._ptr(Q, 6), self._ptr(phi, 1), self._ptr(F),
+                                                 self._stream()))
+
+    def viscousFlux(self, Fv_x: torch.Tensor, Fv_y: torch.Tensor, Fv_z: torch.Tensor, Q: torch.Tensor):
+        self._check(self.lib.f3d_debug_viscous(self._h, self._ptr(Q, 6), self._ptr(Fv_x), self._ptr(Fv_y),
+                                               self._ptr(Fv_z), self._stream()))
+
+    def flowAdvance(self, Q: torch.Tensor, phi: torch.Tensor | None = None):
+        """Face and viscous fluxes of one stage (solver.jl:133-188): (Fx, Fy, Fz, Fv_x, Fv_y, Fv_z)."""
+        if phi is None:
+            phi = self.field(1)
+            self.shockSensor(phi, Q)
+        F = [self.face_field(d) for d in range(3)]
+        for d in range(3):
+            self.advect(d, F[d], phi, Q)
+        Fv = [self.viscous_field() for _ in range(3)] if self.params.viscous else [None] * 3
+        if self.params.viscous:
+            self.viscousFlux(*Fv, Q)
+        return (*F, *Fv)
+
+    def div(self, U, Fx, Fy, Fz, Fv_x, Fv_y, Fv_z, dt: float):
+        self._check(self.lib.f3d_div(self._h, self._ptr(U, 5), self._ptr(Fx), self._ptr(Fy), self._ptr(Fz),
+                                     self._ptr(Fv_x), self._ptr(Fv_y), self._ptr(Fv_z), dt, self._stream()))
+
+    # ---- fused paths ----------------------------------------------------------------
+    def rhs(self, Q: torch.Tensor, dUdt: torch.Tensor | None = None) -> torch.Tensor:
+        """L(U) at interior cells from a ghost-filled Q (fused sensor/split/reconstruction/divergence)."""
+        if dUdt is None:
+            dUdt = self.field(5)
+        self._check(self.lib.f3d_rhs(self._h, self._ptr(Q, 6), self._ptr(dUdt, 5), self._stream()))
+        return dUdt
+
+    def rk3_stage(self, stage: int, dt: float, U, Un, Q):
+        self._check(self.lib.f3d_rk3_stage(self._h, stage, dt, self._ptr(U, 5), self._ptr(Un, 5), self._ptr(Q, 6),
+                                           self._stream()))
+
+    def time_step(self, U, Un, Q, dt: float, nsteps: int):
+        """nsteps SSP-RK3 steps (the hot loop of solver.jl:410-444)."""
+        self._check(self.lib.f3d_rk3_steps(self._h, nsteps, dt, self._ptr(U, 5), self._ptr(Un, 5),
+                                           self._ptr(Q, 6), self._stream()))
+
+    def profile_step(self, U, Un, Q, dt: float) -> dict:
+        """One RK3 step with per-launch CUDA events: {kernel name: (ms, launches)}."""
+        n = self.lib.f3d_kernel_count()
+        ms = (C.c_double * n)()
+        cnt = (C.c_int * n)()
+        self._check(self.lib.f3d_profile_step(self._h, dt, self._ptr(U, 5), self._ptr(Un, 5), self._ptr(Q, 6),
+                                              self._stream(), ms, cnt))
+        return {self.lib.f3d_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n) if cnt[k]}
+
+    def cfl_dt(self, Q: torch.Tensor, cfl: float) -> float:
+        out = C.c_double()
+        self._check(self.lib.f3d_cfl_dt(self._h, self._ptr(Q, 6), cfl, C.byref(out), self._stream()))
+        return out.value
+
+    def check_finite(self, U: torch.Tensor) -> bool:
+        rc = self.lib.f3d_check_finite(self._h, self._ptr(U, 5), self._stream())
+        if rc == abi.F3D_ERR_NONFINITE:
+            return False
+        self._check(rc)
+        return True
+
+
+def measure_pipes() -> tuple[float, float]:
+    """(FP64, FP32) FMA throughput of the current device in TFLOP/s."""
+    lib = abi.load()
+    a, b = C.c_double(), C.c_double()
+    rc = lib.f3d_measure_pipes(C.byref(a), C.byref(b))
+    if rc != abi.F3D_OK:
+        raise F3DError(rc, "f3d_measure_pipes failed")
+    return a.value, b.value

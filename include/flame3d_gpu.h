@@ -1,0 +1,207 @@
+/*
+ * flame3d_gpu.h — C ABI of libflame3d_gpu.so, the GB300 (sm_103a) finite-difference
+ * right-hand side and SSP-RK3 stage of the Flame3D compressible Navier–Stokes solver.
+ *
+ * The library replaces the @cuda launch sites of the reference's finite-difference
+ * path: flowAdvance (solver.jl:19-189, finite_volume=false branch at solver.jl:133-188),
+ * the RK3 stage loop (solver.jl:416-444), exchange_ghost (mpi.jl:2-103) and fillGhost
+ * (boundary.jl:151-156). A Julia driver binds it with ccall; every array keeps the
+ * reference layout: Julia column-major (Nx+2NG, Ny+2NG, Nz+2NG, nvar), i fastest, so the
+ * 0-based linear index of (i,j,k,n) is i + Nxt*(j + Nyt*(k + Nzt*n)).
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers owned by the caller (Julia CuArrays or torch
+ *    tensors). The library never frees them. Scratch space is allocated in f3d_create and
+ *    released in f3d_destroy.
+ *  - Every entry point returns an int status (F3D_OK = 0). No exception or abort crosses
+ *    the ABI. f3d_last_error(ctx) returns a message for the last failure on that ctx.
+ *  - Calls are asynchronous on the given stream (NULL = legacy default stream). A context is
+ *    not thread-safe: use one context per host thread / stream.
+ *  - Physical state (U, Un, Q, metrics, J, x/y/z) is always double precision. The
+ *    precision field of f3d_params selects the arithmetic of the flux kernels.
+ */
+#ifndef FLAME3D_GPU_H
+#define FLAME3D_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define F3D_VERSION 10000 /* 1.0.0 */
+
+/* status codes */
+#define F3D_OK 0
+#define F3D_ERR_ARG 1          /* invalid argument (null pointer, bad dims, bad enum)   */
+#define F3D_ERR_ALIGN 2        /* a pointer is not 16-byte aligned                      */
+#define F3D_ERR_CUDA 3         /* a CUDA runtime call failed                            */
+#define F3D_ERR_NONFINITE 4    /* a NaN/Inf was found in the checked state              */
+#define F3D_ERR_UNSUPPORTED 5  /* valid request that this build does not implement       */
+#define F3D_ERR_STATE 6        /* call order violated (e.g. metrics not set)            */
+
+/* flux-vector splitting (run.jl:69 splitMethod; split.jl) */
+#define F3D_SPLIT_SW 0   /* Steger–Warming, split.jl:2-68   */
+#define F3D_SPLIT_LF 1   /* local Lax–Friedrichs, split.jl:70-108 */
+#define F3D_SPLIT_VL 2   /* van Leer, split.jl:110-183      */
+#define F3D_SPLIT_AUSM 3 /* AUSM, split.jl:185-255          */
+
+/* arithmetic of the flux kernels */
+#define F3D_PREC_FP64 0  /* everything in FP64: the drop-in, parity at 1e-12             */
+#define F3D_PREC_MIXED 1 /* FP32 split/reconstruction/weights/viscous; FP64 state, EOS,
+                            metrics/J, RK accumulation and reductions                   */
+
+/* ghost-cell rules, one per face (x-, x+, y-, y+, z-, z+). Faces are filled in the
+ * order x, y, z over the full transverse extent including ghosts, which is the
+ * order of fill_x, fill_y, fill_z in boundary.jl:151-156. */
+#define F3D_BC_PERIODIC 0        /* copy from the opposite side, mpi.jl:2-103 with self as neighbour */
+#define F3D_BC_DIRICHLET 1       /* fixed (rho,u,v,w,p); T = p/(rho Rg), boundary.jl:12-38,98-118   */
+#define F3D_BC_ZERO_GRADIENT 2   /* copy the adjacent interior layer, boundary.jl:42-51             */
+#define F3D_BC_WALL_ADIABATIC 3  /* mirror: rho,p,T even, u,v,w odd, boundary.jl:67-93             */
+#define F3D_BC_WALL_ISOTHERMAL 4 /* mirror u,v,w odd, p even, T = 2 T_wall - T_in, rho = p/(Rg T)  */
+
+typedef struct f3d_bc {
+    int32_t kind;
+    int32_t pad_;
+    double rho, u, v, w, p; /* F3D_BC_DIRICHLET state                        */
+    double t_wall;          /* F3D_BC_WALL_ISOTHERMAL wall temperature         */
+} f3d_bc;
+
+typedef struct f3d_params {
+    int32_t nx, ny, nz;  /* interior cells per direction (Nxp, Nyp, Nzp; run.jl:84-86)   */
+    int32_t ng;          /* ghost layers; must be 4 (parse_mesh.jl:6)                    */
+    double gamma;        /* run.jl:8                                                     */
+    double rg;           /* run.jl:9                                                     */
+    double cp;           /* run.jl:10; 0 means Rg*gamma/(gamma-1)                        */
+    double c_s, t_s;     /* Sutherland constants, run.jl:11-12                           */
+    double pr;           /* Prandtl number, run.jl:13                                    */
+    double phi1, phi2, phi3; /* hybrid thresholds, run.jl:70-72                          */
+    double linear_phi;   /* UP7/CD6 blend of the linear scheme, run.jl:73-77             */
+    double clamp_eps;    /* lower clamp of rho and e_int in c2Prim (utils.jl:12,18);
+                            0 means the reference value eps(Float32) = 2^-23              */
+    int32_t split_method;   /* F3D_SPLIT_*                                               */
+    int32_t character;      /* 1: characteristic-wise (advect_xc), 0: component-wise     */
+    int32_t viscous;        /* 1: add viscous and heat fluxes (viscous.jl)               */
+    int32_t precision;      /* F3D_PREC_*                                                */
+    f3d_bc bc[6];           /* x-, x+, y-, y+, z-, z+                                    */
+} f3d_params;
+
+typedef struct f3d_ctx f3d_ctx;
+typedef struct CUstream_st* f3d_stream; /* a cudaStream_t */
+
+/* ---- lifetime ------------------------------------------------------------------ */
+
+/* Library version, F3D_VERSION. */
+int f3d_version(void);
+
+/* Fill *p with the reference's run.jl defaults (FDM path, SW split, characteristic,
+ * viscous, thresholds 0.05/1/10, the boundary.jl inlet/outlet/wall/farfield/periodic
+ * BCs) for an nx x ny x nz interior grid. Replaces the compile-time consts of run.jl:3-77. */
+int f3d_default_params(int nx, int ny, int nz, f3d_params* p);
+
+/* Validate p, allocate the device scratch for this grid and return a context.
+ * Replaces the allocations of solver.jl:293-337. */
+int f3d_create(const f3d_params* p, f3d_ctx** out);
+int f3d_destroy(f3d_ctx* ctx);
+const char* f3d_last_error(const f3d_ctx* ctx);
+
+/* Bytes of device scratch the context holds. */
+int f3d_scratch_bytes(const f3d_ctx* ctx, size_t* bytes);
+
+/* ---- geometry ------------------------------------------------------------------ */
+
+/* Borrow the nine J^-1-scaled metric arrays (dxi/dx, dxi/dy, dxi/dz, deta/dx, ...,
+ * dzeta/dz, the order of metrics.h5, parse_mesh.jl:240-248) and J, each (Nxt,Nyt,Nzt),
+ * and derive |grad xi_d| (solver.jl:286-288). The pointers must stay valid while the
+ * context uses them. Replaces the metric load of solver.jl:238-288. */
+int f3d_set_metrics(f3d_ctx* ctx, const double* const metrics[9], const double* jac,
+                    f3d_stream stream);
+
+/* Compute metrics and J from coordinates x,y,z (Nxt,Nyt,Nzt with ghost coordinates) with
+ * the CD6 / one-sided CD2 formulas of parse_mesh.jl:139-248, in FP64 on the device. */
+int f3d_compute_metrics(f3d_ctx* ctx, const double* x, const double* y, const double* z,
+                        double* const metrics[9], double* jac, f3d_stream stream);
+
+/* ---- pointwise kernels (utils.jl) ----------------------------------------------- */
+
+/* U -> Q (rho,u,v,w,p,T) at interior cells with the clamps of utils.jl:2-30. */
+int f3d_c2prim(f3d_ctx* ctx, const double* U, double* Q, f3d_stream stream);
+/* Q -> U at every cell, utils.jl:33-54. */
+int f3d_prim2c(f3d_ctx* ctx, const double* Q, double* U, f3d_stream stream);
+/* U = a U + b Un at interior cells, utils.jl:57-70. */
+int f3d_lincomb(f3d_ctx* ctx, double* U, const double* Un, double a, double b,
+                f3d_stream stream);
+/* Ghost layers of Q (6 vars) and U (5 vars) from their interiors by the context's BCs:
+ * exchange_ghost (mpi.jl:2-103) on one GPU followed by fillGhost (boundary.jl:151-156). */
+int f3d_fill_ghosts(f3d_ctx* ctx, double* Q, double* U, f3d_stream stream);
+
+/* ---- right-hand side ------------------------------------------------------------ */
+
+/* dUdt = L(U) at interior cells (dUdt has the U layout; ghosts are not written) from a
+ * ghost-filled Q: shock sensor, flux splitting and hybrid reconstruction in xi, eta,
+ * zeta, viscous fluxes and the flux divergence (div.jl:1-50 without the dt factor).
+ * Equals (U_after_div - U_before)/dt of one reference stage. */
+int f3d_rhs(f3d_ctx* ctx, const double* Q, double* dUdt, f3d_stream stream);
+
+/* One SSP-RK3 stage (stage = 1,2,3) exactly as solver.jl:416-444: stage 1 copies U to
+ * Un; U += dt L(Q); stage 2: U = U/4 + 3Un/4; stage 3: U = 2U/3 + Un/3; then
+ * Q = c2Prim(U) and the ghost fill of Q and U. Q must be ghost-filled on entry. */
+int f3d_rk3_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double* Q,
+                  f3d_stream stream);
+
+/* nsteps full SSP-RK3 steps (3 stages each). Replays a CUDA graph of one step after the
+ * first call with the same pointers. */
+int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, double* Q,
+                  f3d_stream stream);
+
+/* Largest stable dt for the given CFL number over interior cells:
+ * min over cells and directions of cfl / (J (|U_d| + c |grad xi_d|)), U_d = grad xi_d . u.
+ * Synchronises the stream. */
+int f3d_cfl_dt(f3d_ctx* ctx, const double* Q, double cfl, double* dt_out,
+               f3d_stream stream);
+
+/* Scan the interior of U for NaN/Inf (the reference's NaN check, solver.jl:481-486).
+ * Returns F3D_ERR_NONFINITE if one is found. Synchronises the stream. */
+int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream);
+
+/* ---- stage-by-stage intermediates in the reference's own array shapes ----------- */
+
+/* phi (Nxt,Nyt,Nzt) at cells 2..Nt-1, schemes.jl:1-24. */
+int f3d_debug_sensor(f3d_ctx* ctx, const double* Q, double* phi, f3d_stream stream);
+/* Fp, Fm (Nxt,Nyt,Nzt,5) at every cell for direction dir (0=xi,1=eta,2=zeta), split.jl. */
+int f3d_debug_split(f3d_ctx* ctx, int dir, const double* Q, double* Fp, double* Fm,
+                    f3d_stream stream);
+/* Face flux of direction dir in the shape of Fx (Nx+1,Ny,Nz,5), Fy or Fz from Q and phi
+ * (advect_x/xc ... advect_z/zc, schemes.jl:86-1643). */
+int f3d_debug_face_flux(f3d_ctx* ctx, int dir, const double* Q, const double* phi,
+                        double* F, f3d_stream stream);
+/* Fv_x, Fv_y, Fv_z ((Nx+2NG-4),(Ny+2NG-4),(Nz+2NG-4),4), viscous.jl:1-133. */
+int f3d_debug_viscous(f3d_ctx* ctx, const double* Q, double* Fvx, double* Fvy, double* Fvz,
+                      f3d_stream stream);
+/* The reference's div kernel (div.jl:1-50) on caller arrays: U += dt J (dF + dFv). */
+int f3d_div(f3d_ctx* ctx, double* U, const double* Fx, const double* Fy, const double* Fz,
+            const double* Fvx, const double* Fvy, const double* Fvz, double dt,
+            f3d_stream stream);
+
+/* ---- profiling and device characterisation ---------------------------------------- */
+
+/* Kernel kinds of one RK3 step: their number and names ("sweep_xi", ...). */
+int f3d_kernel_count(void);
+const char* f3d_kernel_name(int kind);
+
+/* Run one SSP-RK3 step like f3d_rk3_steps(nsteps=1) without a graph, with a CUDA event
+ * after every launch; ms_out[k] / launches_out[k] receive the summed device time and the
+ * launch count of kernel kind k (arrays of f3d_kernel_count() entries). Synchronises. */
+int f3d_profile_step(f3d_ctx* ctx, double dt, double* U, double* Un, double* Q, f3d_stream stream,
+                     double* ms_out, int* launches_out);
+
+
+/* Measure the FP64 and FP32 FMA pipe throughput of the current device (TFLOP/s) with
+ * dependent-FMA chains over every SM, for roofline reporting. Synchronises. */
+int f3d_measure_pipes(double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLAME3D_GPU_H */
