@@ -1,0 +1,73 @@
+"""Profiling driver: set up a workload and run a few RHS evaluations through the C ABI.
+
+Used under ncu to capture the kernels of one RHS with few launches before them:
+
+  python -m flame3d_mhd_gb300.profile --case sod --nx 256 --ny 64 --nz 64 --reps 2
+  ncu --set full --clock-control none -k regex:k_sweep -s 3 -c 3 -o prof \
+      python -m flame3d_mhd_gb300.profile --case sod --reps 2
+
+The first RHS evaluation is a warm-up (its launches are the ones skipped with -s).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+import torch
+
+from . import cases
+from .solver import Flame3D
+
+
+def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: int = 0):
+    if case == "sod":
+        c = cases.sod(nx, ny, nz, character=character)
+    elif case == "tgv":
+        c = cases.tgv(nx, character=character)
+    else:
+        raise ValueError(case)
+    P = c["params"]
+    P.precision = precision
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    s = Flame3D(P)
+    ms, J = s.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
+    s.set_metrics(ms, J)
+    Q = dev(c["Q"])
+    U = s.field(5)
+    s.prim2c(U, Q)
+    s.fillGhost(Q, U)
+    return s, c, U, Q
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="sod", choices=["sod", "tgv"])
+    ap.add_argument("--nx", type=int, default=256)
+    ap.add_argument("--ny", type=int, default=64)
+    ap.add_argument("--nz", type=int, default=64)
+    ap.add_argument("--character", type=int, default=1)
+    ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--step", action="store_true", help="profile_step instead of rhs (per-kernel event times)")
+    a = ap.parse_args(argv)
+    s, c, U, Q = setup(a.case, a.nx, a.ny, a.nz, a.character, a.precision)
+    out = s.field(5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.reps):
+        if a.step:
+            Un = s.field(5)
+            print(json.dumps(s.profile_step(U, Un, Q, c["dt"])))
+        else:
+            s.rhs(Q, out)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": a.case, "n": [a.nx, a.ny, a.nz], "reps": a.reps,
+                      "ms_per_rep": (time.perf_counter() - t0) / a.reps * 1e3}), file=sys.stderr)
+    s.close()
+
+
+if __name__ == "__main__":
+    main()
