@@ -13,6 +13,86 @@
 
 using namespace f3d;
 
+namespace f3d {
+
+// Branch every face takes when the thresholds leave no choice for a sensor value in
+// [0, 3] (each directional term of schemes.jl:19-21 lies in [0,1] for positive p).
+static int fixed_branch_of(const f3d_params& p) {
+    const double top = 4.0;
+    if (p.phi1 > top) return 0;
+    if (p.phi1 <= 0.0 && p.phi2 > top) return 1;
+    if (p.phi1 <= 0.0 && p.phi2 <= 0.0 && p.phi3 > top) return 2;
+    if (p.phi1 <= 0.0 && p.phi2 <= 0.0 && p.phi3 <= 0.0) return 3;
+    return -1;
+}
+
+int validate_params(const f3d_params& p, std::string& why) {
+    if (p.ng != NG) { why = "ng must be 4"; return F3D_ERR_ARG; }
+    if (p.nx < NG || p.ny < NG || p.nz < NG) { why = "each interior dimension must be >= 4"; return F3D_ERR_ARG; }
+    if ((long long)p.nx > (1 << 20) || (long long)p.ny > 65535 - 8 || (long long)p.nz > 65535 - 8) {
+        why = "grid too large for the launch shape"; return F3D_ERR_ARG;
+    }
+    const long long cells = (long long)(p.nx + 8) * (p.ny + 8) * (p.nz + 8);
+    if (cells > (1LL << 34)) { why = "grid too large"; return F3D_ERR_ARG; }
+    if (!(p.gamma > 1.0) || !(p.rg > 0.0) || !(p.pr > 0.0) || !(p.c_s >= 0.0) || !(p.t_s >= 0.0)) {
+        why = "gas constants out of range"; return F3D_ERR_ARG;
+    }
+    if (p.split_method < 0 || p.split_method > 3) { why = "unknown split_method"; return F3D_ERR_ARG; }
+    if (p.character != 0 && p.character != 1) { why = "character must be 0 or 1"; return F3D_ERR_ARG; }
+    if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
+    if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
+    if (p.precision == F3D_PREC_MIXED) { why = "mixed precision is not built in this library"; return F3D_ERR_UNSUPPORTED; }
+    int iso_dirs = 0;
+    for (int d = 0; d < 3; d++) {
+        const f3d_bc &lo = p.bc[2 * d], &hi = p.bc[2 * d + 1];
+        for (const f3d_bc* b : {&lo, &hi}) {
+            if (b->kind < 0 || b->kind > 4) { why = "unknown boundary kind"; return F3D_ERR_ARG; }
+            if (b->kind == F3D_BC_DIRICHLET && !(b->rho > 0.0 && b->p > 0.0)) {
+                why = "Dirichlet state needs rho > 0 and p > 0"; return F3D_ERR_ARG;
+            }
+            if (b->kind == F3D_BC_WALL_ISOTHERMAL && !(b->t_wall > 0.0)) {
+                why = "isothermal wall needs t_wall > 0"; return F3D_ERR_ARG;
+            }
+        }
+        if ((lo.kind == F3D_BC_PERIODIC) != (hi.kind == F3D_BC_PERIODIC)) {
+            why = "periodic boundaries must be paired on both faces of a direction"; return F3D_ERR_ARG;
+        }
+        if (lo.kind == F3D_BC_WALL_ISOTHERMAL || hi.kind == F3D_BC_WALL_ISOTHERMAL) iso_dirs++;
+    }
+    if (iso_dirs > 1) { why = "isothermal walls on more than one direction are not supported"; return F3D_ERR_UNSUPPORTED; }
+    return F3D_OK;
+}
+
+DevParams make_dev_params(const f3d_params& p) {
+    DevParams d;
+    std::memset(&d, 0, sizeof(d));
+    d.nx = p.nx; d.ny = p.ny; d.nz = p.nz;
+    d.nxt = p.nx + 2 * NG; d.nyt = p.ny + 2 * NG; d.nzt = p.nz + 2 * NG;
+    d.plane = (long long)d.nxt * d.nyt * d.nzt;
+    d.gamma = p.gamma; d.rg = p.rg;
+    d.cp = p.cp != 0.0 ? p.cp : p.rg * p.gamma / (p.gamma - 1.0);
+    d.c_s = p.c_s; d.t_s = p.t_s; d.pr = p.pr;
+    d.gm1 = p.gamma - 1.0;
+    d.grg = p.gamma * p.rg;
+    d.eps_clamp = p.clamp_eps != 0.0 ? p.clamp_eps : 1.1920928955078125e-07;
+    d.phi1 = p.phi1; d.phi2 = p.phi2; d.phi3 = p.phi3;
+    const double up7[7] = {-3.0 / 420, 25.0 / 420, -101.0 / 420, 319.0 / 420, 214.0 / 420, -38.0 / 420, 4.0 / 420};
+    const double cd6[7] = {0.0, 1.0 / 60, -2.0 / 15, 37.0 / 60, 37.0 / 60, -2.0 / 15, 1.0 / 60};
+    for (int m = 0; m < 7; m++) d.lin[m] = up7[m] * p.linear_phi + cd6[m] * (1.0 - p.linear_phi);
+    d.split = p.split_method; d.character = p.character; d.viscous = p.viscous;
+    d.fixed_branch = fixed_branch_of(p);
+    for (int f = 0; f < 6; f++) {
+        const f3d_bc& b = p.bc[f];
+        d.bc[f].kind = b.kind;
+        d.bc[f].rho = b.rho; d.bc[f].u = b.u; d.bc[f].v = b.v; d.bc[f].w = b.w; d.bc[f].p = b.p;
+        d.bc[f].T = b.kind == F3D_BC_DIRICHLET ? b.p / (b.rho * p.rg) : 0.0;
+        d.bc[f].t_wall = b.t_wall;
+    }
+    return d;
+}
+
+}  // namespace f3d
+
 // Per-launch event recording for f3d_profile_step.
 struct Prof {
     static constexpr int kMax = 64;
@@ -83,82 +163,6 @@ int check_ptrs(f3d_ctx* ctx, std::initializer_list<const void*> ps) {
         if (!aligned(p)) return fail(ctx, F3D_ERR_ALIGN, "array pointer not 16-byte aligned");
     }
     return F3D_OK;
-}
-
-// Branch every face takes when the thresholds leave no choice for a sensor value in
-// [0, 3] (each directional term of schemes.jl:19-21 lies in [0,1] for positive p).
-int fixed_branch_of(const f3d_params& p) {
-    const double top = 4.0;
-    if (p.phi1 > top) return 0;
-    if (p.phi1 <= 0.0 && p.phi2 > top) return 1;
-    if (p.phi1 <= 0.0 && p.phi2 <= 0.0 && p.phi3 > top) return 2;
-    if (p.phi1 <= 0.0 && p.phi2 <= 0.0 && p.phi3 <= 0.0) return 3;
-    return -1;
-}
-
-int validate(const f3d_params& p, std::string& why) {
-    if (p.ng != NG) { why = "ng must be 4"; return F3D_ERR_ARG; }
-    if (p.nx < NG || p.ny < NG || p.nz < NG) { why = "each interior dimension must be >= 4"; return F3D_ERR_ARG; }
-    if ((long long)p.nx > (1 << 20) || (long long)p.ny > 65535 - 8 || (long long)p.nz > 65535 - 8) {
-        why = "grid too large for the launch shape"; return F3D_ERR_ARG;
-    }
-    const long long cells = (long long)(p.nx + 8) * (p.ny + 8) * (p.nz + 8);
-    if (cells > (1LL << 34)) { why = "grid too large"; return F3D_ERR_ARG; }
-    if (!(p.gamma > 1.0) || !(p.rg > 0.0) || !(p.pr > 0.0) || !(p.c_s >= 0.0) || !(p.t_s >= 0.0)) {
-        why = "gas constants out of range"; return F3D_ERR_ARG;
-    }
-    if (p.split_method < 0 || p.split_method > 3) { why = "unknown split_method"; return F3D_ERR_ARG; }
-    if (p.character != 0 && p.character != 1) { why = "character must be 0 or 1"; return F3D_ERR_ARG; }
-    if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
-    if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
-    if (p.precision == F3D_PREC_MIXED) { why = "mixed precision is not built in this library"; return F3D_ERR_UNSUPPORTED; }
-    int iso_dirs = 0;
-    for (int d = 0; d < 3; d++) {
-        const f3d_bc &lo = p.bc[2 * d], &hi = p.bc[2 * d + 1];
-        for (const f3d_bc* b : {&lo, &hi}) {
-            if (b->kind < 0 || b->kind > 4) { why = "unknown boundary kind"; return F3D_ERR_ARG; }
-            if (b->kind == F3D_BC_DIRICHLET && !(b->rho > 0.0 && b->p > 0.0)) {
-                why = "Dirichlet state needs rho > 0 and p > 0"; return F3D_ERR_ARG;
-            }
-            if (b->kind == F3D_BC_WALL_ISOTHERMAL && !(b->t_wall > 0.0)) {
-                why = "isothermal wall needs t_wall > 0"; return F3D_ERR_ARG;
-            }
-        }
-        if ((lo.kind == F3D_BC_PERIODIC) != (hi.kind == F3D_BC_PERIODIC)) {
-            why = "periodic boundaries must be paired on both faces of a direction"; return F3D_ERR_ARG;
-        }
-        if (lo.kind == F3D_BC_WALL_ISOTHERMAL || hi.kind == F3D_BC_WALL_ISOTHERMAL) iso_dirs++;
-    }
-    if (iso_dirs > 1) { why = "isothermal walls on more than one direction are not supported"; return F3D_ERR_UNSUPPORTED; }
-    return F3D_OK;
-}
-
-DevParams make_dev(const f3d_params& p) {
-    DevParams d;
-    std::memset(&d, 0, sizeof(d));
-    d.nx = p.nx; d.ny = p.ny; d.nz = p.nz;
-    d.nxt = p.nx + 2 * NG; d.nyt = p.ny + 2 * NG; d.nzt = p.nz + 2 * NG;
-    d.plane = (long long)d.nxt * d.nyt * d.nzt;
-    d.gamma = p.gamma; d.rg = p.rg;
-    d.cp = p.cp != 0.0 ? p.cp : p.rg * p.gamma / (p.gamma - 1.0);
-    d.c_s = p.c_s; d.t_s = p.t_s; d.pr = p.pr;
-    d.gm1 = p.gamma - 1.0;
-    d.grg = p.gamma * p.rg;
-    d.eps_clamp = p.clamp_eps != 0.0 ? p.clamp_eps : 1.1920928955078125e-07;
-    d.phi1 = p.phi1; d.phi2 = p.phi2; d.phi3 = p.phi3;
-    const double up7[7] = {-3.0 / 420, 25.0 / 420, -101.0 / 420, 319.0 / 420, 214.0 / 420, -38.0 / 420, 4.0 / 420};
-    const double cd6[7] = {0.0, 1.0 / 60, -2.0 / 15, 37.0 / 60, 37.0 / 60, -2.0 / 15, 1.0 / 60};
-    for (int m = 0; m < 7; m++) d.lin[m] = up7[m] * p.linear_phi + cd6[m] * (1.0 - p.linear_phi);
-    d.split = p.split_method; d.character = p.character; d.viscous = p.viscous;
-    d.fixed_branch = fixed_branch_of(p);
-    for (int f = 0; f < 6; f++) {
-        const f3d_bc& b = p.bc[f];
-        d.bc[f].kind = b.kind;
-        d.bc[f].rho = b.rho; d.bc[f].u = b.u; d.bc[f].v = b.v; d.bc[f].w = b.w; d.bc[f].p = b.p;
-        d.bc[f].T = b.kind == F3D_BC_DIRICHLET ? b.p / (b.rho * p.rg) : 0.0;
-        d.bc[f].t_wall = b.t_wall;
-    }
-    return d;
 }
 
 int check_ctx(f3d_ctx* ctx, bool need_metrics) {
@@ -272,14 +276,14 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     if (!p || !out) return F3D_ERR_ARG;
     *out = nullptr;
     std::string why;
-    int rc = validate(*p, why);
+    int rc = validate_params(*p, why);
     if (rc) {
         std::fprintf(stderr, "f3d_create: %s\n", why.c_str());
         return rc;
     }
     f3d_ctx* ctx = new f3d_ctx();
     ctx->params = *p;
-    ctx->dp = make_dev(*p);
+    ctx->dp = make_dev_params(*p);
     if (cudaGetDevice(&ctx->device) != cudaSuccess) { delete ctx; return F3D_ERR_CUDA; }
     const size_t nc = (size_t)ctx->dp.plane;
     const size_t nv = (size_t)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);

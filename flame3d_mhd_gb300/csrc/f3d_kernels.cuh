@@ -1,5 +1,7 @@
 // f3d_kernels.cuh — launch interfaces between the C-ABI layer (api.cu) and the kernels.
 #pragma once
+#include <string>
+
 #include "f3d_common.cuh"
 #include "f3d_flux.cuh"
 
@@ -29,6 +31,10 @@ struct SweepArgs {
     int combine;
     int stage1_copy;      // OUT_STAGE of stage 1: Un = U before the update
 };
+
+// parameter validation and device constants (api.cu)
+int validate_params(const f3d_params& p, std::string& why);
+DevParams make_dev_params(const f3d_params& p);
 
 cudaError_t sweep_configure();
 cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st);

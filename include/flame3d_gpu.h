@@ -40,6 +40,7 @@ extern "C" {
 #define F3D_ERR_NONFINITE 4    /* a NaN/Inf was found in the checked state              */
 #define F3D_ERR_UNSUPPORTED 5  /* valid request that this build does not implement       */
 #define F3D_ERR_STATE 6        /* call order violated (e.g. metrics not set)            */
+#define F3D_ERR_TOO_LARGE 7    /* the grid needs more scratch than f3d_rhs_noalloc holds */
 
 /* flux-vector splitting (run.jl:69 splitMethod; split.jl) */
 #define F3D_SPLIT_SW 0   /* Steger–Warming, split.jl:2-68   */
@@ -164,6 +165,30 @@ int f3d_cfl_dt(f3d_ctx* ctx, const double* Q, double cfl, double* dt_out,
 /* Scan the interior of U for NaN/Inf (the reference's NaN check, solver.jl:481-486).
  * Returns F3D_ERR_NONFINITE if one is found. Synchronises the stream. */
 int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream);
+
+/* ---- right-hand side without device allocation -------------------------------------- */
+
+/* Scratch held by f3d_rhs_noalloc: a file-scope device array of this many bytes, kept by
+ * every GPU that loads the library until the process exits. */
+#define F3D_NOALLOC_SCRATCH_BYTES (32 * 1024 * 1024)
+
+/* The same dUdt as f3d_create + f3d_set_metrics + f3d_rhs, for callers that cannot
+ * allocate device memory: code running while its stream is captured into a CUDA graph, or
+ * hosts whose memory pool owns the device and forbids cudaMalloc/cudaFree (cudaFree would
+ * also synchronise the device). No context is needed: p, the nine metrics, J, the
+ * ghost-filled Q and dUdt are the caller's; nothing is allocated and no allocating library
+ * routine is called. Scratch (|A|, A/|A|, sound speed, sensor and, when viscous, the
+ * viscous fluxes: 14 (Nx+8)(Ny+8)(Nz+8) doubles + 12 (Nx+4)(Ny+4)(Nz+4) doubles) lives in
+ * one shared device array of F3D_NOALLOC_SCRATCH_BYTES; larger grids return
+ * F3D_ERR_TOO_LARGE (about 58^3 interior cells inviscid, 48^3 viscous). The first call on
+ * a device looks up that array's device address and sets kernel attributes for that
+ * device: make it before any stream capture. Every call uses the same array and leaves its
+ * contents behind, so calls whose kernels overlap on the GPU (on different streams or host
+ * threads) race: serialise them. Returns F3D_* codes; messages go to stderr.
+ * This entry point has no counterpart in the reference, whose kernels take preallocated
+ * CuArrays (solver.jl:293-337). */
+int f3d_rhs_noalloc(const f3d_params* p, const double* const metrics[9], const double* jac,
+                    const double* Q, double* dUdt, f3d_stream stream);
 
 /* ---- stage-by-stage intermediates in the reference's own array shapes ----------- */
 
