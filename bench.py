@@ -119,6 +119,18 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_max(x: float, device=None) -> float:
+    """Maximum of x over the ranks of the default process group (x itself when there is none).
+    Host-side control only: one scalar per timed run, no data-path collective."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_sample(target_s: float = 12.0, max_steps: int = 8) -> dict:
     """The oracle (C++ restatement of the reference algorithm, OpenMP on every host core) on
     the same workload: one untimed step, then whole RK3 steps until about target_s."""
@@ -234,12 +246,7 @@ def run_ours(args):
         barrier()
         tw1 = time.time()
     sampler.stop()
-    ms_total = e0.elapsed_time(e1)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = reduce_max(e0.elapsed_time(e1), device="cuda")
     ms_step = ms_total / args.steps
     value = ws * cells * 3 * args.steps / (ms_total / 1e3) / 1e6
     ok = s.check_finite(U)
