@@ -227,29 +227,72 @@ def run_ours(args):
             dist.barrier()
 
     stream = torch.cuda.Stream()
+
+    def timed_steps(solver, U, Un, Q, steps, warmup):
+        """warmup untimed steps, then `steps` timed ones (CUDA events on `stream`, barriers
+        and device syncs on both sides); returns (ms, wall t0, wall t1)."""
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                solver.time_step(U, Un, Q, dt, 1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            stream.synchronize()
+            barrier()
+            torch.cuda.synchronize()
+            t0 = time.time()
+            e0.record(stream)
+            solver.time_step(U, Un, Q, dt, steps)
+            e1.record(stream)
+            e1.synchronize()
+            torch.cuda.synchronize()
+            barrier()
+            t1 = time.time()
+        return reduce_max(e0.elapsed_time(e1), device="cuda"), t0, t1
+
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            s.time_step(U, Un, Q, dt, 1)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        stream.synchronize()
-        barrier()
-        torch.cuda.synchronize()
-        tw0 = time.time()
-        e0.record(stream)
-        s.time_step(U, Un, Q, dt, args.steps)
-        e1.record(stream)
-        e1.synchronize()
-        torch.cuda.synchronize()
-        barrier()
-        tw1 = time.time()
+    ms_total, tw0, tw1 = timed_steps(s, U, Un, Q, args.steps, args.warmup)
     sampler.stop()
-    ms_total = reduce_max(e0.elapsed_time(e1), device="cuda")
+    U_fp64 = U.clone()
     ms_step = ms_total / args.steps
     value = ws * cells * 3 * args.steps / (ms_total / 1e3) / 1e6
     ok = s.check_finite(U)
+
+    # mixed precision on the same workload, from the same initial state, same step count
+    from flame3d_mhd_gb300.abi import PREC_MIXED
+    from flame3d_mhd_gb300.cases import params_copy
+    sm = Flame3D(params_copy(P, precision=PREC_MIXED))
+    sm.set_metrics(ms, J)
+    Um, Unm, Qm = U0.clone(), torch.zeros_like(U0), Q0.clone()
+    ms_mixed, _, _ = timed_steps(sm, Um, Unm, Qm, args.steps, args.warmup)
+    value_mixed = ws * cells * 3 * args.steps / (ms_mixed / 1e3) / 1e6
+    Iin = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+    state_err = float((Um[Iin] - U_fp64[Iin]).abs().max() / U_fp64[Iin].abs().max())
+
+    def kinetic(Uv):
+        r = Uv[Iin][0]
+        return float(((0.5 * (Uv[Iin][1] ** 2 + Uv[Iin][2] ** 2 + Uv[Iin][3] ** 2) / r) / J[Iin[1:]]).sum())
+    ke64, ke32 = kinetic(U_fp64), kinetic(Um)
+    r64, r32 = s.rhs(Q0), sm.rhs(Q0)
+    rhs_err = max(float((r32[n][Iin[1:]] - r64[n][Iin[1:]]).abs().max() / r64[n][Iin[1:]].abs().max())
+                  for n in range(5))
+    prof_m = {}
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            for k, (t_ms, n) in sm.profile_step(Um, Unm, Qm, dt).items():
+                a = prof_m.setdefault(k, [0.0, 0])
+                a[0] += t_ms
+                a[1] += n
+    tot_m = sum(t for t, _ in prof_m.values())
+    mixed = {"value": value_mixed, "unit": UNIT, "ms_per_step": ms_mixed / args.steps,
+             "speedup_vs_fp64": value_mixed / value,
+             "err_vs_fp64": {"rhs_rel_linf_initial_state": rhs_err,
+                             "state_rel_linf_after_steps": state_err,
+                             "kinetic_energy_rel": abs(ke32 - ke64) / abs(ke64) if ke64 else None,
+                             "steps": args.steps + args.warmup},
+             "shares": {k: round(v[0] / tot_m, 4) for k, v in sorted(prof_m.items())},
+             "step_hbm_frac": STEP_BYTES_PER_CELL * cells / (ms_mixed / args.steps / 1e3) / 1e9 / load_peaks()["hbm_gbs"]}
+    sm.close()
 
     # per-kernel device times of single steps (events between launches, outside the timed loop)
     prof = {}
@@ -311,6 +354,7 @@ def run_ours(args):
         "roofline_step": {"bound": "hbm", "achieved": step_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                           "frac": step_gbs / peaks["hbm_gbs"], "alg_bytes_per_cell_step": STEP_BYTES_PER_CELL},
         "mcell_updates_per_s": value / 3,
+        "mixed": mixed,
         "clocks": clocks,
         "state_finite": bool(ok),
     }

@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "f3d_kernels.cuh"
 
@@ -41,7 +42,6 @@ int validate_params(const f3d_params& p, std::string& why) {
     if (p.character != 0 && p.character != 1) { why = "character must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
-    if (p.precision == F3D_PREC_MIXED) { why = "mixed precision is not built in this library"; return F3D_ERR_UNSUPPORTED; }
     int iso_dirs = 0;
     for (int d = 0; d < 3; d++) {
         const f3d_bc &lo = p.bc[2 * d], &hi = p.bc[2 * d + 1];
@@ -80,7 +80,25 @@ DevParams make_dev_params(const f3d_params& p) {
     const double cd6[7] = {0.0, 1.0 / 60, -2.0 / 15, 37.0 / 60, 37.0 / 60, -2.0 / 15, 1.0 / 60};
     for (int m = 0; m < 7; m++) d.lin[m] = up7[m] * p.linear_phi + cd6[m] * (1.0 - p.linear_phi);
     d.split = p.split_method; d.character = p.character; d.viscous = p.viscous;
+    d.precision = p.precision;
     d.fixed_branch = fixed_branch_of(p);
+    const double th[3] = {p.phi1, p.phi2, p.phi3};
+    for (int k = 0; k < 3; k++) {
+        unsigned long long b = 0;
+        if (th[k] > 0.0) std::memcpy(&b, &th[k], 8);
+        d.phib[k] = b;
+    }
+    auto fill = [&](auto& c) {
+        using R = std::remove_reference_t<decltype(c.gamma)>;
+        c.gamma = (R)p.gamma; c.rg = (R)p.rg; c.grg = (R)d.grg; c.gm1 = (R)d.gm1;
+        c.inv_gm1 = (R)(1.0 / d.gm1); c.inv_2g = (R)(1.0 / (2.0 * p.gamma)); c.two_gm1 = (R)(2.0 * d.gm1);
+        c.w2c = (R)((3.0 - p.gamma) / (2.0 * d.gm1));
+        c.c_s = (R)d.c_s; c.t_s = (R)d.t_s; c.cp = (R)d.cp; c.pr = (R)d.pr;
+        c.phi1 = (R)p.phi1; c.phi2 = (R)p.phi2; c.phi3 = (R)p.phi3;
+        for (int m = 0; m < 7; m++) c.lin[m] = (R)d.lin[m];
+    };
+    fill(d.cd);
+    fill(d.cf);
     for (int f = 0; f < 6; f++) {
         const f3d_bc& b = p.bc[f];
         d.bc[f].kind = b.kind;
@@ -118,6 +136,12 @@ struct f3d_ctx {
     double* phi = nullptr;
     double* acc = nullptr;
     double* Fv[3] = {};
+    // mixed precision: FP32 copies and FP32 intermediates
+    float* Q32 = nullptr;
+    MetricPtrs32 m32 = {};
+    float* phi32 = nullptr;
+    float* acc32 = nullptr;
+    float* Fv32[3] = {};
     double* dscalar = nullptr;  // 8 bytes for reductions
     Prof* prof = nullptr;
     // CUDA graph of one RK3 step, keyed by its arguments
@@ -172,10 +196,25 @@ int check_ctx(f3d_ctx* ctx, bool need_metrics) {
     return F3D_OK;
 }
 
-SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, const double* phi) {
+bool mixed(const f3d_ctx* ctx) { return ctx->dp.precision == F3D_PREC_MIXED; }
+
+SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const double* phi_override = nullptr) {
     SweepArgs a;
     std::memset(&a, 0, sizeof(a));
     a.P = ctx->dp;
+    a.J = ctx->J;
+    if (mixed(ctx)) {
+        a.fp32 = 1;
+        a.Q = ctx->Q32;
+        for (int n = 0; n < 3; n++) {
+            a.A[n] = ctx->m32.A[3 * dir + n];
+            a.Ah[n] = ctx->m32.H[3 * dir + n];
+        }
+        a.S = ctx->m32.S[dir];
+        a.phi = hybrid ? ctx->phi32 : nullptr;
+        a.Fv = ctx->params.viscous ? ctx->Fv32[dir] : nullptr;
+        return a;
+    }
     a.Q = Q;
     a.csnd = ctx->csnd;
     for (int n = 0; n < 3; n++) {
@@ -183,29 +222,48 @@ SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, const double* phi) 
         a.Ah[n] = ctx->Ah[3 * dir + n];
     }
     a.S = ctx->S[dir];
-    a.phi = phi;
+    a.phi = hybrid ? (phi_override ? phi_override : ctx->phi) : nullptr;
     a.Fv = ctx->params.viscous ? ctx->Fv[dir] : nullptr;
-    a.J = ctx->J;
     return a;
 }
 
-// Sensor, viscous fluxes and the three sweeps. mode_last is OUT_RHS or OUT_STAGE.
-int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStream_t st) {
+// Sensor, viscous fluxes and the three sweeps. last.out_mode is OUT_RHS or OUT_STAGE.
+// Mixed precision: the FP32 copy of Q is made first unless q32_current says the previous
+// stage's primitive fill already wrote it.
+int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStream_t st, bool q32_current = false) {
     const DevParams& P = ctx->dp;
-    F3D_CUDA(ctx, launch_sound(P, Q, ctx->csnd, st));
-    mark(ctx, K_SOUND, st);
     const bool hybrid = P.fixed_branch < 0;
-    if (hybrid) {
-        F3D_CUDA(ctx, launch_sensor(P, Q, ctx->phi, st));
-        mark(ctx, K_SENSOR, st);
-    }
-    if (ctx->params.viscous) {
-        F3D_CUDA(ctx, launch_viscous(P, Q, ctx->m, ctx->J, ctx->Fv[0], ctx->Fv[1], ctx->Fv[2], st));
-        mark(ctx, K_VISCOUS, st);
+    const bool mx = mixed(ctx);
+    if (mx) {
+        if (!q32_current) {
+            F3D_CUDA(ctx, launch_to_f32(Q, ctx->Q32, 6 * P.plane, st));
+            mark(ctx, K_SOUND, st);
+        }
+        if (hybrid) {
+            F3D_CUDA(ctx, launch_sensor32(P, ctx->Q32, ctx->phi32, st));
+            mark(ctx, K_SENSOR, st);
+        }
+        if (ctx->params.viscous) {
+            const float* m32[9];
+            for (int n = 0; n < 9; n++) m32[n] = ctx->m32.A[n];
+            F3D_CUDA(ctx, launch_viscous32(P, ctx->Q32, m32, ctx->m32.J, ctx->Fv32[0], ctx->Fv32[1], ctx->Fv32[2], st));
+            mark(ctx, K_VISCOUS, st);
+        }
+    } else {
+        F3D_CUDA(ctx, launch_sound(P, Q, ctx->csnd, st));
+        mark(ctx, K_SOUND, st);
+        if (hybrid) {
+            F3D_CUDA(ctx, launch_sensor(P, Q, ctx->phi, st));
+            mark(ctx, K_SENSOR, st);
+        }
+        if (ctx->params.viscous) {
+            F3D_CUDA(ctx, launch_viscous(P, Q, ctx->m, ctx->J, ctx->Fv[0], ctx->Fv[1], ctx->Fv[2], st));
+            mark(ctx, K_VISCOUS, st);
+        }
     }
     for (int d = 0; d < 3; d++) {
-        SweepArgs a = sweep_args(ctx, d, Q, hybrid ? ctx->phi : nullptr);
-        a.acc = acc;
+        SweepArgs a = sweep_args(ctx, d, Q, hybrid);
+        a.acc = mx ? (void*)ctx->acc32 : (void*)acc;
         if (d == 0) a.out_mode = OUT_SET;
         else if (d == 1) a.out_mode = OUT_ADD;
         else {
@@ -225,7 +283,8 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
     return F3D_OK;
 }
 
-int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double* Q, cudaStream_t st) {
+int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double* Q, cudaStream_t st,
+              bool q32_current = false) {
     SweepArgs last;
     std::memset(&last, 0, sizeof(last));
     last.out_mode = OUT_STAGE;
@@ -236,9 +295,9 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
     last.combine = stage != 1;
     last.ca = stage == 2 ? 0.25 : 2.0 / 3.0;  // utils.jl:57-70 via solver.jl:433-435
     last.cb = stage == 2 ? 0.75 : 1.0 / 3.0;
-    int rc = run_rhs(ctx, Q, ctx->acc, last, st);
+    int rc = run_rhs(ctx, Q, ctx->acc, last, st, q32_current);
     if (rc) return rc;
-    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 0, st));
+    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 0, st, mixed(ctx) ? ctx->Q32 : nullptr));
     mark(ctx, K_PRIM_FILL, st);
     return F3D_OK;
 }
@@ -287,10 +346,14 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     if (cudaGetDevice(&ctx->device) != cudaSuccess) { delete ctx; return F3D_ERR_CUDA; }
     const size_t nc = (size_t)ctx->dp.plane;
     const size_t nv = (size_t)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
-    // S(3) + Ah(9) + csnd + phi + acc(5) + viscous(12) + scalar
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t b1 = up(nc * sizeof(double));
-    size_t total = b1 * (3 + 9 + 1 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * sizeof(double)) : 0) + 256;
+    const bool mx = p->precision == F3D_PREC_MIXED;
+    size_t total = 256;
+    if (!mx) {  // S(3) + A/|A|(9) + sound speed + phi + acc(5) [+ viscous 12]
+        total += up(nc * 8) * (3 + 9 + 1 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 8) : 0);
+    } else {    // Q32(6) + A32(9) + H32(9) + S32(3) + J32 + phi32 + acc32(5) [+ viscous 12]
+        total += up(nc * 4) * (6 + 9 + 9 + 3 + 1 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 4) : 0);
+    }
     cudaError_t e = cudaMalloc(&ctx->slab, total);
     if (e != cudaSuccess) {
         delete ctx;
@@ -299,16 +362,34 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     }
     ctx->slab_bytes = total;
     char* q = (char*)ctx->slab;
-    for (int d = 0; d < 3; d++) { ctx->S[d] = (double*)q; q += b1; }
-    for (int n = 0; n < 9; n++) { ctx->Ah[n] = (double*)q; q += b1; }
-    ctx->csnd = (double*)q; q += b1;
-    ctx->phi = (double*)q; q += b1;
-    ctx->acc = (double*)q; q += 5 * b1;
-    if (p->viscous)
-        for (int d = 0; d < 3; d++) { ctx->Fv[d] = (double*)q; q += up(nv * 4 * sizeof(double)); }
+    size_t phi_bytes;
+    if (!mx) {
+        const size_t b1 = up(nc * 8);
+        for (int d = 0; d < 3; d++) { ctx->S[d] = (double*)q; q += b1; }
+        for (int n = 0; n < 9; n++) { ctx->Ah[n] = (double*)q; q += b1; }
+        ctx->csnd = (double*)q; q += b1;
+        ctx->phi = (double*)q; q += b1;
+        ctx->acc = (double*)q; q += 5 * b1;
+        if (p->viscous)
+            for (int d = 0; d < 3; d++) { ctx->Fv[d] = (double*)q; q += up(nv * 4 * 8); }
+        phi_bytes = b1;
+    } else {
+        const size_t b1 = up(nc * 4);
+        ctx->Q32 = (float*)q; q += 6 * b1;
+        for (int n = 0; n < 9; n++) { ctx->m32.A[n] = (float*)q; q += b1; }
+        for (int n = 0; n < 9; n++) { ctx->m32.H[n] = (float*)q; q += b1; }
+        for (int d = 0; d < 3; d++) { ctx->m32.S[d] = (float*)q; q += b1; }
+        ctx->m32.J = (float*)q; q += b1;
+        ctx->phi32 = (float*)q; q += b1;
+        ctx->acc32 = (float*)q; q += 5 * b1;
+        if (p->viscous)
+            for (int d = 0; d < 3; d++) { ctx->Fv32[d] = (float*)q; q += up(nv * 4 * 4); }
+        phi_bytes = b1;
+    }
     ctx->dscalar = (double*)q;
     // phi outside cells 1..Nt-2 is never written; keep it defined (CUDA.zeros in solver.jl:296)
-    if ((e = cudaMemset(ctx->phi, 0, b1)) != cudaSuccess || (e = sweep_configure()) != cudaSuccess) {
+    if ((e = cudaMemset(mx ? (void*)ctx->phi32 : (void*)ctx->phi, 0, phi_bytes)) != cudaSuccess ||
+        (e = sweep_configure()) != cudaSuccess) {
         cudaFree(ctx->slab);
         delete ctx;
         std::fprintf(stderr, "f3d_create: %s\n", cudaGetErrorString(e));
@@ -344,7 +425,14 @@ int f3d_set_metrics(f3d_ctx* ctx, const double* const metrics[9], const double* 
         return rc;
     for (int n = 0; n < 9; n++) ctx->m[n] = metrics[n];
     ctx->J = jac;
-    F3D_CUDA(ctx, launch_metric_prep(ctx->dp, ctx->m, ctx->S, ctx->Ah, (cudaStream_t)stream));
+    if (mixed(ctx)) {
+        MetricPtrs mp;
+        for (int n = 0; n < 9; n++) mp.m[n] = metrics[n];
+        mp.J = jac;
+        F3D_CUDA(ctx, launch_metric_prep32(ctx->dp, mp, ctx->m32, (cudaStream_t)stream));
+    } else {
+        F3D_CUDA(ctx, launch_metric_prep(ctx->dp, ctx->m, ctx->S, ctx->Ah, (cudaStream_t)stream));
+    }
     ctx->metrics_set = true;
     return F3D_OK;
 }
@@ -411,10 +499,14 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
     if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
     if (nsteps < 0) return fail(ctx, F3D_ERR_ARG, "nsteps must be >= 0");
     cudaStream_t st = (cudaStream_t)stream;
+    // Mixed precision: Q's FP32 copy is made once here; afterwards every stage's primitive
+    // fill rewrites it, so the stages inside the step (and the graph) skip the conversion.
+    const bool mx = mixed(ctx);
+    if (mx && nsteps > 0) F3D_CUDA(ctx, launch_to_f32(Q, ctx->Q32, 6 * ctx->dp.plane, st));
     if (st == nullptr) {  // the legacy stream cannot be captured: plain launches
         for (int t = 0; t < nsteps; t++)
             for (int s = 1; s <= 3; s++)
-                if ((rc = run_stage(ctx, s, dt, U, Un, Q, st))) return rc;
+                if ((rc = run_stage(ctx, s, dt, U, Un, Q, st, mx))) return rc;
         return F3D_OK;
     }
     const void* key[4] = {U, Un, Q, st};
@@ -428,7 +520,7 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
         cudaGraph_t g;
         F3D_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         int src = F3D_OK;
-        for (int s = 1; s <= 3 && !src; s++) src = run_stage(ctx, s, dt, U, Un, Q, st);
+        for (int s = 1; s <= 3 && !src; s++) src = run_stage(ctx, s, dt, U, Un, Q, st, mx);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (src) return src;
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
@@ -512,6 +604,7 @@ int f3d_debug_split(f3d_ctx* ctx, int dir, const double* Q, double* Fp, double* 
     int rc = check_ctx(ctx, true);
     if (rc || (rc = check_ptrs(ctx, {Q, Fp, Fm}))) return rc;
     if (dir < 0 || dir > 2) return fail(ctx, F3D_ERR_ARG, "dir must be 0, 1 or 2");
+    if (mixed(ctx)) return fail(ctx, F3D_ERR_UNSUPPORTED, "stage intermediates are FP64-only");
     cudaStream_t st = (cudaStream_t)stream;
     F3D_CUDA(ctx, launch_sound(ctx->dp, Q, ctx->csnd, st));
     const double* A[3] = {ctx->m[3 * dir], ctx->m[3 * dir + 1], ctx->m[3 * dir + 2]};
@@ -526,9 +619,10 @@ int f3d_debug_face_flux(f3d_ctx* ctx, int dir, const double* Q, const double* ph
     if (dir < 0 || dir > 2) return fail(ctx, F3D_ERR_ARG, "dir must be 0, 1 or 2");
     const bool hybrid = ctx->dp.fixed_branch < 0;
     if (hybrid && !phi) return fail(ctx, F3D_ERR_ARG, "hybrid thresholds need phi");
+    if (mixed(ctx)) return fail(ctx, F3D_ERR_UNSUPPORTED, "stage intermediates are FP64-only");
     cudaStream_t st = (cudaStream_t)stream;
     F3D_CUDA(ctx, launch_sound(ctx->dp, Q, ctx->csnd, st));
-    SweepArgs a = sweep_args(ctx, dir, Q, hybrid ? phi : nullptr);
+    SweepArgs a = sweep_args(ctx, dir, Q, hybrid, phi);
     a.out_mode = OUT_FACES;
     a.faces = F;
     a.Fv = nullptr;
@@ -539,6 +633,7 @@ int f3d_debug_face_flux(f3d_ctx* ctx, int dir, const double* Q, const double* ph
 int f3d_debug_viscous(f3d_ctx* ctx, const double* Q, double* Fvx, double* Fvy, double* Fvz, f3d_stream stream) {
     int rc = check_ctx(ctx, true);
     if (rc || (rc = check_ptrs(ctx, {Q, Fvx, Fvy, Fvz}))) return rc;
+    if (mixed(ctx)) return fail(ctx, F3D_ERR_UNSUPPORTED, "stage intermediates are FP64-only");
     F3D_CUDA(ctx, launch_viscous(ctx->dp, Q, ctx->m, ctx->J, Fvx, Fvy, Fvz, (cudaStream_t)stream));
     return F3D_OK;
 }

@@ -21,6 +21,18 @@ struct BcDev {
     double t_wall;
 };
 
+// Gas and scheme constants in the arithmetic type of a kernel, derived once on the host.
+template <class R> struct Cst {
+    R gamma, grg, gm1, rg;
+    R inv_gm1;   // 1/(gamma-1)
+    R inv_2g;    // 1/(2 gamma)          (split.jl:54)
+    R two_gm1;   // 2 (gamma-1)          (split.jl:55)
+    R w2c;       // (3-gamma)/(2(gamma-1)) (split.jl:52)
+    R c_s, t_s, cp, pr;
+    R phi1, phi2, phi3;
+    R lin[7];
+};
+
 // Runtime constants of one context, passed to every kernel by value.
 struct DevParams {
     int nx, ny, nz;     // interior
@@ -33,9 +45,20 @@ struct DevParams {
     double phi1, phi2, phi3;
     double lin[7];       // run.jl:75-77
     int split, character, viscous;
+    int precision;       // F3D_PREC_FP64 or F3D_PREC_MIXED
     int fixed_branch;    // -1: per-face hybrid switch; 0..3: every face takes that branch
+    // FP64 sensor thresholds as bit patterns: for phi >= 0 (or NaN) the comparison
+    // phi < t of the reference equals bits(phi) < phib (thresholds <= 0 or NaN map to 0,
+    // which no phi is below), so the branch needs no FP64 instruction
+    unsigned long long phib[3];
+    Cst<double> cd;
+    Cst<float> cf;
     BcDev bc[6];
 };
+
+template <class R> __host__ __device__ inline const Cst<R>& cst(const DevParams& P);
+template <> __host__ __device__ inline const Cst<double>& cst<double>(const DevParams& P) { return P.cd; }
+template <> __host__ __device__ inline const Cst<float>& cst<float>(const DevParams& P) { return P.cf; }
 
 __host__ __device__ inline long long lin3(const DevParams& P, int i, int j, int k) {
     return (long long)i + (long long)P.nxt * ((long long)j + (long long)P.nyt * k);

@@ -5,32 +5,49 @@
 
 namespace f3d {
 
+// Sign split E+ = max(E,0), E- = min(E,0): equal to (E+|E|)/2 and E-(E+|E|)/2 of
+// split.jl:34-40 for every finite E. In FP64 the choice is made on the sign bit with
+// integer instructions, keeping it off the FP64 pipe.
+__device__ __forceinline__ void sign_split(double e, double& ep, double& em) {
+    const bool pos = __double2hiint(e) >= 0;
+    ep = pos ? e : 0.0;
+    em = pos ? 0.0 : e;
+}
+__device__ __forceinline__ void sign_split(float e, float& ep, float& em) {
+    ep = fmaxf(e, 0.f);
+    em = fminf(e, 0.f);
+}
+__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
+
 // Flux-vector splitting of one cell (split.jl). q = (rho,u,v,w,p,T); A = the J^-1-scaled
 // metric row of the sweep direction; Ah = A/|A| (precomputed as A*(1/|A|), split.jl:28-32);
-// ss = |A|; c = sound speed (precomputed: sqrt(gamma Rg T) for SW, split.jl:22;
-// sqrt(gamma p/rho) for LF/VL/AUSM, split.jl:90,130,205).
+// ss = |A|; c = sound speed (sqrt(gamma Rg T) for SW, split.jl:22; sqrt(gamma p/rho) for
+// LF/VL/AUSM, split.jl:90,130,205). Constant quotients such as 1/(2 gamma) and
+// (3-gamma)/(2(gamma-1)) come precomputed in K instead of being divided per cell.
 template <class R>
-__device__ __forceinline__ void split_cell(int method, R g, const R q[6], R c, R A1, R A2, R A3, R Ah1, R Ah2,
-                                           R Ah3, R ss, R fp[5], R fm[5]) {
+__device__ __forceinline__ void split_cell(int method, const Cst<R>& K, const R q[6], R c, R A1, R A2, R A3, R Ah1,
+                                           R Ah2, R Ah3, R ss, R fp[5], R fm[5]) {
     const R rho = q[0], u = q[1], v = q[2], w = q[3], p = q[4];
     const R half = R(0.5), one = R(1), two = R(2);
+    const R g = K.gamma;
     if (method == F3D_SPLIT_SW) {  // split.jl:2-68
         R E1 = A1 * u + A2 * v + A3 * w;
         R E2 = E1 - c * ss;
         R E3 = E1 + c * ss;
-        R E1P = (E1 + fabs(E1)) * half, E2P = (E2 + fabs(E2)) * half, E3P = (E3 + fabs(E3)) * half;
-        R E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
+        R E1P, E2P, E3P, E1M, E2M, E3M;
+        sign_split(E1, E1P, E1M);
+        sign_split(E2, E2P, E2M);
+        sign_split(E3, E3P, E3M);
         R uc1 = u - c * Ah1, uc2 = u + c * Ah1;
         R vc1 = v - c * Ah2, vc2 = v + c * Ah2;
         R wc1 = w - c * Ah3, wc2 = w + c * Ah3;
         R vvc1 = (uc1 * uc1 + vc1 * vc1 + wc1 * wc1) * half;
         R vvc2 = (uc2 * uc2 + vc2 * vc2 + wc2 * wc2) * half;
-        R gm1 = g - one;
-        R vv = gm1 * (u * u + v * v + w * w);
-        R W2 = (R(3) - g) / (two * gm1) * (c * c);
-        R t1 = rho / (two * g);
-        R t2 = two * gm1;
-        R a1 = t2 * E1P, b1 = t2 * E1M;
+        R vv = K.gm1 * (u * u + v * v + w * w);
+        R W2 = K.w2c * (c * c);
+        R t1 = rho * K.inv_2g;
+        R a1 = K.two_gm1 * E1P, b1 = K.two_gm1 * E1M;
         fp[0] = t1 * (a1 + E2P + E3P);
         fp[1] = t1 * (a1 * u + E2P * uc1 + E3P * uc2);
         fp[2] = t1 * (a1 * v + E2P * vc1 + E3P * vc2);
@@ -44,7 +61,7 @@ __device__ __forceinline__ void split_cell(int method, R g, const R q[6], R c, R
     } else if (method == F3D_SPLIT_LF) {  // split.jl:70-108
         R un = A1 * u + A2 * v + A3 * w;
         R l0 = fabs(un) + c * ss;
-        R E0 = p / (g - one) + half * rho * (u * u + v * v + w * w);
+        R E0 = p * K.inv_gm1 + half * rho * (u * u + v * v + w * w);
         R ru = rho * u, rv = rho * v, rw = rho * w;
         fp[0] = half * (rho * un + l0 * rho);
         fp[1] = half * (ru * un + A1 * p + l0 * ru);
@@ -60,13 +77,13 @@ __device__ __forceinline__ void split_cell(int method, R g, const R q[6], R c, R
         R un = A1 * u + A2 * v + A3 * w;
         R M = un / (c * ss);
         R kin = u * u + v * v + w * w;
-        R f4;  // energy flux coefficient of the supersonic state
+        R f4;  // energy flux of the supersonic state
         R h = R(0);
         if (method == F3D_SPLIT_VL) {
-            R E0 = p / (g - one) + half * rho * kin;
+            R E0 = p * K.inv_gm1 + half * rho * kin;
             f4 = (E0 + p) * un;
         } else {
-            h = g * p / (rho * (g - one)) + half * kin;
+            h = g * p / (rho * K.gm1) + half * kin;
             f4 = rho * h * un;
         }
         if (M <= R(-1) || M >= R(1)) {
@@ -88,12 +105,12 @@ __device__ __forceinline__ void split_cell(int method, R g, const R q[6], R c, R
             fp[1] = f1p * (A1 * t1 + u);
             fp[2] = f1p * (A2 * t1 + v);
             fp[3] = f1p * (A3 * t1 + w);
-            fp[4] = f1p * (sq((g - one) * unn + two * c) * t3 + t4);
+            fp[4] = f1p * (sq(K.gm1 * unn + two * c) * t3 + t4);
             fm[0] = f1m;
             fm[1] = f1m * (A1 * t2 + u);
             fm[2] = f1m * (A2 * t2 + v);
             fm[3] = f1m * (A3 * t2 + w);
-            fm[4] = f1m * (sq((g - one) * unn - two * c) * t3 + t4);
+            fm[4] = f1m * (sq(K.gm1 * unn - two * c) * t3 + t4);
         } else {
             R f_p = R(0.25) * sq(M + one) * rho * c * ss;
             R f_m = -R(0.25) * sq(M - one) * rho * c * ss;

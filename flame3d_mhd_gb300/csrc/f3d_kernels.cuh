@@ -11,18 +11,21 @@ constexpr int SWEEP_THREADS = 256;
 
 enum OutMode { OUT_SET = 0, OUT_ADD = 1, OUT_RHS = 2, OUT_STAGE = 3, OUT_FACES = 4 };
 
+// Arguments of one sweep. The field pointers are typed by the sweep's arithmetic: double
+// arrays for the FP64 form, float arrays (FP32 copies) for the mixed form (fp32 = 1).
+// J, U, Un, out and faces are double in both forms.
 struct SweepArgs {
     DevParams P;
-    const double* Q;      // primitive state (Nt^3 x 6), ghost-filled
-    const double* csnd;   // sound speed per cell for the split
-    const double* A[3];   // metric row of the sweep direction (J^-1 scaled)
-    const double* Ah[3];  // A * (1/|A|)
-    const double* S;      // |A|
-    const double* phi;    // shock sensor (only read when P.fixed_branch < 0)
-    const double* Fv;     // viscous flux of this direction ((Nt-4)^3 x 4) or null
+    const void* Q;        // primitive state (Nt^3 x 6), ghost-filled
+    const void* csnd;     // FP64 form: sound speed per cell for the split
+    const void* A[3];     // metric row of the sweep direction (J^-1 scaled)
+    const void* Ah[3];    // A * (1/|A|)
+    const void* S;        // |A|
+    const void* phi;      // shock sensor (only read when P.fixed_branch < 0)
+    const void* Fv;       // viscous flux of this direction ((Nt-4)^3 x 4) or null
     const double* J;      // Jacobian
-    double* acc;          // RHS accumulator (U layout)
-    double* out;          // OUT_RHS destination (may alias acc)
+    void* acc;            // RHS accumulator (U layout)
+    double* out;          // OUT_RHS destination (may alias acc in the FP64 form)
     double* U;            // OUT_STAGE state, updated in place
     double* Un;           // OUT_STAGE stage-start copy
     double* faces;        // OUT_FACES destination (Fx/Fy/Fz shape) or null
@@ -30,6 +33,7 @@ struct SweepArgs {
     int out_mode;
     int combine;
     int stage1_copy;      // OUT_STAGE of stage 1: Un = U before the update
+    int fp32;             // 1: the mixed-precision (FP32) sweep
 };
 
 // parameter validation and device constants (api.cu)
@@ -39,12 +43,27 @@ DevParams make_dev_params(const f3d_params& p);
 cudaError_t sweep_configure();
 cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st);
 
+// metric pointer bundles (passed by value to kernels)
+struct MetricPtrs {
+    const double* m[9];
+    const double* J;
+};
+struct MetricPtrs32 {
+    float* A[9];
+    float* H[9];
+    float* S[3];
+    float* J;
+};
+
 // pointwise / stencil kernels (k_pointwise.cu)
 // Q at every cell from the interior of U (c2Prim) or of Q itself (from_q), with the
 // ghost layers produced by the composed boundary rules. U ghosts are written when
 // U_ghost_out is not null. csnd (optional) receives the split's sound speed.
 cudaError_t launch_prim_fill(const DevParams& P, const double* U, double* Q, double* U_ghost_out, double* csnd,
-                             int from_q, cudaStream_t st);
+                             int from_q, cudaStream_t st, float* Q32 = nullptr);
+cudaError_t launch_to_f32(const double* src, float* dst, long long n, cudaStream_t st);
+cudaError_t launch_sensor32(const DevParams& P, const float* Q32, float* phi, cudaStream_t st);
+cudaError_t launch_metric_prep32(const DevParams& P, const MetricPtrs& m, const MetricPtrs32& o, cudaStream_t st);
 cudaError_t launch_c2prim_interior(const DevParams& P, const double* U, double* Q, cudaStream_t st);
 cudaError_t launch_prim2c(const DevParams& P, const double* Q, double* U, cudaStream_t st);
 cudaError_t launch_lincomb(const DevParams& P, double* U, const double* Un, double a, double b, cudaStream_t st);
@@ -61,9 +80,11 @@ cudaError_t launch_check_finite(const DevParams& P, const double* U, int* flag, 
 cudaError_t launch_cfl(const DevParams& P, const double* Q, const double* const m[9], const double* J, double cfl,
                        unsigned long long* dtbits, cudaStream_t st);
 
-// viscous fluxes (k_viscous.cu)
+// viscous fluxes (k_viscous.cu): FP64 from the FP64 arrays, or FP32 from the FP32 copies
 cudaError_t launch_viscous(const DevParams& P, const double* Q, const double* const m[9], const double* J,
                            double* Fvx, double* Fvy, double* Fvz, cudaStream_t st);
+cudaError_t launch_viscous32(const DevParams& P, const float* Q, const float* const m[9], const float* J,
+                             float* Fvx, float* Fvy, float* Fvz, cudaStream_t st);
 
 // metrics from coordinates (k_metrics.cu)
 cudaError_t launch_metrics(const DevParams& P, const double* x, const double* y, const double* z,

@@ -31,7 +31,8 @@ __device__ __forceinline__ double sound_speed(const DevParams& P, const double q
 // c2Prim at interior cells and the composed ghost rules everywhere else, in one pass.
 // A ghost cell recomputes c2Prim at its interior source cell, which is bitwise what
 // c2Prim followed by the reference's copies produces.
-__global__ void k_prim_fill(const DevParams P, const double* U, double* Q, double* Ug, double* csnd, int from_q) {
+__global__ void k_prim_fill(const DevParams P, const double* U, double* Q, double* Ug, double* csnd, float* Q32,
+                            int from_q) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
     const long long pl = P.plane;
@@ -40,7 +41,7 @@ __global__ void k_prim_fill(const DevParams P, const double* U, double* Q, doubl
     double q[6];
     if (is_interior(P, i, j, k)) {
         if (from_q) {
-            if (!csnd) return;
+            if (!csnd && !Q32) return;
 #pragma unroll
             for (int n = 0; n < 6; n++) q[n] = Q[c + n * pl];
         } else {
@@ -81,11 +82,74 @@ __global__ void k_prim_fill(const DevParams P, const double* U, double* Q, doubl
         }
     }
     if (csnd) csnd[c] = sound_speed(P, q);
+    if (Q32) {
+#pragma unroll
+        for (int n = 0; n < 6; n++) Q32[c + n * pl] = (float)q[n];
+    }
 }
 
 cudaError_t launch_prim_fill(const DevParams& P, const double* U, double* Q, double* Ug, double* csnd, int from_q,
-                             cudaStream_t st) {
-    k_prim_fill<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, U, Q, Ug, csnd, from_q);
+                             cudaStream_t st, float* Q32) {
+    k_prim_fill<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, U, Q, Ug, csnd, Q32, from_q);
+    return cudaGetLastError();
+}
+
+// FP32 copy of an FP64 array (n elements): the mixed form's view of Q.
+__global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+    long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+    if (i + 1 < n) {
+        const double2 v = *reinterpret_cast<const double2*>(src + i);
+        *reinterpret_cast<float2*>(dst + i) = make_float2((float)v.x, (float)v.y);
+    } else if (i < n) {
+        dst[i] = (float)src[i];
+    }
+}
+cudaError_t launch_to_f32(const double* src, float* dst, long long n, cudaStream_t st) {
+    const long long pairs = (n + 1) / 2;
+    k_to_f32<<<pw_blocks(pairs), PW_THREADS, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+// Shock sensor of the mixed form: the same formula (schemes.jl:1-24) on the FP32 pressure.
+__global__ void k_sensor32(const DevParams P, const float* Q32, float* phi) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.plane) return;
+    int i, j, k;
+    cell_ijk(P, c, i, j, k);
+    if (i < 1 || i > P.nxt - 2 || j < 1 || j > P.nyt - 2 || k < 1 || k > P.nzt - 2) return;
+    const float* p = Q32 + 4 * P.plane;
+    const long long sy = P.nxt, sz = (long long)P.nxt * P.nyt;
+    const float pc = p[c];
+    auto term = [](float a, float b, float d) { return fabsf(-a + 2.f * b - d) / (a + 2.f * b + d); };
+    phi[c] = term(p[c - 1], pc, p[c + 1]) + term(p[c - sy], pc, p[c + sy]) + term(p[c - sz], pc, p[c + sz]);
+}
+cudaError_t launch_sensor32(const DevParams& P, const float* Q32, float* phi, cudaStream_t st) {
+    k_sensor32<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, Q32, phi);
+    return cudaGetLastError();
+}
+
+// FP32 copies of the metrics, |A_d|, A_d/|A_d| and J for the mixed form; |A_d| and A_d/|A_d|
+// are formed in FP64 (the metric computation stays FP64) and rounded once.
+__global__ void k_metric_prep32(const DevParams P, MetricPtrs m, MetricPtrs32 o) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.plane) return;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const double a = m.m[3 * d][c], b = m.m[3 * d + 1][c], e = m.m[3 * d + 2][c];
+        const double s = sqrt(a * a + b * b + e * e);
+        const double si = 1.0 / s;
+        o.S[d][c] = (float)s;
+        o.A[3 * d][c] = (float)a;
+        o.A[3 * d + 1][c] = (float)b;
+        o.A[3 * d + 2][c] = (float)e;
+        o.H[3 * d][c] = (float)(a * si);
+        o.H[3 * d + 1][c] = (float)(b * si);
+        o.H[3 * d + 2][c] = (float)(e * si);
+    }
+    o.J[c] = (float)m.J[c];
+}
+cudaError_t launch_metric_prep32(const DevParams& P, const MetricPtrs& m, const MetricPtrs32& o, cudaStream_t st) {
+    k_metric_prep32<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, m, o);
     return cudaGetLastError();
 }
 
@@ -220,7 +284,7 @@ __global__ void k_split_debug(const DevParams P, const double* Q, const double* 
     double q[6], fp[5], fm[5];
 #pragma unroll
     for (int n = 0; n < 6; n++) q[n] = Q[c + n * P.plane];
-    split_cell<double>(P.split, P.gamma, q, csnd[c], A0[c], A1[c], A2[c], H0[c], H1[c], H2[c], S[c], fp, fm);
+    split_cell<double>(P.split, P.cd, q, csnd[c], A0[c], A1[c], A2[c], H0[c], H1[c], H2[c], S[c], fp, fm);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
         Fp[c + n * P.plane] = fp[n];

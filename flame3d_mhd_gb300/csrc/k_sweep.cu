@@ -35,9 +35,10 @@ template <int DIR, class R> constexpr size_t sweep_smem_bytes(bool hybrid) {
 template <bool CHAR, class R, class FPA, class FMA>
 __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a, int br, int p0, R s0,
                                           long long cl, long long cr, FPA FP, FMA FM, R out[5]) {
+    const Cst<R>& K = cst<R>(P);
     if (br == 0) {  // UP7, schemes.jl:119-142
-        const R c1 = R(P.lin[0]), c2 = R(P.lin[1]), c3 = R(P.lin[2]), c4 = R(P.lin[3]), c5 = R(P.lin[4]),
-                c6 = R(P.lin[5]), c7 = R(P.lin[6]);
+        const R c1 = K.lin[0], c2 = K.lin[1], c3 = K.lin[2], c4 = K.lin[3], c5 = K.lin[4], c6 = K.lin[5],
+                c7 = K.lin[6];
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             R fp = c1 * FP(n, p0) + c2 * FP(n, p0 + 1) + c3 * FP(n, p0 + 2) + c4 * FP(n, p0 + 3) +
@@ -78,22 +79,26 @@ __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a
     // characteristic-wise, schemes.jl:756-999: eigenvectors of the face from the arithmetic
     // mean of u,v,w,T and of the metric row at the two adjacent cells.
     const long long pl = P.plane;
-    const R u = R(0.5) * (R(a.Q[cr + pl]) + R(a.Q[cl + pl]));
-    const R v = R(0.5) * (R(a.Q[cr + 2 * pl]) + R(a.Q[cl + 2 * pl]));
-    const R w = R(0.5) * (R(a.Q[cr + 3 * pl]) + R(a.Q[cl + 3 * pl]));
-    const R T = R(0.5) * (R(a.Q[cr + 5 * pl]) + R(a.Q[cl + 5 * pl]));
-    const R A1 = (R(a.A[0][cr]) + R(a.A[0][cl])) * R(0.5);
-    const R A2 = (R(a.A[1][cr]) + R(a.A[1][cl])) * R(0.5);
-    const R A3 = (R(a.A[2][cr]) + R(a.A[2][cl])) * R(0.5);
+    const R* Qr = static_cast<const R*>(a.Q);
+    const R* A0 = static_cast<const R*>(a.A[0]);
+    const R* A1p = static_cast<const R*>(a.A[1]);
+    const R* A2p = static_cast<const R*>(a.A[2]);
+    const R u = R(0.5) * (Qr[cr + pl] + Qr[cl + pl]);
+    const R v = R(0.5) * (Qr[cr + 2 * pl] + Qr[cl + 2 * pl]);
+    const R w = R(0.5) * (Qr[cr + 3 * pl] + Qr[cl + 3 * pl]);
+    const R T = R(0.5) * (Qr[cr + 5 * pl] + Qr[cl + 5 * pl]);
+    const R A1 = (A0[cr] + A0[cl]) * R(0.5);
+    const R A2 = (A1p[cr] + A1p[cl]) * R(0.5);
+    const R A3 = (A2p[cr] + A2p[cl]) * R(0.5);
     const R nx = A1 * s0, ny = A2 * s0, nz = A3 * s0;
     R lx, ly, lz;
     if (fabs(nz) <= fabs(ny)) {
-        R ss = rsqrt(nx * nx + ny * ny);
+        R ss = rsq(nx * nx + ny * ny);
         lx = -ny * ss;
         ly = nx * ss;
         lz = R(0);
     } else {
-        R ss = rsqrt(nx * nx + nz * nz);
+        R ss = rsq(nx * nx + nz * nz);
         lx = -nz * ss;
         ly = R(0);
         lz = nx * ss;
@@ -103,19 +108,19 @@ __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a
     const R ql = u * lx + v * ly + w * lz;
     const R qm = u * mx + v * my + w * mz;
     const R q2 = R(0.5) * (u * u + v * v + w * w);
-    const R gT = R(P.grg) * T;
-    const R rc = rsqrt(gT);         // 1/c
-    const R c = gT * rc;            // c = sqrt(gamma Rg T)
-    const R c2 = R(0.5) * rc;       // 1/(2c)
-    const R K = R(P.gm1) * (rc * rc);  // (gamma-1)/c^2
-    const R K2 = K * R(0.5);
-    const R H = gT / R(P.gm1) + q2;    // 1/K + q2
+    const R gT = K.grg * T;
+    const R rc = rsq(gT);              // 1/c
+    const R c = gT * rc;               // c = sqrt(gamma Rg T)
+    const R c2 = R(0.5) * rc;          // 1/(2c)
+    const R Kc = K.gm1 * (rc * rc);    // (gamma-1)/c^2
+    const R K2 = Kc * R(0.5);
+    const R H = gT * K.inv_gm1 + q2;   // 1/K + q2
     R flux[5];
 #pragma unroll 1
     for (int n = 0; n < 5; n++) {
         R l0, l1, l2, l3, l4;  // row n of L
         if (n == 0) { l0 = K2 * q2 + qn * c2; l1 = -(K2 * u + nx * c2); l2 = -(K2 * v + ny * c2); l3 = -(K2 * w + nz * c2); l4 = K2; }
-        else if (n == 1) { l0 = R(1) - K * q2; l1 = K * u; l2 = K * v; l3 = K * w; l4 = -K; }
+        else if (n == 1) { l0 = R(1) - Kc * q2; l1 = Kc * u; l2 = Kc * v; l3 = Kc * w; l4 = -Kc; }
         else if (n == 2) { l0 = K2 * q2 - qn * c2; l1 = -(K2 * u - nx * c2); l2 = -(K2 * v - ny * c2); l3 = -(K2 * w - nz * c2); l4 = K2; }
         else if (n == 3) { l0 = -ql; l1 = lx; l2 = ly; l3 = lz; l4 = R(0); }
         else { l0 = -qm; l1 = mx; l2 = my; l3 = mz; l4 = R(0); }
@@ -144,9 +149,41 @@ __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a
     out[4] = flux[0] * (H - qn * c) + flux[1] * q2 + flux[2] * (H + qn * c) + flux[3] * ql + flux[4] * qm;
 }
 
-template <int DIR, bool CHAR>
+// Branch of a face from the sensor values of cells i-3..i+2 (schemes.jl:112-117 and
+// :119, :143, :231): the FP64 values compare as bit patterns (see DevParams::phib), FP32
+// values directly. NaN fails every comparison and selects NND2, like the reference.
+__device__ __forceinline__ int branch_of(const DevParams& P, const double* ph) {
+    unsigned long long m = __double_as_longlong(ph[0]);
+#pragma unroll
+    for (int o = 1; o < 6; o++) {
+        unsigned long long b = __double_as_longlong(ph[o]);
+        m = b > m ? b : m;
+    }
+    return m < P.phib[0] ? 0 : (m < P.phib[1] ? 1 : (m < P.phib[2] ? 2 : 3));
+}
+__device__ __forceinline__ int branch_of(const DevParams& P, const float* ph) {
+    float m = ph[0];
+#pragma unroll
+    for (int o = 1; o < 6; o++) m = fmaxf(m, ph[o]);
+    const Cst<float>& K = P.cf;
+    int br = m < K.phi1 ? 0 : (m < K.phi2 ? 1 : (m < K.phi3 ? 2 : 3));
+    return m != m ? 3 : br;
+}
+
+// Sound speed for the split: precomputed per cell in FP64; computed in place in FP32.
+template <class R> __device__ __forceinline__ R split_sound(const DevParams& P, const SweepArgs& a, long long c,
+                                                            const R q[6]);
+template <> __device__ __forceinline__ double split_sound<double>(const DevParams&, const SweepArgs& a, long long c,
+                                                                  const double*) {
+    return static_cast<const double*>(a.csnd)[c];
+}
+template <> __device__ __forceinline__ float split_sound<float>(const DevParams& P, const SweepArgs&, long long,
+                                                                const float* q) {
+    return P.split == F3D_SPLIT_SW ? sqrtf(P.cf.grg * q[5]) : sqrtf(P.cf.gamma * q[4] / q[0]);
+}
+
+template <int DIR, bool CHAR, class R>
 __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
-    using R = double;
     constexpr int TL = Tile<DIR>::TL, TC = Tile<DIR>::TC, NP = TC + 8, NF = TC + 1;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;
@@ -155,6 +192,12 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
     R* sFm = sFp + 5 * TL * NP;
     R* sF = sFm + 5 * TL * NP;
     R* sPhi = sF + 5 * TL * NF;
+    const R* Qr = static_cast<const R*>(a.Q);
+    const R* Ar[3] = {static_cast<const R*>(a.A[0]), static_cast<const R*>(a.A[1]), static_cast<const R*>(a.A[2])};
+    const R* Hr[3] = {static_cast<const R*>(a.Ah[0]), static_cast<const R*>(a.Ah[1]),
+                      static_cast<const R*>(a.Ah[2])};
+    const R* Sr = static_cast<const R*>(a.S);
+    const R* Phr = static_cast<const R*>(a.phi);
 
     // tile geometry: interior start c0 along d, first line l0 and line count
     const int Nd = DIR == 0 ? P.nx : (DIR == 1 ? P.ny : P.nz);
@@ -184,17 +227,17 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
         const long long c = cell(l, c0 + p);
         R q[6];
 #pragma unroll
-        for (int n = 0; n < 6; n++) q[n] = a.Q[c + n * pl];
+        for (int n = 0; n < 6; n++) q[n] = Qr[c + n * pl];
         R fp[5], fm[5];
-        split_cell<R>(P.split, R(P.gamma), q, a.csnd[c], a.A[0][c], a.A[1][c], a.A[2][c], a.Ah[0][c], a.Ah[1][c],
-                      a.Ah[2][c], a.S[c], fp, fm);
+        split_cell<R>(P.split, cst<R>(P), q, split_sound<R>(P, a, c, q), Ar[0][c], Ar[1][c], Ar[2][c], Hr[0][c],
+                      Hr[1][c], Hr[2][c], Sr[c], fp, fm);
         const int s = sidx(l, p);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             sFp[n * TL * NP + s] = fp[n];
             sFm[n * TL * NP + s] = fm[n];
         }
-        if (hybrid) sPhi[s] = a.phi[c];
+        if (hybrid) sPhi[s] = Phr[c];
     }
     __syncthreads();
 
@@ -204,17 +247,16 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
         if (DIR == 0) { l = it / NF; t = it - l * NF; } else { t = it / TL; l = it - t * TL; }
         if (l >= nl || t > nc) continue;
         int br = P.fixed_branch;
-        if (hybrid) {  // Jameson sensor max over cells i-3..i+2, schemes.jl:112-117
-            R pm = sPhi[sidx(l, t + 1)];
+        if (hybrid) {
+            R ph[6];
 #pragma unroll
-            for (int o = 2; o <= 6; o++) pm = fmax(pm, sPhi[sidx(l, t + o)]);
-            br = pm < R(P.phi1) ? 0 : (pm < R(P.phi2) ? 1 : (pm < R(P.phi3) ? 2 : 3));
-            if (pm != pm) br = 3;  // NaN fails every comparison in the reference
+            for (int o = 0; o < 6; o++) ph[o] = sPhi[sidx(l, t + 1 + o)];
+            br = branch_of(P, ph);
         }
         const long long cl = cell(l, c0 + t + 3), cr = cl + stride;
         R out[5];
         R s0 = R(0);
-        if (br == 1 || br == 2) s0 = R(2) / (a.S[cl] + a.S[cr]);
+        if (br == 1 || br == 2) s0 = R(2) / (Sr[cl] + Sr[cr]);
         auto FP = [&](int n, int p) { return sFp[n * TL * NP + sidx(l, p)]; };
         auto FM = [&](int n, int p) { return sFm[n * TL * NP + sidx(l, p)]; };
         face_flux<CHAR, R>(P, a, br, t, s0, cl, cr, FP, FM, out);
@@ -229,7 +271,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
             else { fi = l0 + l; fj = other; fk = c0 + t; }
             const long long fo = fi + fx * (fj + fy * fk), nf = fx * fy * fz;
 #pragma unroll
-            for (int n = 0; n < 5; n++) a.faces[fo + n * nf] = out[n];
+            for (int n = 0; n < 5; n++) a.faces[fo + n * nf] = (double)out[n];
         }
     }
     if (a.out_mode == OUT_FACES) return;
@@ -238,6 +280,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
     // ---- Phase C: cells t = 0..nc-1 (full position c0 + t + NG).
     const int vxt = P.nxt - 4, vyt = P.nyt - 4, vzt = P.nzt - 4;
     const long long vplane = (long long)vxt * vyt * vzt;
+    R* acc = static_cast<R*>(a.acc);
+    const R* Fvr = static_cast<const R*>(a.Fv);
     for (int it = threadIdx.x; it < TL * TC; it += SWEEP_THREADS) {
         int l, t;
         if (DIR == 0) { l = it / TC; t = it - l * TC; } else { t = it / TL; l = it - t * TL; }
@@ -246,7 +290,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
         R d[5];
 #pragma unroll
         for (int n = 0; n < 5; n++) d[n] = sF[n * TL * NF + fidx(l, t)] - sF[n * TL * NF + fidx(l, t + 1)];
-        if (a.Fv) {
+        if (Fvr) {
             // Fv index = full index - 2 in every dimension (viscous.jl:119, div.jl:14-39)
             long long vi, vj, vk;
             const int g = c0 + t + NG - 2;
@@ -258,27 +302,27 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
             const R k1 = R(1) / R(12), k2 = R(-2) / R(3);
 #pragma unroll
             for (int n = 0; n < 4; n++) {
-                const R* F = a.Fv + n * vplane + vc;
+                const R* F = Fvr + n * vplane + vc;
                 d[n + 1] += k1 * (F[-2 * vs] - F[2 * vs]) + k2 * (F[-vs] - F[vs]);
             }
         }
         if (a.out_mode == OUT_SET) {
 #pragma unroll
-            for (int n = 0; n < 5; n++) a.acc[c + n * pl] = d[n];
+            for (int n = 0; n < 5; n++) acc[c + n * pl] = d[n];
         } else if (a.out_mode == OUT_ADD) {
 #pragma unroll
-            for (int n = 0; n < 5; n++) a.acc[c + n * pl] += d[n];
+            for (int n = 0; n < 5; n++) acc[c + n * pl] += d[n];
         } else if (a.out_mode == OUT_RHS) {
-            const R Jc = a.J[c];
+            const double Jc = a.J[c];
 #pragma unroll
-            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * (a.acc[c + n * pl] + d[n]);
-        } else {  // OUT_STAGE
-            const R Jact = a.J[c] * a.dt;
+            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * (double)(acc[c + n * pl] + d[n]);
+        } else {  // OUT_STAGE: RK state accumulation in FP64
+            const double Jact = a.J[c] * a.dt;
 #pragma unroll
             for (int n = 0; n < 5; n++) {
-                const R u = a.U[c + n * pl];
+                const double u = a.U[c + n * pl];
                 if (a.stage1_copy) a.Un[c + n * pl] = u;
-                R un = u + (a.acc[c + n * pl] + d[n]) * Jact;
+                double un = u + (double)(acc[c + n * pl] + d[n]) * Jact;
                 if (a.combine) un = un * a.ca + a.Un[c + n * pl] * a.cb;
                 a.U[c + n * pl] = un;
             }
@@ -286,40 +330,49 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
     }
 }
 
-template <int DIR, bool CHAR> static cudaError_t configure_dir() {
-    return cudaFuncSetAttribute(k_sweep<DIR, CHAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sweep_smem_bytes<DIR, double>(true));
+template <int DIR, bool CHAR, class R> static cudaError_t configure_dir() {
+    return cudaFuncSetAttribute(k_sweep<DIR, CHAR, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sweep_smem_bytes<DIR, R>(true));
+}
+
+template <class R> static cudaError_t configure_type() {
+    cudaError_t e;
+    if ((e = configure_dir<0, false, R>()) != cudaSuccess) return e;
+    if ((e = configure_dir<0, true, R>()) != cudaSuccess) return e;
+    if ((e = configure_dir<1, false, R>()) != cudaSuccess) return e;
+    if ((e = configure_dir<1, true, R>()) != cudaSuccess) return e;
+    if ((e = configure_dir<2, false, R>()) != cudaSuccess) return e;
+    return configure_dir<2, true, R>();
 }
 
 // Dynamic shared memory above 48 KB must be enabled per kernel before the first launch
 // (and outside stream capture): called from f3d_create.
 cudaError_t sweep_configure() {
-    cudaError_t e;
-    if ((e = configure_dir<0, false>()) != cudaSuccess) return e;
-    if ((e = configure_dir<0, true>()) != cudaSuccess) return e;
-    if ((e = configure_dir<1, false>()) != cudaSuccess) return e;
-    if ((e = configure_dir<1, true>()) != cudaSuccess) return e;
-    if ((e = configure_dir<2, false>()) != cudaSuccess) return e;
-    return configure_dir<2, true>();
+    cudaError_t e = configure_type<double>();
+    return e != cudaSuccess ? e : configure_type<float>();
 }
 
-template <int DIR, bool CHAR> static cudaError_t launch_dir(const SweepArgs& a, cudaStream_t st) {
+template <int DIR, bool CHAR, class R> static cudaError_t launch_dir(const SweepArgs& a, cudaStream_t st) {
     constexpr int TL = Tile<DIR>::TL, TC = Tile<DIR>::TC;
     const DevParams& P = a.P;
-    const size_t smem = sweep_smem_bytes<DIR, double>(true);
+    const size_t smem = sweep_smem_bytes<DIR, R>(true);
     dim3 grid;
     if (DIR == 0) grid = dim3(cdiv(P.nx, TC), cdiv(P.ny, TL), P.nz);
     else if (DIR == 1) grid = dim3(cdiv(P.nx, TL), cdiv(P.ny, TC), P.nz);
     else grid = dim3(cdiv(P.nx, TL), cdiv(P.nz, TC), P.ny);
-    k_sweep<DIR, CHAR><<<grid, SWEEP_THREADS, smem, st>>>(a);
+    k_sweep<DIR, CHAR, R><<<grid, SWEEP_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st) {
+template <class R> static cudaError_t launch_typed(int dir, const SweepArgs& a, cudaStream_t st) {
     const bool ch = a.P.character != 0;
-    if (dir == 0) return ch ? launch_dir<0, true>(a, st) : launch_dir<0, false>(a, st);
-    if (dir == 1) return ch ? launch_dir<1, true>(a, st) : launch_dir<1, false>(a, st);
-    return ch ? launch_dir<2, true>(a, st) : launch_dir<2, false>(a, st);
+    if (dir == 0) return ch ? launch_dir<0, true, R>(a, st) : launch_dir<0, false, R>(a, st);
+    if (dir == 1) return ch ? launch_dir<1, true, R>(a, st) : launch_dir<1, false, R>(a, st);
+    return ch ? launch_dir<2, true, R>(a, st) : launch_dir<2, false, R>(a, st);
+}
+
+cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st) {
+    return a.fp32 ? launch_typed<float>(dir, a, st) : launch_typed<double>(dir, a, st);
 }
 
 }  // namespace f3d

@@ -67,6 +67,10 @@ extern "C" int f3d_rhs_noalloc(const f3d_params* p, const double* const metrics[
         std::fprintf(stderr, "f3d_rhs_noalloc: %s\n", why.c_str());
         return rc;
     }
+    if (p->precision != F3D_PREC_FP64) {
+        std::fprintf(stderr, "f3d_rhs_noalloc: only the FP64 form is available without a context\n");
+        return F3D_ERR_UNSUPPORTED;
+    }
     for (int n = 0; n < 9; n++)
         if (!aligned16(metrics[n])) return F3D_ERR_ALIGN;
     if (!aligned16(jac) || !aligned16(Q) || !aligned16(dUdt)) return F3D_ERR_ALIGN;
