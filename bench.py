@@ -192,6 +192,51 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_cost(args, n: int = 128, steps: int = 4) -> dict:
+    """Adjoint / forward cost of one SSP-RK3 step on the viscous curvilinear Taylor-Green
+    vortex (128^3, Re 1600, Mach 0.1, FP64, component-wise hybrid): the adjoint step
+    recomputes two stage states and applies three RHS VJPs (f3d_rk3_step_vjp)."""
+    import numpy as np
+    import torch
+
+    from flame3d_mhd_gb300 import cases
+    from flame3d_mhd_gb300.solver import Flame3D
+    c = cases.tgv_viscous_curvilinear(n)
+    P = c["params"]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    s = Flame3D(P)
+    ms, J = s.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
+    s.set_metrics(ms, J)
+    Q = dev(c["Q"])
+    U, Un = s.field(5), s.field(5)
+    s.prim2c(U, Q)
+    s.fillGhost(Q, U)
+    dt = c["dt"]
+    stream = torch.cuda.Stream()
+    Ub, Ub2 = torch.ones_like(U), s.field(5)
+    with torch.cuda.stream(stream):
+        s.time_step(U, Un, Q, dt, 2)
+        s.rk3_step_vjp(dt, U, Ub, Ub2)
+        stream.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        s.time_step(U, Un, Q, dt, steps)
+        e[1].record(stream)
+        e[2].record(stream)
+        for _ in range(steps):
+            s.rk3_step_vjp(dt, U, Ub, Ub2)
+        e[3].record(stream)
+        e[3].synchronize()
+    fwd = e[0].elapsed_time(e[1]) / steps
+    adj = e[2].elapsed_time(e[3]) / steps
+    s.close()
+    cells = n ** 3
+    return {"workload": f"tgv{n}^3 viscous, curvilinear amp 0.05, Re 1600, Mach 0.1, FP64, component-wise hybrid",
+            "forward_ms_per_step": fwd, "adjoint_ms_per_step": adj, "adjoint_over_forward": adj / fwd,
+            "forward_mcell_rhs_per_s": cells * 3 / (fwd / 1e3) / 1e6,
+            "adjoint_includes": "recompute of 2 stage states + 3 RHS VJPs per step"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -293,6 +338,7 @@ def run_ours(args):
              "shares": {k: round(v[0] / tot_m, 4) for k, v in sorted(prof_m.items())},
              "step_hbm_frac": STEP_BYTES_PER_CELL * cells / (ms_mixed / args.steps / 1e3) / 1e9 / load_peaks()["hbm_gbs"]}
     sm.close()
+    adjoint = adjoint_cost(args)
 
     # per-kernel device times of single steps (events between launches, outside the timed loop)
     prof = {}
@@ -355,6 +401,7 @@ def run_ours(args):
                           "frac": step_gbs / peaks["hbm_gbs"], "alg_bytes_per_cell_step": STEP_BYTES_PER_CELL},
         "mcell_updates_per_s": value / 3,
         "mixed": mixed,
+        "adjoint": adjoint,
         "clocks": clocks,
         "state_finite": bool(ok),
     }

@@ -120,6 +120,8 @@ def load() -> C.CDLL:
         "f3d_kernel_name": (C.c_char_p, [ip]),
         "f3d_profile_step": (ip, [vp, C.c_double, vp, vp, vp, vp, dp, C.POINTER(C.c_int)]),
         "f3d_rhs_noalloc": (ip, [P, vp * 9, vp, vp, vp, vp]),
+        "f3d_rhs_vjp": (ip, [vp, vp, vp, vp, vp]),
+        "f3d_rk3_step_vjp": (ip, [vp, C.c_double, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -135,7 +137,7 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_lincomb", "f3d_fill_ghosts", "f3d_rhs", "f3d_rk3_stage", "f3d_rk3_steps", "f3d_cfl_dt",
             "f3d_check_finite", "f3d_debug_sensor", "f3d_debug_split", "f3d_debug_face_flux",
             "f3d_debug_viscous", "f3d_div", "f3d_measure_pipes", "f3d_kernel_count", "f3d_kernel_name",
-            "f3d_profile_step", "f3d_rhs_noalloc"]
+            "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp"]
 
 
 class F3DError(RuntimeError):

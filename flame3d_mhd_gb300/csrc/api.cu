@@ -144,6 +144,10 @@ struct f3d_ctx {
     float* Fv32[3] = {};
     double* dscalar = nullptr;  // 8 bytes for reductions
     Prof* prof = nullptr;
+    // adjoint scratch, allocated by the first VJP call
+    void* adj_slab = nullptr;
+    double *Qs = nullptr, *Qb = nullptr, *Lt = nullptr, *U1 = nullptr, *U2 = nullptr, *Xb = nullptr, *Yb = nullptr;
+    double *Fvb[3] = {}, *gb = nullptr;
     // CUDA graph of one RK3 step, keyed by its arguments
     cudaGraphExec_t step_graph = nullptr;
     const void* g_key[4] = {};
@@ -302,6 +306,85 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
     return F3D_OK;
 }
 
+// ---- discrete adjoint ------------------------------------------------------------------
+int adjoint_supported(f3d_ctx* ctx) {
+    if (mixed(ctx)) return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for the FP64 form");
+    if (ctx->params.character) return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for component-wise reconstruction");
+    if (ctx->params.split_method != F3D_SPLIT_SW && ctx->params.split_method != F3D_SPLIT_LF)
+        return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for SW and LF splitting");
+    return F3D_OK;
+}
+
+int adjoint_alloc(f3d_ctx* ctx) {
+    if (ctx->adj_slab) return F3D_OK;
+    const size_t nc = (size_t)ctx->dp.plane;
+    const size_t nv = (size_t)(ctx->params.nx + 4) * (ctx->params.ny + 4) * (ctx->params.nz + 4);
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t b1 = up(nc * 8);
+    const size_t bv = up(nv * 8);
+    size_t total = b1 * (6 + 6 + 5 * 5) + (ctx->params.viscous ? bv * (12 + 12) : 0);
+    cudaError_t e = cudaMalloc(&ctx->adj_slab, total);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc (adjoint scratch)");
+    char* q = (char*)ctx->adj_slab;
+    ctx->Qs = (double*)q; q += 6 * b1;
+    ctx->Qb = (double*)q; q += 6 * b1;
+    ctx->Lt = (double*)q; q += 5 * b1;
+    ctx->U1 = (double*)q; q += 5 * b1;
+    ctx->U2 = (double*)q; q += 5 * b1;
+    ctx->Xb = (double*)q; q += 5 * b1;
+    ctx->Yb = (double*)q; q += 5 * b1;
+    if (ctx->params.viscous) {
+        for (int d = 0; d < 3; d++) { ctx->Fvb[d] = (double*)q; q += 4 * bv; }
+        ctx->gb = (double*)q;
+    }
+    e = cudaMemset(ctx->adj_slab, 0, total);
+    if (e == cudaSuccess) e = adjoint_configure();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "adjoint set-up");
+    return F3D_OK;
+}
+
+// L(U) at interior cells into out (U layout): Q = c2Prim(U) + ghost fill into ctx->Qs
+int rhs_of_state(f3d_ctx* ctx, const double* U, double* out, cudaStream_t st) {
+    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, ctx->Qs, nullptr, nullptr, 0, st));
+    SweepArgs last;
+    std::memset(&last, 0, sizeof(last));
+    last.out_mode = OUT_RHS;
+    last.out = out;
+    return run_rhs(ctx, ctx->Qs, out, last, st);
+}
+
+// out = beta out + alpha (dL/dU)^T Lb at interior cells, for the state U
+int rhs_vjp_of_state(f3d_ctx* ctx, const double* U, const double* Lb, double* out, double alpha, double beta,
+                     cudaStream_t st) {
+    const DevParams& P = ctx->dp;
+    F3D_CUDA(ctx, launch_prim_fill(P, U, ctx->Qs, nullptr, ctx->csnd, 0, st));
+    const bool hybrid = P.fixed_branch < 0;
+    if (hybrid) F3D_CUDA(ctx, launch_sensor(P, ctx->Qs, ctx->phi, st));
+    F3D_CUDA(ctx, cudaMemsetAsync(ctx->Qb, 0, (size_t)P.plane * 6 * sizeof(double), st));
+    for (int d = 0; d < 3; d++) {
+        AdjArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.P = P;
+        a.Q = ctx->Qs;
+        a.csnd = ctx->csnd;
+        for (int n = 0; n < 3; n++) {
+            a.A[n] = ctx->m[3 * d + n];
+            a.Ah[n] = ctx->Ah[3 * d + n];
+        }
+        a.S = ctx->S[d];
+        a.phi = hybrid ? ctx->phi : nullptr;
+        a.J = ctx->J;
+        a.Lb = Lb;
+        a.Qb = ctx->Qb;
+        F3D_CUDA(ctx, launch_sweep_vjp(d, a, st));
+    }
+    if (ctx->params.viscous)
+        F3D_CUDA(ctx, launch_viscous_vjp(P, ctx->Qs, ctx->m, ctx->J, Lb, ctx->Fvb, ctx->gb, ctx->Qb, st));
+    F3D_CUDA(ctx, launch_fill_vjp(P, ctx->Qs, ctx->Qb, st));
+    F3D_CUDA(ctx, launch_c2prim_vjp(P, U, ctx->Qb, out, alpha, beta, st));
+    return F3D_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -403,6 +486,7 @@ int f3d_destroy(f3d_ctx* ctx) {
     if (!ctx) return F3D_OK;
     cudaSetDevice(ctx->device);
     if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
+    if (ctx->adj_slab) cudaFree(ctx->adj_slab);
     cudaError_t e = cudaFree(ctx->slab);
     delete ctx;
     return e == cudaSuccess ? F3D_OK : F3D_ERR_CUDA;
@@ -532,6 +616,47 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
     }
     for (int t = 0; t < nsteps; t++) F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
     return F3D_OK;
+}
+
+int f3d_rhs_vjp(f3d_ctx* ctx, const double* U, const double* Lbar, double* Ubar, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U, Lbar, Ubar}))) return rc;
+    if ((rc = adjoint_supported(ctx)) || (rc = adjoint_alloc(ctx))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    F3D_CUDA(ctx, cudaMemsetAsync(Ubar, 0, (size_t)ctx->dp.plane * 5 * sizeof(double), st));
+    return rhs_vjp_of_state(ctx, U, Lbar, Ubar, 1.0, 0.0, st);
+}
+
+// SSP-RK3 step U1 = U0 + dt L(U0), U2 = 3/4 U0 + 1/4 (U1 + dt L(U1)),
+// U3 = 1/3 U0 + 2/3 (U2 + dt L(U2)), with L(U) = RHS(ghost-filled c2Prim(U)); the stage
+// states are recomputed from U0, then the stages are reversed.
+int f3d_rk3_step_vjp(f3d_ctx* ctx, double dt, const double* U0, const double* Ubar_next, double* Ubar,
+                     f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U0, Ubar_next, Ubar}))) return rc;
+    if (Ubar == Ubar_next || Ubar == U0) return fail(ctx, F3D_ERR_ARG, "Ubar must not alias U0 or Ubar_next");
+    if ((rc = adjoint_supported(ctx)) || (rc = adjoint_alloc(ctx))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const DevParams& P = ctx->dp;
+    // forward recompute of the stage states
+    if ((rc = rhs_of_state(ctx, U0, ctx->Lt, st))) return rc;
+    F3D_CUDA(ctx, launch_axpby(P, ctx->U1, U0, 1.0, ctx->Lt, dt, st));
+    if ((rc = rhs_of_state(ctx, ctx->U1, ctx->Lt, st))) return rc;
+    F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U1, 0.25, ctx->Lt, 0.25 * dt, st));
+    F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U2, 1.0, U0, 0.75, st));
+    // stage 3: U3 = 1/3 U0 + 2/3 W, W = U2 + dt L(U2)
+    F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar_next, 1.0 / 3.0, nullptr, 0.0, st));
+    F3D_CUDA(ctx, launch_axpby(P, ctx->Xb, Ubar_next, 2.0 / 3.0, nullptr, 0.0, st));  // Wb
+    F3D_CUDA(ctx, launch_axpby(P, ctx->Yb, ctx->Xb, 1.0, nullptr, 0.0, st));          // U2b = Wb + dt J^T Wb
+    if ((rc = rhs_vjp_of_state(ctx, ctx->U2, ctx->Xb, ctx->Yb, dt, 1.0, st))) return rc;
+    // stage 2: U2 = 3/4 U0 + 1/4 V, V = U1 + dt L(U1)
+    F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar, 1.0, ctx->Yb, 0.75, st));
+    F3D_CUDA(ctx, launch_axpby(P, ctx->Xb, ctx->Yb, 0.25, nullptr, 0.0, st));  // Vb
+    F3D_CUDA(ctx, launch_axpby(P, ctx->Yb, ctx->Xb, 1.0, nullptr, 0.0, st));    // U1b = Vb + dt J^T Vb
+    if ((rc = rhs_vjp_of_state(ctx, ctx->U1, ctx->Xb, ctx->Yb, dt, 1.0, st))) return rc;
+    // stage 1: U1 = U0 + dt L(U0)
+    F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar, 1.0, ctx->Yb, 1.0, st));
+    return rhs_vjp_of_state(ctx, U0, ctx->Yb, Ubar, dt, 1.0, st);
 }
 
 int f3d_kernel_count(void) { return K_NKIND; }

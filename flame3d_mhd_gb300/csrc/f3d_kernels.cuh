@@ -36,6 +36,30 @@ struct SweepArgs {
     int fp32;             // 1: the mixed-precision (FP32) sweep
 };
 
+// Arguments of one sweep VJP (k_adjoint.cu, FP64, component-wise reconstruction)
+struct AdjArgs {
+    DevParams P;
+    const double* Q;      // forward primitive state, ghost-filled
+    const double* csnd;   // forward split sound speed
+    const double* A[3];
+    const double* Ah[3];
+    const double* S;
+    const double* phi;    // forward sensor (hybrid)
+    const double* J;
+    const double* Lb;     // cotangent of the RHS (U layout, interior cells)
+    double* Qb;           // accumulated cotangent of Q (6 x Nt^3)
+};
+
+cudaError_t adjoint_configure();
+cudaError_t launch_sweep_vjp(int dir, const AdjArgs& a, cudaStream_t st);
+cudaError_t launch_viscous_vjp(const DevParams& P, const double* Q, const double* const m[9], const double* J,
+                               const double* Lb, double* Fvb[3], double* gb, double* Qb, cudaStream_t st);
+cudaError_t launch_fill_vjp(const DevParams& P, const double* Q, double* Qb, cudaStream_t st);
+cudaError_t launch_c2prim_vjp(const DevParams& P, const double* U, const double* Qb, double* out, double alpha,
+                              double beta, cudaStream_t st);
+cudaError_t launch_axpby(const DevParams& P, double* out, const double* x, double a, const double* y, double b,
+                         cudaStream_t st);
+
 // parameter validation and device constants (api.cu)
 int validate_params(const f3d_params& p, std::string& why);
 DevParams make_dev_params(const f3d_params& p);

@@ -175,6 +175,32 @@ class Flame3D:
         self._check(self.lib.f3d_rk3_steps(self._h, nsteps, dt, self._ptr(U, 5), self._ptr(Un, 5),
                                            self._ptr(Q, 6), self._stream()))
 
+    # ---- discrete adjoint ----------------------------------------------------------
+    def rhs_vjp(self, U: torch.Tensor, Lbar: torch.Tensor, Ubar: torch.Tensor | None = None) -> torch.Tensor:
+        """(dL/dU)^T Lbar for L(U) = RHS(ghost-filled c2Prim(U)), interior cells."""
+        if Ubar is None:
+            Ubar = self.field(5)
+        self._check(self.lib.f3d_rhs_vjp(self._h, self._ptr(U, 5), self._ptr(Lbar, 5), self._ptr(Ubar, 5),
+                                         self._stream()))
+        return Ubar
+
+    def rk3_step_vjp(self, dt: float, U0: torch.Tensor, Ubar_next: torch.Tensor,
+                     Ubar: torch.Tensor | None = None) -> torch.Tensor:
+        """Cotangent of the state at the start of one SSP-RK3 step from the one at its end."""
+        if Ubar is None:
+            Ubar = self.field(5)
+        self._check(self.lib.f3d_rk3_step_vjp(self._h, dt, self._ptr(U0, 5), self._ptr(Ubar_next, 5),
+                                              self._ptr(Ubar, 5), self._stream()))
+        return Ubar
+
+    def q_from_u(self, U: torch.Tensor, Q: torch.Tensor | None = None) -> torch.Tensor:
+        """Q = c2Prim(U) with its ghost layers (and U's) filled: the stage input of solver.jl."""
+        if Q is None:
+            Q = self.field(6)
+        self.c2Prim(U, Q)
+        self.fillGhost(Q, U)
+        return Q
+
     def profile_step(self, U, Un, Q, dt: float) -> dict:
         """One RK3 step with per-launch CUDA events: {kernel name: (ms, launches)}."""
         n = self.lib.f3d_kernel_count()

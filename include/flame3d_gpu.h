@@ -190,6 +190,23 @@ int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream);
 int f3d_rhs_noalloc(const f3d_params* p, const double* const metrics[9], const double* jac,
                     const double* Q, double* dUdt, f3d_stream stream);
 
+/* ---- discrete adjoint (FP64, component-wise reconstruction, SW or LF splitting) ---- */
+
+/* Ubar = (dL/dU)^T Lbar at interior cells (ghost cells of Ubar are zeroed), where
+ * L(U) = RHS(ghost-filled c2Prim(U)) is the right-hand side as a function of the interior
+ * conserved state. Branches (hybrid scheme choice, minmod, sign splits, c2Prim clamps)
+ * are those of the forward state: the exact derivative of the scheme as evaluated.
+ * The first adjoint call of a context allocates its adjoint scratch. */
+int f3d_rhs_vjp(f3d_ctx* ctx, const double* U, const double* Lbar, double* Ubar, f3d_stream stream);
+
+/* Cotangent of the state at the start of one SSP-RK3 step from the cotangent of the state
+ * at its end: Ubar = (dU_{n+1}/dU_n)^T Ubar_next. Recomputes the two intermediate stage
+ * states from U0 (2 RHS) and applies three RHS VJPs. Ubar must not alias the inputs.
+ * Long trajectories use checkpoints of U every ~sqrt(N) steps and recompute each segment
+ * (flame3d_mhd_gb300/adjoint.py). */
+int f3d_rk3_step_vjp(f3d_ctx* ctx, double dt, const double* U0, const double* Ubar_next, double* Ubar,
+                     f3d_stream stream);
+
 /* ---- stage-by-stage intermediates in the reference's own array shapes ----------- */
 
 /* phi (Nxt,Nyt,Nzt) at cells 2..Nt-1, schemes.jl:1-24. */
