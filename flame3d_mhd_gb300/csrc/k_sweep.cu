@@ -25,7 +25,8 @@ template <> struct Tile<2> { static constexpr int TL = 16, TC = 32; };
 
 template <int DIR, class R> constexpr size_t sweep_smem_bytes(bool hybrid) {
     return sizeof(R) * ((size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 8) * (10 + (hybrid ? 1 : 0)) +
-                        (size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 1) * 5);
+                        (size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 1) * 5) +
+           sizeof(int) * (2 * (size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 1) + 4);
 }
 
 // Face flux of one face from the split fluxes of the 8 cells around it, positions
@@ -218,6 +219,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
     auto fidx = [&](int l, int t) { return DIR == 0 ? l * NF + t : t * TL + l; };
     const long long pl = P.plane;
 
+    if (threadIdx.x < 2) reinterpret_cast<int*>(sPhi + TL * NP)[2 * TL * NF + threadIdx.x] = 0;
     // ---- Phase A: split every cell the tile's stencils reach (positions 0..nc+7, full
     // index c0 + p along d).
     for (int it = threadIdx.x; it < TL * NP; it += SWEEP_THREADS) {
@@ -242,17 +244,11 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
     __syncthreads();
 
     // ---- Phase B: faces t = 0..nc (face t lies between positions t+3 and t+4).
-    for (int it = threadIdx.x; it < TL * NF; it += SWEEP_THREADS) {
-        int l, t;
-        if (DIR == 0) { l = it / NF; t = it - l * NF; } else { t = it / TL; l = it - t * TL; }
-        if (l >= nl || t > nc) continue;
-        int br = P.fixed_branch;
-        if (hybrid) {
-            R ph[6];
-#pragma unroll
-            for (int o = 0; o < 6; o++) ph[o] = sPhi[sidx(l, t + 1 + o)];
-            br = branch_of(P, ph);
-        }
+    // With the hybrid switch, UP7 and NND2 faces are done at once and the WENO7 / WENO5
+    // faces are queued and then processed by consecutive threads: near a shock only a few
+    // faces of a warp take the long WENO paths, and done in place they would run with the
+    // other lanes idle (and a warp holding both kinds would run both paths).
+    auto do_face = [&](int l, int t, int br) {
         const long long cl = cell(l, c0 + t + 3), cr = cl + stride;
         R out[5];
         R s0 = R(0);
@@ -272,6 +268,37 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
             const long long fo = fi + fx * (fj + fy * fk), nf = fx * fy * fz;
 #pragma unroll
             for (int n = 0; n < 5; n++) a.faces[fo + n * nf] = (double)out[n];
+        }
+    };
+    int* list7 = reinterpret_cast<int*>(sPhi + TL * NP);
+    int* list5 = list7 + TL * NF;
+    int* counts = list5 + TL * NF;
+    for (int it = threadIdx.x; it < TL * NF; it += SWEEP_THREADS) {
+        int l, t;
+        if (DIR == 0) { l = it / NF; t = it - l * NF; } else { t = it / TL; l = it - t * TL; }
+        if (l >= nl || t > nc) continue;
+        int br = P.fixed_branch;
+        if (hybrid) {
+            R ph[6];
+#pragma unroll
+            for (int o = 0; o < 6; o++) ph[o] = sPhi[sidx(l, t + 1 + o)];
+            br = branch_of(P, ph);
+            if (br == 1 || br == 2) {
+                const int k = atomicAdd(&counts[br - 1], 1);
+                (br == 1 ? list7 : list5)[k] = it;
+                continue;
+            }
+        }
+        do_face(l, t, br);
+    }
+    if (hybrid) {
+        __syncthreads();
+        const int n7 = counts[0], n5 = counts[1];
+        for (int k = threadIdx.x; k < n7 + n5; k += SWEEP_THREADS) {
+            const int it = k < n7 ? list7[k] : list5[k - n7];
+            int l, t;
+            if (DIR == 0) { l = it / NF; t = it - l * NF; } else { t = it / TL; l = it - t * TL; }
+            do_face(l, t, k < n7 ? 1 : 2);
         }
     }
     if (a.out_mode == OUT_FACES) return;
