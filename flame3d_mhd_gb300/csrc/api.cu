@@ -73,6 +73,7 @@ DevParams make_dev_params(const f3d_params& p) {
     d.cp = p.cp != 0.0 ? p.cp : p.rg * p.gamma / (p.gamma - 1.0);
     d.c_s = p.c_s; d.t_s = p.t_s; d.pr = p.pr;
     d.gm1 = p.gamma - 1.0;
+    d.inv_rg = 1.0 / p.rg;
     d.grg = p.gamma * p.rg;
     d.eps_clamp = p.clamp_eps != 0.0 ? p.clamp_eps : 1.1920928955078125e-07;
     d.phi1 = p.phi1; d.phi2 = p.phi2; d.phi3 = p.phi3;
@@ -146,7 +147,8 @@ struct f3d_ctx {
     Prof* prof = nullptr;
     // adjoint scratch, allocated by the first VJP call
     void* adj_slab = nullptr;
-    double *Qs = nullptr, *Qb = nullptr, *Lt = nullptr, *U1 = nullptr, *U2 = nullptr, *Xb = nullptr, *Yb = nullptr;
+    double *Qb = nullptr, *Lt = nullptr, *U1 = nullptr, *U2 = nullptr, *Xb = nullptr, *Yb = nullptr;
+    double *Qst[3] = {}, *cst_[3] = {}, *phst[3] = {};  // Q, sound speed and sensor of the 3 stage states
     double *Fvb[3] = {}, *gb = nullptr;
     // CUDA graph of one RK3 step, keyed by its arguments
     cudaGraphExec_t step_graph = nullptr;
@@ -322,17 +324,21 @@ int adjoint_alloc(f3d_ctx* ctx) {
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t b1 = up(nc * 8);
     const size_t bv = up(nv * 8);
-    size_t total = b1 * (6 + 6 + 5 * 5) + (ctx->params.viscous ? bv * (12 + 12) : 0);
+    size_t total = b1 * (6 + 5 * 5 + 3 * 8) + (ctx->params.viscous ? bv * (12 + 12) : 0);
     cudaError_t e = cudaMalloc(&ctx->adj_slab, total);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc (adjoint scratch)");
     char* q = (char*)ctx->adj_slab;
-    ctx->Qs = (double*)q; q += 6 * b1;
     ctx->Qb = (double*)q; q += 6 * b1;
     ctx->Lt = (double*)q; q += 5 * b1;
     ctx->U1 = (double*)q; q += 5 * b1;
     ctx->U2 = (double*)q; q += 5 * b1;
     ctx->Xb = (double*)q; q += 5 * b1;
     ctx->Yb = (double*)q; q += 5 * b1;
+    for (int k = 0; k < 3; k++) {
+        ctx->Qst[k] = (double*)q; q += 6 * b1;
+        ctx->cst_[k] = (double*)q; q += b1;
+        ctx->phst[k] = (double*)q; q += b1;
+    }
     if (ctx->params.viscous) {
         for (int d = 0; d < 3; d++) { ctx->Fvb[d] = (double*)q; q += 4 * bv; }
         ctx->gb = (double*)q;
@@ -343,44 +349,56 @@ int adjoint_alloc(f3d_ctx* ctx) {
     return F3D_OK;
 }
 
-// L(U) at interior cells into out (U layout): Q = c2Prim(U) + ghost fill into ctx->Qs
-int rhs_of_state(f3d_ctx* ctx, const double* U, double* out, cudaStream_t st) {
-    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, ctx->Qs, nullptr, nullptr, 0, st));
-    SweepArgs last;
-    std::memset(&last, 0, sizeof(last));
-    last.out_mode = OUT_RHS;
-    last.out = out;
-    return run_rhs(ctx, ctx->Qs, out, last, st);
+// Q (ghost-filled c2Prim(U)), split sound speed and sensor of a state U, into the given
+// buffers: everything the RHS and its VJP need from the forward state.
+int prep_state(f3d_ctx* ctx, const double* U, double* Q, double* csnd, double* phi, cudaStream_t st) {
+    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, nullptr, csnd, 0, st));
+    if (ctx->dp.fixed_branch < 0) F3D_CUDA(ctx, launch_sensor(ctx->dp, Q, phi, st));
+    return F3D_OK;
 }
 
-// out = beta out + alpha (dL/dU)^T Lb at interior cells, for the state U
-int rhs_vjp_of_state(f3d_ctx* ctx, const double* U, const double* Lb, double* out, double alpha, double beta,
-                     cudaStream_t st) {
+// L at interior cells into out, from a prepared state (the sweeps only)
+int rhs_prepared(f3d_ctx* ctx, const double* Q, const double* csnd, const double* phi, double* out, cudaStream_t st) {
     const DevParams& P = ctx->dp;
-    F3D_CUDA(ctx, launch_prim_fill(P, U, ctx->Qs, nullptr, ctx->csnd, 0, st));
     const bool hybrid = P.fixed_branch < 0;
-    if (hybrid) F3D_CUDA(ctx, launch_sensor(P, ctx->Qs, ctx->phi, st));
+    if (ctx->params.viscous) F3D_CUDA(ctx, launch_viscous(P, Q, ctx->m, ctx->J, ctx->Fv[0], ctx->Fv[1], ctx->Fv[2], st));
+    for (int d = 0; d < 3; d++) {
+        SweepArgs a = sweep_args(ctx, d, Q, hybrid, phi);
+        a.csnd = csnd;
+        a.acc = out;
+        a.out = out;
+        a.out_mode = d == 0 ? OUT_SET : (d == 1 ? OUT_ADD : OUT_RHS);
+        F3D_CUDA(ctx, launch_sweep(d, a, st));
+    }
+    return F3D_OK;
+}
+
+// out = beta out + alpha (dL/dU)^T Lb at interior cells, for the state U prepared in Q/csnd/phi
+int rhs_vjp_prepared(f3d_ctx* ctx, const double* U, const double* Q, const double* csnd, const double* phi,
+                     const double* Lb, double* out, double alpha, double beta, cudaStream_t st) {
+    const DevParams& P = ctx->dp;
+    const bool hybrid = P.fixed_branch < 0;
     F3D_CUDA(ctx, cudaMemsetAsync(ctx->Qb, 0, (size_t)P.plane * 6 * sizeof(double), st));
     for (int d = 0; d < 3; d++) {
         AdjArgs a;
         std::memset(&a, 0, sizeof(a));
         a.P = P;
-        a.Q = ctx->Qs;
-        a.csnd = ctx->csnd;
+        a.Q = Q;
+        a.csnd = csnd;
         for (int n = 0; n < 3; n++) {
             a.A[n] = ctx->m[3 * d + n];
             a.Ah[n] = ctx->Ah[3 * d + n];
         }
         a.S = ctx->S[d];
-        a.phi = hybrid ? ctx->phi : nullptr;
+        a.phi = hybrid ? phi : nullptr;
         a.J = ctx->J;
         a.Lb = Lb;
         a.Qb = ctx->Qb;
         F3D_CUDA(ctx, launch_sweep_vjp(d, a, st));
     }
     if (ctx->params.viscous)
-        F3D_CUDA(ctx, launch_viscous_vjp(P, ctx->Qs, ctx->m, ctx->J, Lb, ctx->Fvb, ctx->gb, ctx->Qb, st));
-    F3D_CUDA(ctx, launch_fill_vjp(P, ctx->Qs, ctx->Qb, st));
+        F3D_CUDA(ctx, launch_viscous_vjp(P, Q, ctx->m, ctx->J, Lb, ctx->Fvb, ctx->gb, ctx->Qb, st));
+    F3D_CUDA(ctx, launch_fill_vjp(P, Q, ctx->Qb, st));
     F3D_CUDA(ctx, launch_c2prim_vjp(P, U, ctx->Qb, out, alpha, beta, st));
     return F3D_OK;
 }
@@ -624,7 +642,8 @@ int f3d_rhs_vjp(f3d_ctx* ctx, const double* U, const double* Lbar, double* Ubar,
     if ((rc = adjoint_supported(ctx)) || (rc = adjoint_alloc(ctx))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     F3D_CUDA(ctx, cudaMemsetAsync(Ubar, 0, (size_t)ctx->dp.plane * 5 * sizeof(double), st));
-    return rhs_vjp_of_state(ctx, U, Lbar, Ubar, 1.0, 0.0, st);
+    if ((rc = prep_state(ctx, U, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
+    return rhs_vjp_prepared(ctx, U, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], Lbar, Ubar, 1.0, 0.0, st);
 }
 
 // SSP-RK3 step U1 = U0 + dt L(U0), U2 = 3/4 U0 + 1/4 (U1 + dt L(U1)),
@@ -638,25 +657,32 @@ int f3d_rk3_step_vjp(f3d_ctx* ctx, double dt, const double* U0, const double* Ub
     if ((rc = adjoint_supported(ctx)) || (rc = adjoint_alloc(ctx))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const DevParams& P = ctx->dp;
-    // forward recompute of the stage states
-    if ((rc = rhs_of_state(ctx, U0, ctx->Lt, st))) return rc;
+    // forward recompute of the stage states, keeping what each stage's VJP needs
+    const double* Us[3] = {U0, ctx->U1, ctx->U2};
+    if ((rc = prep_state(ctx, U0, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
+    if ((rc = rhs_prepared(ctx, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], ctx->Lt, st))) return rc;
     F3D_CUDA(ctx, launch_axpby(P, ctx->U1, U0, 1.0, ctx->Lt, dt, st));
-    if ((rc = rhs_of_state(ctx, ctx->U1, ctx->Lt, st))) return rc;
+    if ((rc = prep_state(ctx, ctx->U1, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], st))) return rc;
+    if ((rc = rhs_prepared(ctx, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], ctx->Lt, st))) return rc;
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U1, 0.25, ctx->Lt, 0.25 * dt, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U2, 1.0, U0, 0.75, st));
+    if ((rc = prep_state(ctx, ctx->U2, ctx->Qst[2], ctx->cst_[2], ctx->phst[2], st))) return rc;
+    auto vjp = [&](int k, const double* Lb, double* out) {
+        return rhs_vjp_prepared(ctx, Us[k], ctx->Qst[k], ctx->cst_[k], ctx->phst[k], Lb, out, dt, 1.0, st);
+    };
     // stage 3: U3 = 1/3 U0 + 2/3 W, W = U2 + dt L(U2)
     F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar_next, 1.0 / 3.0, nullptr, 0.0, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->Xb, Ubar_next, 2.0 / 3.0, nullptr, 0.0, st));  // Wb
     F3D_CUDA(ctx, launch_axpby(P, ctx->Yb, ctx->Xb, 1.0, nullptr, 0.0, st));          // U2b = Wb + dt J^T Wb
-    if ((rc = rhs_vjp_of_state(ctx, ctx->U2, ctx->Xb, ctx->Yb, dt, 1.0, st))) return rc;
+    if ((rc = vjp(2, ctx->Xb, ctx->Yb))) return rc;
     // stage 2: U2 = 3/4 U0 + 1/4 V, V = U1 + dt L(U1)
     F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar, 1.0, ctx->Yb, 0.75, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->Xb, ctx->Yb, 0.25, nullptr, 0.0, st));  // Vb
     F3D_CUDA(ctx, launch_axpby(P, ctx->Yb, ctx->Xb, 1.0, nullptr, 0.0, st));    // U1b = Vb + dt J^T Vb
-    if ((rc = rhs_vjp_of_state(ctx, ctx->U1, ctx->Xb, ctx->Yb, dt, 1.0, st))) return rc;
+    if ((rc = vjp(1, ctx->Xb, ctx->Yb))) return rc;
     // stage 1: U1 = U0 + dt L(U0)
     F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar, 1.0, ctx->Yb, 1.0, st));
-    return rhs_vjp_of_state(ctx, U0, ctx->Yb, Ubar, dt, 1.0, st);
+    return vjp(0, ctx->Yb, Ubar);
 }
 
 int f3d_kernel_count(void) { return K_NKIND; }

@@ -40,6 +40,7 @@ struct DevParams {
     long long plane;    // nxt*nyt*nzt
     double gamma, rg, cp, c_s, t_s, pr;
     double gm1;          // gamma - 1
+    double inv_rg;       // 1 / Rg
     double grg;          // gamma * Rg (split.jl:22)
     double eps_clamp;    // utils.jl:12,18
     double phi1, phi2, phi3;
@@ -82,6 +83,21 @@ __device__ __forceinline__ void c2prim_cell(const DevParams& P, const double U[5
     double p = __dmul_rn(P.gm1, ei);
     double T = p / __dmul_rn(rho, P.rg);
     q[0] = rho; q[1] = u; q[2] = v; q[3] = w; q[4] = p; q[5] = T;
+}
+
+// The same recovery for the mixed-precision form: still FP64 (the pressure/temperature
+// recovery from total energy stays FP64), with T = p (1/rho)(1/Rg) instead of a second
+// division. FP64 divisions are ~10 FMA issue slots on GB300.
+__device__ __forceinline__ void c2prim_cell_fast(const DevParams& P, const double U[5], double q[6]) {
+    double rho = fmax(U[0], P.eps_clamp);
+    if (U[0] != U[0]) rho = U[0];
+    const double rinv = 1.0 / rho;
+    const double u = U[1] * rinv, v = U[2] * rinv, w = U[3] * rinv;
+    const double eraw = U[4] - 0.5 * rho * (u * u + v * v + w * w);
+    double ei = fmax(eraw, P.eps_clamp);
+    if (eraw != eraw) ei = eraw;
+    const double p = P.gm1 * ei;
+    q[0] = rho; q[1] = u; q[2] = v; q[3] = w; q[4] = p; q[5] = p * (rinv * P.inv_rg);
 }
 
 // utils.jl:33-54 prim2c of one cell (also the U of Dirichlet and wall ghosts,

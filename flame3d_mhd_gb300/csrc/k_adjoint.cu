@@ -20,12 +20,13 @@ namespace f3d {
 
 template <int DIR> struct VTile;
 template <> struct VTile<0> { static constexpr int TL = 4, TC = 64; };
-template <> struct VTile<1> { static constexpr int TL = 16, TC = 16; };
-template <> struct VTile<2> { static constexpr int TL = 16, TC = 16; };
+template <> struct VTile<1> { static constexpr int TL = 16, TC = 32; };
+template <> struct VTile<2> { static constexpr int TL = 16, TC = 32; };
 constexpr int VJP_THREADS = 256;
 
 template <int DIR> constexpr size_t vjp_smem_bytes() {
-    return sizeof(double) * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 8) * 21;
+    return sizeof(double) * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 8) * 21 +
+           sizeof(int) * (2 * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 1) + 4);
 }
 
 template <int DIR>
@@ -58,6 +59,10 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
     auto sidx = [&](int l, int p) { return DIR == 0 ? l * NP + p : p * TL + l; };
     const long long pl = P.plane;
 
+    int* list7 = reinterpret_cast<int*>(sPhi + TL * NP);
+    int* list5 = list7 + TL * (TC + 1);
+    int* counts = list5 + TL * (TC + 1);
+    if (threadIdx.x < 2) counts[threadIdx.x] = 0;
     // Phase A: forward split at positions 0..nc+7 (full index c0 + p); zero the cotangents
     for (int it = threadIdx.x; it < TL * NP; it += VJP_THREADS) {
         int l, p;
@@ -81,11 +86,9 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
     }
     __syncthreads();
 
-    // Phase B: owned faces t (interior face c0+t, between positions t+3 and t+4)
-    for (int it = threadIdx.x; it < TL * (TC + 1); it += VJP_THREADS) {
-        int l, t;
-        if (DIR == 0) { l = it / (TC + 1); t = it - l * (TC + 1); } else { t = it / TL; l = it - t * TL; }
-        if (l >= nl || t >= nfaces) continue;
+    // Phase B: owned faces t (interior face c0+t, between positions t+3 and t+4). UP7 and
+    // NND2 faces at once; WENO7 / WENO5 faces queued and done by consecutive threads.
+    auto face_vjp = [&](int l, int t, int br) {
         const int f = c0 + t;  // interior face index 0..Nd
         // L_c = J_c (F[left face of c] - F[right face of c]): face f is the left face of
         // interior cell f and the right face of interior cell f-1
@@ -98,15 +101,6 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
         if (f >= 1) {
             const double j = a.J[cl];
             for (int n = 0; n < 5; n++) Fb[n] -= j * a.Lb[cl + n * pl];
-        }
-        int br = P.fixed_branch;
-        if (hybrid) {
-            unsigned long long m = __double_as_longlong(sPhi[sidx(l, t + 1)]);
-            for (int o = 2; o <= 6; o++) {
-                unsigned long long b = __double_as_longlong(sPhi[sidx(l, t + o)]);
-                m = b > m ? b : m;
-            }
-            br = m < P.phib[0] ? 0 : (m < P.phib[1] ? 1 : (m < P.phib[2] ? 2 : 3));
         }
         const double s0 = (br == 1 || br == 2) ? 2.0 / (a.S[cl] + a.S[cr]) : 0.0;
         for (int n = 0; n < 5; n++) {
@@ -165,6 +159,36 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
                     }
                 }
             }
+        }
+    };
+    for (int it = threadIdx.x; it < TL * (TC + 1); it += VJP_THREADS) {
+        int l, t;
+        if (DIR == 0) { l = it / (TC + 1); t = it - l * (TC + 1); } else { t = it / TL; l = it - t * TL; }
+        if (l >= nl || t >= nfaces) continue;
+        int br = P.fixed_branch;
+        if (hybrid) {
+            unsigned long long m = __double_as_longlong(sPhi[sidx(l, t + 1)]);
+            for (int o = 2; o <= 6; o++) {
+                unsigned long long b = __double_as_longlong(sPhi[sidx(l, t + o)]);
+                m = b > m ? b : m;
+            }
+            br = m < P.phib[0] ? 0 : (m < P.phib[1] ? 1 : (m < P.phib[2] ? 2 : 3));
+            if (br == 1 || br == 2) {
+                const int k = atomicAdd(&counts[br - 1], 1);
+                (br == 1 ? list7 : list5)[k] = it;
+                continue;
+            }
+        }
+        face_vjp(l, t, br);
+    }
+    if (hybrid) {
+        __syncthreads();
+        const int n7 = counts[0], n5 = counts[1];
+        for (int k = threadIdx.x; k < n7 + n5; k += VJP_THREADS) {
+            const int it = k < n7 ? list7[k] : list5[k - n7];
+            int l, t;
+            if (DIR == 0) { l = it / (TC + 1); t = it - l * (TC + 1); } else { t = it / TL; l = it - t * TL; }
+            face_vjp(l, t, k < n7 ? 1 : 2);
         }
     }
     __syncthreads();

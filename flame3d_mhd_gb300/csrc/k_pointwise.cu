@@ -48,7 +48,8 @@ __global__ void k_prim_fill(const DevParams P, const double* U, double* Q, doubl
             double u[5];
 #pragma unroll
             for (int n = 0; n < 5; n++) u[n] = U[c + n * pl];
-            c2prim_cell(P, u, q);
+            if (Q32) c2prim_cell_fast(P, u, q);  // mixed precision
+            else c2prim_cell(P, u, q);
 #pragma unroll
             for (int n = 0; n < 6; n++) Q[c + n * pl] = q[n];
         }
@@ -63,7 +64,8 @@ __global__ void k_prim_fill(const DevParams P, const double* U, double* Q, doubl
                 double u[5];
 #pragma unroll
                 for (int n = 0; n < 5; n++) u[n] = U[s + n * pl];
-                c2prim_cell(P, u, q);
+                if (Q32) c2prim_cell_fast(P, u, q);
+                else c2prim_cell(P, u, q);
             }
         }
         apply_chain(P, ch, q);
