@@ -95,6 +95,7 @@ DevParams make_dev_params(const f3d_params& p) {
         c.inv_gm1 = (R)(1.0 / d.gm1); c.inv_2g = (R)(1.0 / (2.0 * p.gamma)); c.two_gm1 = (R)(2.0 * d.gm1);
         c.w2c = (R)((3.0 - p.gamma) / (2.0 * d.gm1));
         c.c_s = (R)d.c_s; c.t_s = (R)d.t_s; c.cp = (R)d.cp; c.pr = (R)d.pr;
+        c.cp_pr = (R)(d.cp / d.pr);
         c.phi1 = (R)p.phi1; c.phi2 = (R)p.phi2; c.phi3 = (R)p.phi3;
         for (int m = 0; m < 7; m++) c.lin[m] = (R)d.lin[m];
     };

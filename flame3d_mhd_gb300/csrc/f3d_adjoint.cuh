@@ -21,9 +21,9 @@ __device__ __forceinline__ void c2prim_vjp(const DevParams& P, const double U[5]
     const bool e_free = eraw > P.eps_clamp;
     const double ei = e_free ? eraw : P.eps_clamp;
     const double p = P.gm1 * ei;
-    // T = p/(rho Rg)
-    double pb = qb[4] + qb[5] * rinv / P.rg;
-    double rhob = qb[0] - qb[5] * p * rinv * rinv / P.rg;
+    const double Tr = qb[5] * rinv * P.inv_rg;  // T = p/(rho Rg)
+    double pb = qb[4] + Tr;
+    double rhob = qb[0] - Tr * p * rinv;
     const double eb = e_free ? P.gm1 * pb : 0.0;
     Ub[4] = eb;
     rhob += -0.5 * ke * eb;
@@ -181,19 +181,24 @@ __device__ __forceinline__ void weno5_vjp(const double V[5], double s0, double f
     const double IS[3] = {13 * a1_ * a1_ + 3 * b1_ * b1_, 13 * a2_ * a2_ + 3 * b2_ * b2_, 13 * a3_ * a3_ + 3 * b3_ * b3_};
     const double d[3] = {1.0, 6.0, 3.0};
     const double q[3] = {2 * V1 - 7 * V2 + 11 * V3, -V2 + 5 * V3 + 2 * V4, 2 * V3 + 5 * V4 - V5};
-    double t[3], al[3], sum = 0, num = 0;
+    // two FP64 divisions: 1/t_k from 1/(t1 t2 t3), and 1/sum alpha
+    const double t0 = 1e-16 + IS[0] * s0, t1 = 1e-16 + IS[1] * s0, t2 = 1e-16 + IS[2] * s0;
+    const double t12 = t1 * t2, rall = 1.0 / (t0 * t12);
+    const double it[3] = {t12 * rall, t0 * t2 * rall, t0 * t1 * rall};
+    double al[3], sum = 0;
     for (int k = 0; k < 3; k++) {
-        t[k] = 1e-16 + IS[k] * s0;
-        al[k] = d[k] / (t[k] * t[k]);
+        al[k] = d[k] * it[k] * it[k];
         sum += al[k];
-        num += al[k] * q[k];
     }
-    const double f = num / sum;
+    const double rs = 1.0 / sum;
+    double f = 0;
+    for (int k = 0; k < 3; k++) f += al[k] * rs * q[k];
     double qb[3], ISb[3];
     for (int k = 0; k < 3; k++) {
-        qb[k] = fb * al[k] / sum;
-        const double alb = fb * (q[k] - f) / sum;
-        ISb[k] = -2.0 * al[k] / t[k] * alb * s0;
+        const double wk = al[k] * rs;
+        qb[k] = fb * wk;
+        // alpha_k-bar = fb (q_k - f) / sum, t_k-bar = -2 alpha_k / t_k alpha_k-bar
+        ISb[k] = -2.0 * s0 * fb * (q[k] - f) * wk * it[k];
     }
     for (int j = 0; j < 5; j++) Vb[j] = 0.0;
     // q
@@ -220,7 +225,7 @@ __device__ __constant__ const double kW7Q[4][4] = {{-3, 13, -23, 25}, {1, -5, 13
 
 __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double fb, double Vb[7]) {
     const double d[4] = {1.0, 12.0, 18.0, 4.0};
-    double q[4], t[4], al[4], sum = 0, num = 0;
+    double q[4], t[4];
     for (int k = 0; k < 4; k++) {
         double is = 0, qq = 0;
         for (int i = 0; i < 4; i++) {
@@ -229,16 +234,23 @@ __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double f
         }
         q[k] = qq;
         t[k] = 1e-20 + is * s0;
-        al[k] = d[k] / (t[k] * t[k]);
-        sum += al[k];
-        num += al[k] * qq;
     }
-    const double f = num / sum;
+    // two FP64 divisions: 1/t_k from 1/(t1 t2 t3 t4), and 1/sum alpha
+    const double t01 = t[0] * t[1], t23 = t[2] * t[3], rall = 1.0 / (t01 * t23);
+    const double it[4] = {t[1] * t23 * rall, t[0] * t23 * rall, t01 * t[3] * rall, t01 * t[2] * rall};
+    double al[4], sum = 0;
+    for (int k = 0; k < 4; k++) {
+        al[k] = d[k] * it[k] * it[k];
+        sum += al[k];
+    }
+    const double rs = 1.0 / sum;
+    double f = 0;
+    for (int k = 0; k < 4; k++) f += al[k] * rs * q[k];
     for (int j = 0; j < 7; j++) Vb[j] = 0.0;
     for (int k = 0; k < 4; k++) {
-        const double qb = fb * al[k] / sum;
-        const double alb = fb * (q[k] - f) / sum;
-        const double ISb = -2.0 * al[k] / t[k] * alb * s0;
+        const double wk = al[k] * rs;
+        const double qb = fb * wk;
+        const double ISb = -2.0 * s0 * fb * (q[k] - f) * wk * it[k];
         for (int i = 0; i < 4; i++) {
             Vb[k + i] += kW7Q[k][i] * qb;
             double g = 0;  // dIS/dV_{k+i}

@@ -29,6 +29,7 @@ template <class R> struct Cst {
     R two_gm1;   // 2 (gamma-1)          (split.jl:55)
     R w2c;       // (3-gamma)/(2(gamma-1)) (split.jl:52)
     R c_s, t_s, cp, pr;
+    R cp_pr;     // cp / Pr: heat conductivity per unit viscosity
     R phi1, phi2, phi3;
     R lin[7];
 };

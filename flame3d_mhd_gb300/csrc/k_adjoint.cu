@@ -18,11 +18,12 @@
 
 namespace f3d {
 
+// Tile of TL lines x TC cells; NT threads cover the TL x (TC + 8) stencil positions of
+// phases A and C in whole rounds (one block per SM: about 160 registers a thread).
 template <int DIR> struct VTile;
-template <> struct VTile<0> { static constexpr int TL = 4, TC = 64; };
-template <> struct VTile<1> { static constexpr int TL = 16, TC = 32; };
-template <> struct VTile<2> { static constexpr int TL = 16, TC = 32; };
-constexpr int VJP_THREADS = 256;
+template <> struct VTile<0> { static constexpr int TL = 4, TC = 64, NT = 288; };
+template <> struct VTile<1> { static constexpr int TL = 16, TC = 64, NT = 384; };
+template <> struct VTile<2> { static constexpr int TL = 16, TC = 64, NT = 384; };
 
 template <int DIR> constexpr size_t vjp_smem_bytes() {
     return sizeof(double) * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 8) * 21 +
@@ -30,8 +31,8 @@ template <int DIR> constexpr size_t vjp_smem_bytes() {
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
-    constexpr int TL = VTile<DIR>::TL, TC = VTile<DIR>::TC, NP = TC + 8;
+__global__ void __launch_bounds__(VTile<DIR>::NT) k_sweep_vjp(const AdjArgs a) {
+    constexpr int TL = VTile<DIR>::TL, TC = VTile<DIR>::TC, NP = TC + 8, NT = VTile<DIR>::NT;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
     int* counts = list5 + TL * (TC + 1);
     if (threadIdx.x < 2) counts[threadIdx.x] = 0;
     // Phase A: forward split at positions 0..nc+7 (full index c0 + p); zero the cotangents
-    for (int it = threadIdx.x; it < TL * NP; it += VJP_THREADS) {
+    for (int it = threadIdx.x; it < TL * NP; it += NT) {
         int l, p;
         if (DIR == 0) { l = it / NP; p = it - l * NP; } else { p = it / TL; l = it - p * TL; }
         const int s = sidx(l, p);
@@ -120,18 +121,18 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
             } else if (br == 1) {  // WENO7, (fp + fm)/12
                 double V[7], Vb[7];
                 for (int k = 0; k < 7; k++) V[k] = P_(t + k);
-                weno7_vjp(V, s0, g / 12.0, Vb);
+                weno7_vjp(V, s0, g * (1.0 / 12.0), Vb);
                 for (int k = 0; k < 7; k++) atomicAdd(&pb[sidx(l, t + k)], Vb[k]);
                 for (int k = 0; k < 7; k++) V[k] = M_(t + 7 - k);
-                weno7_vjp(V, s0, g / 12.0, Vb);
+                weno7_vjp(V, s0, g * (1.0 / 12.0), Vb);
                 for (int k = 0; k < 7; k++) atomicAdd(&mb[sidx(l, t + 7 - k)], Vb[k]);
             } else if (br == 2) {  // WENO5, (fp + fm)/6: Fp at t+1..t+5, Fm at t+6..t+2
                 double V[5], Vb[5];
                 for (int k = 0; k < 5; k++) V[k] = P_(t + 1 + k);
-                weno5_vjp(V, s0, g / 6.0, Vb);
+                weno5_vjp(V, s0, g * (1.0 / 6.0), Vb);
                 for (int k = 0; k < 5; k++) atomicAdd(&pb[sidx(l, t + 1 + k)], Vb[k]);
                 for (int k = 0; k < 5; k++) V[k] = M_(t + 6 - k);
-                weno5_vjp(V, s0, g / 6.0, Vb);
+                weno5_vjp(V, s0, g * (1.0 / 6.0), Vb);
                 for (int k = 0; k < 5; k++) atomicAdd(&mb[sidx(l, t + 6 - k)], Vb[k]);
             } else {  // NND2 (schemes.jl:277-286): minmod picks one difference or none
                 // fp = Fp[t+3] + 0.5 minmod(Fp[t+4]-Fp[t+3], Fp[t+3]-Fp[t+2])
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
             }
         }
     };
-    for (int it = threadIdx.x; it < TL * (TC + 1); it += VJP_THREADS) {
+    for (int it = threadIdx.x; it < TL * (TC + 1); it += NT) {
         int l, t;
         if (DIR == 0) { l = it / (TC + 1); t = it - l * (TC + 1); } else { t = it / TL; l = it - t * TL; }
         if (l >= nl || t >= nfaces) continue;
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
     if (hybrid) {
         __syncthreads();
         const int n7 = counts[0], n5 = counts[1];
-        for (int k = threadIdx.x; k < n7 + n5; k += VJP_THREADS) {
+        for (int k = threadIdx.x; k < n7 + n5; k += NT) {
             const int it = k < n7 ? list7[k] : list5[k - n7];
             int l, t;
             if (DIR == 0) { l = it / (TC + 1); t = it - l * (TC + 1); } else { t = it / TL; l = it - t * TL; }
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(VJP_THREADS) k_sweep_vjp(const AdjArgs a) {
     __syncthreads();
 
     // Phase C: reverse of the split at every position, into Qb
-    for (int it = threadIdx.x; it < TL * NP; it += VJP_THREADS) {
+    for (int it = threadIdx.x; it < TL * NP; it += NT) {
         int l, p;
         if (DIR == 0) { l = it / NP; p = it - l * NP; } else { p = it / TL; l = it - p * TL; }
         if (l >= nl || p >= nc + 8) continue;
@@ -277,8 +278,9 @@ __global__ void k_visc_vjp(const DevParams P, const double* __restrict__ Q, cons
     const double Jac = J[c];
     const double T = Q[c + 5 * pl];
     const double sT = sqrt(T);
-    const double mu = P.c_s * T * sT / (T + P.t_s);
-    const double lam = P.cp * mu / P.pr;
+    const double rTs = 1.0 / (T + P.t_s);
+    const double mu = P.c_s * T * sT * rTs;
+    const double lam = mu * P.cd.cp_pr;
     const double c1 = 1.0 / 12.0, c2 = -2.0 / 3.0, c23 = 2.0 / 3.0;
     // forward: computational gradients G[var][d] of (u, v, w, T) and physical D[var][x]
     const int vars[4] = {1, 2, 3, 5};
@@ -337,8 +339,8 @@ __global__ void k_visc_vjp(const DevParams P, const double* __restrict__ Q, cons
     Db[1][1] += dvb;
     Db[2][2] += dvb;
     // lambda = cp mu / Pr; mu = C_s T^1.5 / (T + T_s)
-    mub += lamb * P.cp / P.pr;
-    const double Tb_mu = mub * P.c_s * (1.5 * sT * (T + P.t_s) - T * sT) / ((T + P.t_s) * (T + P.t_s));
+    mub += lamb * P.cd.cp_pr;
+    const double Tb_mu = mub * P.c_s * (1.5 * sT * (T + P.t_s) - T * sT) * (rTs * rTs);
     // D[a][x] = (sum_d G[a][d] M[d][x]) J
     for (int a = 0; a < 4; a++)
         for (int d = 0; d < 3; d++) {
@@ -460,7 +462,7 @@ template <int DIR> static cudaError_t launch_vjp_dir(const AdjArgs& a, cudaStrea
     if (DIR == 0) grid = dim3(cdiv(P.nx, TC), cdiv(P.ny, TL), P.nz);
     else if (DIR == 1) grid = dim3(cdiv(P.nx, TL), cdiv(P.ny, TC), P.nz);
     else grid = dim3(cdiv(P.nx, TL), cdiv(P.nz, TC), P.ny);
-    k_sweep_vjp<DIR><<<grid, VJP_THREADS, vjp_smem_bytes<DIR>(), st>>>(a);
+    k_sweep_vjp<DIR><<<grid, VTile<DIR>::NT, vjp_smem_bytes<DIR>(), st>>>(a);
     return cudaGetLastError();
 }
 

@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(128) k_viscous(const DevParams P, const R* __r
     const R Jac = J[c];
     const R T = Q[c + 5 * pl];
     const R mu = K.c_s * T * sqrt(T) / (T + K.t_s);
-    const R lam = K.cp * mu / K.pr;
+    const R lam = mu * K.cp_pr;
     const R c1 = R(1) / R(12), c2 = R(-2) / R(3), c23 = R(2) / R(3);
     auto d4 = [&](int n, long long s) {
         const R* f = Q + n * pl + c;

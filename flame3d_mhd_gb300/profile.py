@@ -7,6 +7,8 @@ Used under ncu to capture the kernels of one RHS with few launches before them:
       python -m flame3d_mhd_gb300.profile --case sod --reps 2
 
 The first RHS evaluation is a warm-up (its launches are the ones skipped with -s).
+With --adjoint the workload is the viscous curvilinear Taylor-Green vortex (--nx cells per
+side, FP64, component-wise) and each repetition is one RK3 step VJP (f3d_rk3_step_vjp).
 """
 from __future__ import annotations
 
@@ -25,6 +27,8 @@ from .solver import Flame3D
 def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: int = 0):
     if case == "sod":
         c = cases.sod(nx, ny, nz, character=character)
+    elif case == "tgv_viscous":
+        c = cases.tgv_viscous_curvilinear(nx)
     elif case == "tgv":
         c = cases.tgv(nx, character=character)
     else:
@@ -44,7 +48,7 @@ def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: i
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="sod", choices=["sod", "tgv"])
+    ap.add_argument("--case", default="sod", choices=["sod", "tgv", "tgv_viscous"])
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--ny", type=int, default=64)
     ap.add_argument("--nz", type=int, default=64)
@@ -52,13 +56,18 @@ def main(argv=None):
     ap.add_argument("--precision", type=int, default=0)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--step", action="store_true", help="profile_step instead of rhs (per-kernel event times)")
+    ap.add_argument("--adjoint", action="store_true", help="RK3 step VJPs on the viscous curvilinear TGV")
     a = ap.parse_args(argv)
+    if a.adjoint:
+        a.case = "tgv_viscous"
     s, c, U, Q = setup(a.case, a.nx, a.ny, a.nz, a.character, a.precision)
     out = s.field(5)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(a.reps):
-        if a.step:
+        if a.adjoint:
+            s.rk3_step_vjp(c["dt"], U, torch.ones_like(U), out)
+        elif a.step:
             Un = s.field(5)
             print(json.dumps(s.profile_step(U, Un, Q, c["dt"])))
         else:
