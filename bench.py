@@ -200,7 +200,7 @@ def adjoint_cost(args, n: int = 128, steps: int = 4) -> dict:
     import torch
 
     from flame3d_mhd_gb300 import cases
-    from flame3d_mhd_gb300.solver import Flame3D
+    from flame3d_mhd_gb300.solver import Flame3D, side_stream
     c = cases.tgv_viscous_curvilinear(n)
     P = c["params"]
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
@@ -212,9 +212,8 @@ def adjoint_cost(args, n: int = 128, steps: int = 4) -> dict:
     s.prim2c(U, Q)
     s.fillGhost(Q, U)
     dt = c["dt"]
-    stream = torch.cuda.Stream()
     Ub, Ub2 = torch.ones_like(U), s.field(5)
-    with torch.cuda.stream(stream):
+    with side_stream() as stream:
         s.time_step(U, Un, Q, dt, 2)
         s.rk3_step_vjp(dt, U, Ub, Ub2)
         stream.synchronize()
@@ -250,7 +249,7 @@ def run_ours(args):
     from flame3d_mhd_gb300 import build as fbuild
     fbuild.build()
     from flame3d_mhd_gb300 import cases
-    from flame3d_mhd_gb300.solver import Flame3D
+    from flame3d_mhd_gb300.solver import Flame3D, side_stream
 
     c = cases.sod(**WORKLOAD)
     P = c["params"]
@@ -276,7 +275,7 @@ def run_ours(args):
     def timed_steps(solver, U, Un, Q, steps, warmup):
         """warmup untimed steps, then `steps` timed ones (CUDA events on `stream`, barriers
         and device syncs on both sides); returns (ms, wall t0, wall t1)."""
-        with torch.cuda.stream(stream):
+        with side_stream(stream):
             for _ in range(warmup):
                 solver.time_step(U, Un, Q, dt, 1)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -322,7 +321,7 @@ def run_ours(args):
     rhs_err = max(float((r32[n][Iin[1:]] - r64[n][Iin[1:]]).abs().max() / r64[n][Iin[1:]].abs().max())
                   for n in range(5))
     prof_m = {}
-    with torch.cuda.stream(stream):
+    with side_stream(stream):
         for _ in range(3):
             for k, (t_ms, n) in sm.profile_step(Um, Unm, Qm, dt).items():
                 a = prof_m.setdefault(k, [0.0, 0])
@@ -342,7 +341,7 @@ def run_ours(args):
 
     # per-kernel device times of single steps (events between launches, outside the timed loop)
     prof = {}
-    with torch.cuda.stream(stream):
+    with side_stream(stream):
         for _ in range(3):
             for k, (t_ms, n) in s.profile_step(U, Un, Q, dt).items():
                 a = prof.setdefault(k, [0.0, 0])
@@ -367,7 +366,7 @@ def run_ours(args):
     Q_h = Q0.cpu().pin_memory()
     U_out = torch.empty_like(U_h).pin_memory()
     e2e_steps = max(3, min(args.steps, 20))
-    with torch.cuda.stream(stream):
+    with side_stream(stream):
         for it in range(e2e_steps + 1):
             if it == 1:
                 stream.synchronize()

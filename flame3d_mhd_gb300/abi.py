@@ -23,6 +23,7 @@ SPLIT_SW, SPLIT_LF, SPLIT_VL, SPLIT_AUSM = 0, 1, 2, 3
 SPLIT_NAMES = {"SW": SPLIT_SW, "LF": SPLIT_LF, "VL": SPLIT_VL, "AUSM": SPLIT_AUSM}
 PREC_FP64, PREC_MIXED = 0, 1
 BC_PERIODIC, BC_DIRICHLET, BC_ZERO_GRADIENT, BC_WALL_ADIABATIC, BC_WALL_ISOTHERMAL = 0, 1, 2, 3, 4
+BC_INFLOW_PROFILE = 5
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libflame3d_gpu.so"
 
@@ -122,6 +123,7 @@ def load() -> C.CDLL:
         "f3d_rhs_noalloc": (ip, [P, vp * 9, vp, vp, vp, vp]),
         "f3d_rhs_vjp": (ip, [vp, vp, vp, vp, vp]),
         "f3d_rk3_step_vjp": (ip, [vp, C.c_double, vp, vp, vp, vp]),
+        "f3d_set_inflow_profile": (ip, [vp, ip, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -137,7 +139,7 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_lincomb", "f3d_fill_ghosts", "f3d_rhs", "f3d_rk3_stage", "f3d_rk3_steps", "f3d_cfl_dt",
             "f3d_check_finite", "f3d_debug_sensor", "f3d_debug_split", "f3d_debug_face_flux",
             "f3d_debug_viscous", "f3d_div", "f3d_measure_pipes", "f3d_kernel_count", "f3d_kernel_name",
-            "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp"]
+            "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp", "f3d_set_inflow_profile"]
 
 
 class F3DError(RuntimeError):

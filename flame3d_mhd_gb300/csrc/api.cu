@@ -46,7 +46,7 @@ int validate_params(const f3d_params& p, std::string& why) {
     for (int d = 0; d < 3; d++) {
         const f3d_bc &lo = p.bc[2 * d], &hi = p.bc[2 * d + 1];
         for (const f3d_bc* b : {&lo, &hi}) {
-            if (b->kind < 0 || b->kind > 4) { why = "unknown boundary kind"; return F3D_ERR_ARG; }
+            if (b->kind < 0 || b->kind > 5) { why = "unknown boundary kind"; return F3D_ERR_ARG; }
             if (b->kind == F3D_BC_DIRICHLET && !(b->rho > 0.0 && b->p > 0.0)) {
                 why = "Dirichlet state needs rho > 0 and p > 0"; return F3D_ERR_ARG;
             }
@@ -196,14 +196,24 @@ int check_ptrs(f3d_ctx* ctx, std::initializer_list<const void*> ps) {
     return F3D_OK;
 }
 
-int check_ctx(f3d_ctx* ctx, bool need_metrics) {
+// need_state: a compute call (metrics set, and every inflow-profile face has its profile)
+int check_ctx(f3d_ctx* ctx, bool need_state) {
     if (!ctx) return F3D_ERR_ARG;
-    if (need_metrics && !ctx->metrics_set) return fail(ctx, F3D_ERR_STATE, "metrics not set (call f3d_set_metrics)");
+    if (need_state && !ctx->metrics_set) return fail(ctx, F3D_ERR_STATE, "metrics not set (call f3d_set_metrics)");
+    for (int f = 0; f < 6 && need_state; f++)
+        if (ctx->params.bc[f].kind == F3D_BC_INFLOW_PROFILE && !ctx->dp.prof[f])
+            return fail(ctx, F3D_ERR_STATE, "inflow profile not set (call f3d_set_inflow_profile)");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, F3D_ERR_CUDA, "cudaSetDevice failed");
     return F3D_OK;
 }
 
 bool mixed(const f3d_ctx* ctx) { return ctx->dp.precision == F3D_PREC_MIXED; }
+
+// Forget the captured RK3 step: its kernels hold pointers and parameters by value.
+void drop_step_graph(f3d_ctx* ctx) {
+    if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
+    ctx->step_graph = nullptr;
+}
 
 SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const double* phi_override = nullptr) {
     SweepArgs a;
@@ -528,6 +538,7 @@ int f3d_set_metrics(f3d_ctx* ctx, const double* const metrics[9], const double* 
         return rc;
     for (int n = 0; n < 9; n++) ctx->m[n] = metrics[n];
     ctx->J = jac;
+    drop_step_graph(ctx);  // a captured step holds the previous metric pointers
     if (mixed(ctx)) {
         MetricPtrs mp;
         for (int n = 0; n < 9; n++) mp.m[n] = metrics[n];
@@ -575,6 +586,9 @@ int f3d_lincomb(f3d_ctx* ctx, double* U, const double* Un, double a, double b, f
 
 int f3d_fill_ghosts(f3d_ctx* ctx, double* Q, double* U, f3d_stream stream) {
     int rc = check_ctx(ctx, false);
+    for (int f = 0; f < 6 && !rc; f++)
+        if (ctx->params.bc[f].kind == F3D_BC_INFLOW_PROFILE && !ctx->dp.prof[f])
+            rc = fail(ctx, F3D_ERR_STATE, "inflow profile not set (call f3d_set_inflow_profile)");
     if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;
     F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 1, (cudaStream_t)stream));
     return F3D_OK;
@@ -634,6 +648,19 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
         ctx->g_dt = dt;
     }
     for (int t = 0; t < nsteps; t++) F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
+    return F3D_OK;
+}
+
+int f3d_set_inflow_profile(f3d_ctx* ctx, int face, const double* prof, f3d_stream stream) {
+    (void)stream;
+    if (!ctx) return F3D_ERR_ARG;
+    if (face < 0 || face > 5) return fail(ctx, F3D_ERR_ARG, "face must be 0..5");
+    if (ctx->params.bc[face].kind != F3D_BC_INFLOW_PROFILE)
+        return fail(ctx, F3D_ERR_ARG, "face is not an F3D_BC_INFLOW_PROFILE face");
+    int rc = check_ptrs(ctx, {prof});
+    if (rc) return rc;
+    ctx->dp.prof[face] = prof;
+    drop_step_graph(ctx);
     return F3D_OK;
 }
 

@@ -56,6 +56,7 @@ struct DevParams {
     Cst<double> cd;
     Cst<float> cf;
     BcDev bc[6];
+    const double* prof[6];  // F3D_BC_INFLOW_PROFILE states (5 x Ta x Tb), borrowed
 };
 
 template <class R> __host__ __device__ inline const Cst<R>& cst(const DevParams& P);
@@ -124,6 +125,7 @@ struct GhostChain {
     int nmirror;        // number of wall mirrors applied (velocity sign flips)
     int iso_face;       // last isothermal wall face applied, -1 if none
     bool nontrivial;    // a wall or Dirichlet rule is in the chain (U ghost = prim2c(Q))
+    long long poff, pst; // inflow-profile chains: transverse offset and plane size
 };
 
 __device__ __forceinline__ int ghost_src(int kind, bool high, int g, int N) {
@@ -137,6 +139,8 @@ __device__ __forceinline__ int ghost_src(int kind, bool high, int g, int N) {
 
 __device__ __forceinline__ GhostChain resolve_ghost(const DevParams& P, int i, int j, int k) {
     GhostChain c;
+    c.poff = 0;
+    c.pst = 0;
     c.dirichlet = -1;
     c.nmirror = 0;
     c.iso_face = -1;
@@ -151,9 +155,16 @@ __device__ __forceinline__ GhostChain resolve_ghost(const DevParams& P, int i, i
         const bool lo = g < NG, hi = g >= N[d] + NG;
         if (!lo && !hi) continue;
         const BcDev& b = P.bc[2 * d + (hi ? 1 : 0)];
-        if (b.kind == F3D_BC_DIRICHLET) {
+        if (b.kind == F3D_BC_DIRICHLET || b.kind == F3D_BC_INFLOW_PROFILE) {
             c.dirichlet = 2 * d + (hi ? 1 : 0);
             c.nontrivial = true;
+            if (b.kind == F3D_BC_INFLOW_PROFILE) {
+                // transverse point where the chain reaches this face's pass
+                const int a = d == 0 ? idx[1] : idx[0], bb = d == 2 ? idx[1] : idx[2];
+                const long long ta = d == 0 ? P.nyt : P.nxt, tb = d == 2 ? P.nyt : P.nzt;
+                c.poff = a + ta * bb;
+                c.pst = ta * tb;
+            }
             break;
         }
         if (b.kind == F3D_BC_WALL_ADIABATIC || b.kind == F3D_BC_WALL_ISOTHERMAL) {
@@ -176,7 +187,13 @@ __device__ __forceinline__ GhostChain resolve_ghost(const DevParams& P, int i, i
 __device__ __forceinline__ void apply_chain(const DevParams& P, const GhostChain& c, double q[6]) {
     if (c.dirichlet >= 0) {
         const BcDev& b = P.bc[c.dirichlet];
-        q[0] = b.rho; q[1] = b.u; q[2] = b.v; q[3] = b.w; q[4] = b.p; q[5] = b.T;
+        if (b.kind == F3D_BC_INFLOW_PROFILE) {
+            const double* pr = P.prof[c.dirichlet] + c.poff;
+            q[0] = pr[0]; q[1] = pr[c.pst]; q[2] = pr[2 * c.pst]; q[3] = pr[3 * c.pst]; q[4] = pr[4 * c.pst];
+            q[5] = q[4] / __dmul_rn(q[0], P.rg);
+        } else {
+            q[0] = b.rho; q[1] = b.u; q[2] = b.v; q[3] = b.w; q[4] = b.p; q[5] = b.T;
+        }
     }
     if (c.nmirror & 1) {
         q[1] = -q[1];

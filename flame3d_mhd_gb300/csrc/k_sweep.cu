@@ -184,7 +184,7 @@ template <> __device__ __forceinline__ float split_sound<float>(const DevParams&
 }
 
 template <int DIR, bool CHAR, class R>
-__global__ void __launch_bounds__(SWEEP_THREADS) k_sweep(const SweepArgs a) {
+__global__ void __launch_bounds__(SWEEP_THREADS, (sizeof(R) == 4 ? 3 : 2)) k_sweep(const SweepArgs a) {
     constexpr int TL = Tile<DIR>::TL, TC = Tile<DIR>::TC, NP = TC + 8, NF = TC + 1;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;

@@ -67,6 +67,11 @@ extern "C" int f3d_rhs_noalloc(const f3d_params* p, const double* const metrics[
         std::fprintf(stderr, "f3d_rhs_noalloc: %s\n", why.c_str());
         return rc;
     }
+    for (int f = 0; f < 6; f++)
+        if (p->bc[f].kind == F3D_BC_INFLOW_PROFILE) {
+            std::fprintf(stderr, "f3d_rhs_noalloc: inflow-profile faces need a context\n");
+            return F3D_ERR_UNSUPPORTED;
+        }
     if (p->precision != F3D_PREC_FP64) {
         std::fprintf(stderr, "f3d_rhs_noalloc: only the FP64 form is available without a context\n");
         return F3D_ERR_UNSUPPORTED;

@@ -12,6 +12,7 @@ CUDA kernels of libflame3d_gpu.so, and a missing library or a non-CUDA tensor ra
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 
 import torch
@@ -20,6 +21,22 @@ from . import abi
 from .abi import F3DError, F3DParams
 
 NG = 4
+
+
+@contextlib.contextmanager
+def side_stream(stream: torch.cuda.Stream | None = None):
+    """Run the enclosed calls on a side stream (f3d_rk3_steps captures its step into a CUDA
+    graph only on a non-default stream), ordered after the work already queued on the
+    current stream; on exit the current stream is ordered after the side stream's work.
+    PyTorch's pool streams are non-blocking: without these waits the side stream's kernels
+    could start before the set-up launched on the default stream (metrics, ghost fill,
+    host-to-device copies) has finished."""
+    cur = torch.cuda.current_stream()
+    s = stream if stream is not None else torch.cuda.Stream()
+    s.wait_stream(cur)
+    with torch.cuda.stream(s):
+        yield s
+    cur.wait_stream(s)
 
 
 class Flame3D:
@@ -100,6 +117,22 @@ class Flame3D:
         arr = (C.c_void_p * 9)(*[self._ptr(m, 1) for m in metrics])
         self._check(self.lib.f3d_set_metrics(self._h, arr, self._ptr(J, 1), self._stream()))
         self.metrics, self.J = list(metrics), J  # keep the borrowed arrays alive
+
+    def profile_shape(self, face: int) -> tuple[int, int, int]:
+        """(5, Tb, Ta) of an inflow-profile face: its transverse extent including ghosts."""
+        nxt, nyt, nzt = self.shape3[2], self.shape3[1], self.shape3[0]
+        d = face // 2
+        return (5, nzt, nyt) if d == 0 else ((5, nzt, nxt) if d == 1 else (5, nyt, nxt))
+
+    def set_inflow_profile(self, face: int, prof: torch.Tensor):
+        """Per-point (rho, u, v, w, p) of an F3D_BC_INFLOW_PROFILE face (borrowed)."""
+        if not (prof.is_cuda and prof.dtype == torch.float64 and prof.is_contiguous()):
+            raise TypeError("profile must be a contiguous float64 CUDA tensor")
+        if tuple(prof.shape) != self.profile_shape(face):
+            raise ValueError(f"expected shape {self.profile_shape(face)}, got {tuple(prof.shape)}")
+        self._check(self.lib.f3d_set_inflow_profile(self._h, face, C.c_void_p(prof.data_ptr()), self._stream()))
+        self._profiles = getattr(self, "_profiles", {})
+        self._profiles[face] = prof  # keep the borrowed array alive
 
     def compute_metrics(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor):
         """Metrics and J from coordinates on the device (parse_mesh.jl:139-248)."""

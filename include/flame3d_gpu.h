@@ -61,6 +61,10 @@ extern "C" {
 #define F3D_BC_ZERO_GRADIENT 2   /* copy the adjacent interior layer, boundary.jl:42-51             */
 #define F3D_BC_WALL_ADIABATIC 3  /* mirror: rho,p,T even, u,v,w odd, boundary.jl:67-93             */
 #define F3D_BC_WALL_ISOTHERMAL 4 /* mirror u,v,w odd, p even, T = 2 T_wall - T_in, rho = p/(Rg T)  */
+#define F3D_BC_INFLOW_PROFILE 5  /* Dirichlet with (rho,u,v,w,p) per boundary point from a caller
+                                    array (f3d_set_inflow_profile); T = p/(rho Rg). The inlet
+                                    rule of boundary.jl:10-38 with a per-point state, as fed by an
+                                    inflow file (SCU-benchmark/flow-inlet.dat)                 */
 
 typedef struct f3d_bc {
     int32_t kind;
@@ -189,6 +193,16 @@ int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream);
  * CuArrays (solver.jl:293-337). */
 int f3d_rhs_noalloc(const f3d_params* p, const double* const metrics[9], const double* jac,
                     const double* Q, double* dUdt, f3d_stream stream);
+
+/* Borrow the state of an F3D_BC_INFLOW_PROFILE face (0..5 = x-, x+, y-, y+, z-, z+): a
+ * device array of 5 x Ta x Tb doubles, variable-major (rho, u, v, w, p), each plane indexed
+ * a + Ta * b over the full transverse extent including ghosts: (a, b) = (j, k) with
+ * Ta = Ny+8 on x faces, (i, k) with Ta = Nx+8 on y faces, (i, j) with Ta = Nx+8 on z faces.
+ * Every ghost layer of the face takes the state of its transverse point. While a face of
+ * that kind has no profile, f3d_fill_ghosts and every call that needs the metrics return
+ * F3D_ERR_STATE. The caller keeps the array alive and may rewrite it between calls (the
+ * kernels read it at each launch). */
+int f3d_set_inflow_profile(f3d_ctx* ctx, int face, const double* prof, f3d_stream stream);
 
 /* ---- discrete adjoint (FP64, component-wise reconstruction, SW or LF splitting) ---- */
 

@@ -22,6 +22,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include "../include/flame3d_gpu.h"
@@ -213,6 +214,13 @@ void fill_ghost_cell(const f3d_params& P, const Consts<R>& C, const f3d_bc& bc, 
     }
 }
 
+// Per-point inflow states of F3D_BC_INFLOW_PROFILE faces (5 x Ta x Tb doubles each, the
+// layout of f3d_set_inflow_profile), registered by orc_set_inflow_profile.
+inline const double*& inflow_profile(int face) {
+    static const double* prof[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return prof[face];
+}
+
 // Source layer (1-based index along the direction) of ghost layer g for a face rule.
 inline long ghost_source(int kind, bool high, long g, long N, long NG) {
     if (kind == F3D_BC_PERIODIC) return high ? g - N : g + N;           // mpi.jl:105-282
@@ -246,6 +254,21 @@ template <class R> void fill_ghosts(const f3d_params& P, R* Qp, R* Up) {
                         if (d == 0) { gi = gg; gj = a; gk = b; si = s; sj = a; sk = b; }
                         else if (d == 1) { gi = a; gj = gg; gk = b; si = a; sj = s; sk = b; }
                         else { gi = a; gj = b; gk = gg; si = a; sj = b; sk = s; }
+                        if (bc.kind == F3D_BC_INFLOW_PROFILE) {
+                            // the inlet of boundary.jl:10-38 with the state of this point
+                            const double* pr = inflow_profile(2 * d + side);
+                            const long st = ta * tb, off = (a - 1) + ta * (b - 1);
+                            f3d_bc pb = bc;
+                            pb.kind = F3D_BC_DIRICHLET;
+                            if (pr) {
+                                pb.rho = pr[off]; pb.u = pr[off + st]; pb.v = pr[off + 2 * st];
+                                pb.w = pr[off + 3 * st]; pb.p = pr[off + 4 * st];
+                            } else {  // not registered: poison the ghosts so the caller sees it
+                                pb.rho = pb.u = pb.v = pb.w = pb.p = std::numeric_limits<double>::quiet_NaN();
+                            }
+                            fill_ghost_cell(P, C, pb, Q, U, gi, gj, gk, si, sj, sk);
+                            continue;
+                        }
                         fill_ghost_cell(P, C, bc, Q, U, gi, gj, gk, si, sj, sk);
                     }
         }

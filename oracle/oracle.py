@@ -35,7 +35,24 @@ def lib() -> C.CDLL:
         _lib = C.CDLL(str(LIB))
         _lib.orc_set_threads.restype = C.c_int
         _lib.orc_set_threads.argtypes = [C.c_int]
+        _lib.orc_set_inflow_profile.restype = None
+        _lib.orc_set_inflow_profile.argtypes = [C.c_int, C.c_void_p]
     return _lib
+
+
+_profiles: dict = {}
+
+
+def set_inflow_profile(face: int, prof: np.ndarray | None) -> None:
+    """Register the (5, Tb, Ta) state of an inflow-profile face for every oracle call
+    (the layout of f3d_set_inflow_profile); None clears it."""
+    if prof is None:
+        _profiles.pop(face, None)
+        lib().orc_set_inflow_profile(face, None)
+        return
+    a = np.ascontiguousarray(prof, dtype=np.float64)
+    _profiles[face] = a  # keep it alive while registered
+    lib().orc_set_inflow_profile(face, a.ctypes.data)
 
 
 def set_threads(n: int) -> int:

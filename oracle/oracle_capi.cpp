@@ -21,6 +21,11 @@ int orc_set_threads(int n) {
     return omp_get_max_threads();
 }
 
+// Register (or clear, with nullptr) the state array of an inflow-profile face.
+void orc_set_inflow_profile(int face, const double* prof) {
+    if (face >= 0 && face < 6) inflow_profile(face) = prof;
+}
+
 void orc_c2prim(const f3d_params* P, const double* U, double* Q) { c2prim<double>(*P, U, Q); }
 void orc_prim2c(const f3d_params* P, const double* Q, double* U) { prim2c<double>(*P, Q, U); }
 void orc_lincomb(const f3d_params* P, double* U, const double* Un, double a, double b) {

@@ -17,7 +17,7 @@ import torch
 from conftest import rel_linf
 from flame3d_mhd_gb300 import cases
 from flame3d_mhd_gb300.abi import BC_PERIODIC, PREC_MIXED, make_params
-from flame3d_mhd_gb300.solver import Flame3D
+from flame3d_mhd_gb300.solver import Flame3D, side_stream
 from oracle import oracle as orc
 from test_gpu_parity import curvilinear_coords, dev, host, random_state
 
@@ -78,8 +78,7 @@ def _run(P, m, J, Q, U, dt, steps):
     s = Flame3D(P)
     s.set_metrics([dev(a) for a in m], dev(J))
     Ud, Und, Qd = dev(U), dev(np.zeros_like(U)), dev(Q)
-    stream = torch.cuda.Stream()
-    with torch.cuda.stream(stream):
+    with side_stream() as stream:
         s.time_step(Ud, Und, Qd, dt, steps)
     stream.synchronize()
     out = host(Ud), host(Qd)

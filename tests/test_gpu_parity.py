@@ -12,7 +12,7 @@ from conftest import rel_linf
 from flame3d_mhd_gb300 import cases
 from flame3d_mhd_gb300.abi import (BC_DIRICHLET, BC_PERIODIC, BC_WALL_ADIABATIC, BC_WALL_ISOTHERMAL,
                                    BC_ZERO_GRADIENT, make_params)
-from flame3d_mhd_gb300.solver import Flame3D
+from flame3d_mhd_gb300.solver import Flame3D, side_stream
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
@@ -293,8 +293,7 @@ def test_rk3_steps_parity(gpu_lib, name):
     dt = 1e-3 if name.startswith("tgv") else 2e-4
     steps = 10
     U, Un, Q = dev(c.U), torch.zeros_like(dev(c.U)), dev(c.Q)
-    stream = torch.cuda.Stream()
-    with torch.cuda.stream(stream):
+    with side_stream() as stream:
         c.s.time_step(U, Un, Q, dt, steps)  # graph-captured
     stream.synchronize()
     Uo, Uno, Qo = c.U.copy(), np.zeros_like(c.U), c.Q.copy()
