@@ -22,6 +22,7 @@ NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 SPLIT_SW, SPLIT_LF, SPLIT_VL, SPLIT_AUSM = 0, 1, 2, 3
 SPLIT_NAMES = {"SW": SPLIT_SW, "LF": SPLIT_LF, "VL": SPLIT_VL, "AUSM": SPLIT_AUSM}
 PREC_FP64, PREC_MIXED = 0, 1
+SCHEME_FDM, SCHEME_FVM_EIGEN, SCHEME_FVM_CONS = 0, 1, 2
 BC_PERIODIC, BC_DIRICHLET, BC_ZERO_GRADIENT, BC_WALL_ADIABATIC, BC_WALL_ISOTHERMAL = 0, 1, 2, 3, 4
 BC_INFLOW_PROFILE = 5
 
@@ -39,11 +40,11 @@ class F3DParams(C.Structure):
                 ("t_s", C.c_double), ("pr", C.c_double), ("phi1", C.c_double), ("phi2", C.c_double),
                 ("phi3", C.c_double), ("linear_phi", C.c_double), ("clamp_eps", C.c_double),
                 ("split_method", C.c_int32), ("character", C.c_int32), ("viscous", C.c_int32),
-                ("precision", C.c_int32), ("bc", F3DBc * 6)]
+                ("precision", C.c_int32), ("bc", F3DBc * 6), ("scheme", C.c_int32), ("pad2_", C.c_int32)]
 
 
 def params_to_dict(p: F3DParams) -> dict:
-    d = {f: getattr(p, f) for f, _ in F3DParams._fields_ if f != "bc"}
+    d = {f: getattr(p, f) for f, _ in F3DParams._fields_ if f not in ("bc", "pad2_")}
     d["bc"] = [{f: getattr(b, f) for f, _ in F3DBc._fields_ if f != "pad_"} for b in p.bc]
     return d
 
@@ -124,6 +125,7 @@ def load() -> C.CDLL:
         "f3d_rhs_vjp": (ip, [vp, vp, vp, vp, vp]),
         "f3d_rk3_step_vjp": (ip, [vp, C.c_double, vp, vp, vp, vp]),
         "f3d_set_inflow_profile": (ip, [vp, ip, vp, vp]),
+        "f3d_set_coordinates": (ip, [vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -139,7 +141,8 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_lincomb", "f3d_fill_ghosts", "f3d_rhs", "f3d_rk3_stage", "f3d_rk3_steps", "f3d_cfl_dt",
             "f3d_check_finite", "f3d_debug_sensor", "f3d_debug_split", "f3d_debug_face_flux",
             "f3d_debug_viscous", "f3d_div", "f3d_measure_pipes", "f3d_kernel_count", "f3d_kernel_name",
-            "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp", "f3d_set_inflow_profile"]
+            "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp", "f3d_set_inflow_profile",
+            "f3d_set_coordinates"]
 
 
 class F3DError(RuntimeError):

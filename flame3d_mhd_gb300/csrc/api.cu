@@ -42,6 +42,11 @@ int validate_params(const f3d_params& p, std::string& why) {
     if (p.character != 0 && p.character != 1) { why = "character must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
+    if (p.scheme < F3D_SCHEME_FDM || p.scheme > F3D_SCHEME_FVM_CONS) { why = "unknown scheme"; return F3D_ERR_ARG; }
+    if (p.scheme != F3D_SCHEME_FDM && p.precision != F3D_PREC_FP64) {
+        why = "the finite-volume schemes are built for FP64";
+        return F3D_ERR_UNSUPPORTED;
+    }
     int iso_dirs = 0;
     for (int d = 0; d < 3; d++) {
         const f3d_bc &lo = p.bc[2 * d], &hi = p.bc[2 * d + 1];
@@ -138,6 +143,11 @@ struct f3d_ctx {
     double* phi = nullptr;
     double* acc = nullptr;
     double* Fv[3] = {};
+    // finite-volume schemes: face normals and areas (nx, ny, nz, area per direction) and
+    // the conserved state f3d_rhs reconstructs from (prim2c of its Q)
+    double* geo[12] = {};
+    double* Ufv = nullptr;
+    bool coords_set = false;
     // mixed precision: FP32 copies and FP32 intermediates
     float* Q32 = nullptr;
     MetricPtrs32 m32 = {};
@@ -200,6 +210,8 @@ int check_ptrs(f3d_ctx* ctx, std::initializer_list<const void*> ps) {
 int check_ctx(f3d_ctx* ctx, bool need_state) {
     if (!ctx) return F3D_ERR_ARG;
     if (need_state && !ctx->metrics_set) return fail(ctx, F3D_ERR_STATE, "metrics not set (call f3d_set_metrics)");
+    if (need_state && ctx->params.scheme != F3D_SCHEME_FDM && !ctx->coords_set)
+        return fail(ctx, F3D_ERR_STATE, "coordinates not set (call f3d_set_coordinates)");
     for (int f = 0; f < 6 && need_state; f++)
         if (ctx->params.bc[f].kind == F3D_BC_INFLOW_PROFILE && !ctx->dp.prof[f])
             return fail(ctx, F3D_ERR_STATE, "inflow profile not set (call f3d_set_inflow_profile)");
@@ -247,7 +259,44 @@ SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const 
 // Sensor, viscous fluxes and the three sweeps. last.out_mode is OUT_RHS or OUT_STAGE.
 // Mixed precision: the FP32 copy of Q is made first unless q32_current says the previous
 // stage's primitive fill already wrote it.
+// Finite-volume RHS (FVM.jl): sensor, viscous fluxes, three face sweeps reconstructing the
+// conserved state (the stage's U, or prim2c(Q) for f3d_rhs) and, for a stage, the RK update
+// after the last sweep (the sweeps read U, so it cannot be updated inside them).
+int run_rhs_fvm(f3d_ctx* ctx, const double* Q, double* acc, const SweepArgs& last, cudaStream_t st) {
+    const DevParams& P = ctx->dp;
+    const bool hybrid = P.fixed_branch < 0;
+    const bool stage = last.out_mode == OUT_STAGE;
+    const double* U = stage ? last.U : ctx->Ufv;
+    if (!stage) F3D_CUDA(ctx, launch_prim2c(P, Q, ctx->Ufv, st));
+    if (hybrid) {
+        F3D_CUDA(ctx, launch_sensor(P, Q, ctx->phi, st));
+        mark(ctx, K_SENSOR, st);
+    }
+    if (ctx->params.viscous) {
+        F3D_CUDA(ctx, launch_viscous(P, Q, ctx->m, ctx->J, ctx->Fv[0], ctx->Fv[1], ctx->Fv[2], st));
+        mark(ctx, K_VISCOUS, st);
+    }
+    const bool eigen = ctx->params.scheme == F3D_SCHEME_FVM_EIGEN;
+    for (int d = 0; d < 3; d++) {
+        SweepArgs a = sweep_args(ctx, d, Q, hybrid);
+        a.acc = acc;
+        a.out = acc;
+        a.out_mode = d == 0 ? OUT_SET : OUT_ADD;
+        if (d == 2 && !stage) {
+            a.out_mode = last.out_mode;
+            a.out = last.out;
+        }
+        F3D_CUDA(ctx, launch_fvm_sweep(d, eigen, a, U, ctx->geo, st));
+        mark(ctx, K_SWEEP_X + d, st);
+    }
+    if (stage)
+        F3D_CUDA(ctx, launch_stage_update(P, acc, ctx->J, last.dt, last.U, last.Un, last.stage1_copy, last.combine,
+                                          last.ca, last.cb, st));
+    return F3D_OK;
+}
+
 int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStream_t st, bool q32_current = false) {
+    if (ctx->params.scheme != F3D_SCHEME_FDM) return run_rhs_fvm(ctx, Q, acc, last, st);
     const DevParams& P = ctx->dp;
     const bool hybrid = P.fixed_branch < 0;
     const bool mx = mixed(ctx);
@@ -322,6 +371,8 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
 // ---- discrete adjoint ------------------------------------------------------------------
 int adjoint_supported(f3d_ctx* ctx) {
     if (mixed(ctx)) return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for the FP64 form");
+    if (ctx->params.scheme != F3D_SCHEME_FDM)
+        return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for the finite-difference scheme");
     if (ctx->params.character) return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for component-wise reconstruction");
     if (ctx->params.split_method != F3D_SPLIT_SW && ctx->params.split_method != F3D_SPLIT_LF)
         return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for SW and LF splitting");
@@ -461,8 +512,9 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const bool mx = p->precision == F3D_PREC_MIXED;
     size_t total = 256;
-    if (!mx) {  // S(3) + A/|A|(9) + sound speed + phi + acc(5) [+ viscous 12]
-        total += up(nc * 8) * (3 + 9 + 1 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 8) : 0);
+    const bool fvm = p->scheme != F3D_SCHEME_FDM;
+    if (!mx) {  // S(3) + A/|A|(9) + sound speed + phi + acc(5) [+ viscous 12] [+ FVM 12 + 5]
+        total += up(nc * 8) * (3 + 9 + 1 + 1 + 5 + (fvm ? 17 : 0)) + (p->viscous ? 3 * up(nv * 4 * 8) : 0);
     } else {    // Q32(6) + A32(9) + H32(9) + S32(3) + J32 + phi32 + acc32(5) [+ viscous 12]
         total += up(nc * 4) * (6 + 9 + 9 + 3 + 1 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 4) : 0);
     }
@@ -484,6 +536,10 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
         ctx->acc = (double*)q; q += 5 * b1;
         if (p->viscous)
             for (int d = 0; d < 3; d++) { ctx->Fv[d] = (double*)q; q += up(nv * 4 * 8); }
+        if (fvm) {
+            for (int n = 0; n < 12; n++) { ctx->geo[n] = (double*)q; q += b1; }
+            ctx->Ufv = (double*)q; q += 5 * b1;
+        }
         phi_bytes = b1;
     } else {
         const size_t b1 = up(nc * 4);
@@ -501,7 +557,7 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     ctx->dscalar = (double*)q;
     // phi outside cells 1..Nt-2 is never written; keep it defined (CUDA.zeros in solver.jl:296)
     if ((e = cudaMemset(mx ? (void*)ctx->phi32 : (void*)ctx->phi, 0, phi_bytes)) != cudaSuccess ||
-        (e = sweep_configure()) != cudaSuccess) {
+        (e = sweep_configure()) != cudaSuccess || (fvm && (e = fvm_configure()) != cudaSuccess)) {
         cudaFree(ctx->slab);
         delete ctx;
         std::fprintf(stderr, "f3d_create: %s\n", cudaGetErrorString(e));
@@ -648,6 +704,16 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
         ctx->g_dt = dt;
     }
     for (int t = 0; t < nsteps; t++) F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
+    return F3D_OK;
+}
+
+int f3d_set_coordinates(f3d_ctx* ctx, const double* x, const double* y, const double* z, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {x, y, z}))) return rc;
+    if (ctx->params.scheme == F3D_SCHEME_FDM) return F3D_OK;
+    F3D_CUDA(ctx, launch_face_geometry(ctx->dp, x, y, z, ctx->geo, (cudaStream_t)stream));
+    ctx->coords_set = true;
+    drop_step_graph(ctx);
     return F3D_OK;
 }
 
@@ -800,6 +866,15 @@ int f3d_debug_face_flux(f3d_ctx* ctx, int dir, const double* Q, const double* ph
     if (hybrid && !phi) return fail(ctx, F3D_ERR_ARG, "hybrid thresholds need phi");
     if (mixed(ctx)) return fail(ctx, F3D_ERR_UNSUPPORTED, "stage intermediates are FP64-only");
     cudaStream_t st = (cudaStream_t)stream;
+    if (ctx->params.scheme != F3D_SCHEME_FDM) {  // FVM.jl face fluxes from U = prim2c(Q)
+        F3D_CUDA(ctx, launch_prim2c(ctx->dp, Q, ctx->Ufv, st));
+        SweepArgs a = sweep_args(ctx, dir, Q, hybrid, phi);
+        a.out_mode = OUT_FACES;
+        a.faces = F;
+        a.Fv = nullptr;
+        F3D_CUDA(ctx, launch_fvm_sweep(dir, ctx->params.scheme == F3D_SCHEME_FVM_EIGEN, a, ctx->Ufv, ctx->geo, st));
+        return F3D_OK;
+    }
     F3D_CUDA(ctx, launch_sound(ctx->dp, Q, ctx->csnd, st));
     SweepArgs a = sweep_args(ctx, dir, Q, hybrid, phi);
     a.out_mode = OUT_FACES;

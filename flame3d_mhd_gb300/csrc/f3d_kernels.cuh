@@ -67,6 +67,16 @@ DevParams make_dev_params(const f3d_params& p);
 cudaError_t sweep_configure();
 cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st);
 
+// finite-volume scheme (k_fvm.cu): geo = (nx, ny, nz, area) of the faces of x, y, z at
+// their left cells; U the conserved state the faces reconstruct from
+cudaError_t fvm_configure();
+cudaError_t launch_face_geometry(const DevParams& P, const double* x, const double* y, const double* z,
+                                 double* const geo[12], cudaStream_t st);
+cudaError_t launch_fvm_sweep(int dir, bool eigen, const SweepArgs& a, const double* U, const double* const geo[12],
+                             cudaStream_t st);
+cudaError_t launch_stage_update(const DevParams& P, const double* acc, const double* J, double dt, double* U,
+                                double* Un, int stage1_copy, int combine, double ca, double cb, cudaStream_t st);
+
 // metric pointer bundles (passed by value to kernels)
 struct MetricPtrs {
     const double* m[9];

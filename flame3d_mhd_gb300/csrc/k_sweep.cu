@@ -15,6 +15,7 @@
 // [var][pos][line] for d = y, z (threads run across x-adjacent lines), so global loads
 // coalesce along i and shared loads are conflict-free in both cases.
 #include "f3d_kernels.cuh"
+#include "f3d_sweep_epilogue.cuh"
 
 namespace f3d {
 
@@ -150,27 +151,6 @@ __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a
     out[4] = flux[0] * (H - qn * c) + flux[1] * q2 + flux[2] * (H + qn * c) + flux[3] * ql + flux[4] * qm;
 }
 
-// Branch of a face from the sensor values of cells i-3..i+2 (schemes.jl:112-117 and
-// :119, :143, :231): the FP64 values compare as bit patterns (see DevParams::phib), FP32
-// values directly. NaN fails every comparison and selects NND2, like the reference.
-__device__ __forceinline__ int branch_of(const DevParams& P, const double* ph) {
-    unsigned long long m = __double_as_longlong(ph[0]);
-#pragma unroll
-    for (int o = 1; o < 6; o++) {
-        unsigned long long b = __double_as_longlong(ph[o]);
-        m = b > m ? b : m;
-    }
-    return m < P.phib[0] ? 0 : (m < P.phib[1] ? 1 : (m < P.phib[2] ? 2 : 3));
-}
-__device__ __forceinline__ int branch_of(const DevParams& P, const float* ph) {
-    float m = ph[0];
-#pragma unroll
-    for (int o = 1; o < 6; o++) m = fmaxf(m, ph[o]);
-    const Cst<float>& K = P.cf;
-    int br = m < K.phi1 ? 0 : (m < K.phi2 ? 1 : (m < K.phi3 ? 2 : 3));
-    return m != m ? 3 : br;
-}
-
 // Sound speed for the split: precomputed per cell in FP64; computed in place in FP32.
 template <class R> __device__ __forceinline__ R split_sound(const DevParams& P, const SweepArgs& a, long long c,
                                                             const R q[6]);
@@ -304,57 +284,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS, (sizeof(R) == 4 ? 3 : 2)) k_swe
     if (a.out_mode == OUT_FACES) return;
     __syncthreads();
 
-    // ---- Phase C: cells t = 0..nc-1 (full position c0 + t + NG).
-    const int vxt = P.nxt - 4, vyt = P.nyt - 4, vzt = P.nzt - 4;
-    const long long vplane = (long long)vxt * vyt * vzt;
-    R* acc = static_cast<R*>(a.acc);
-    const R* Fvr = static_cast<const R*>(a.Fv);
-    for (int it = threadIdx.x; it < TL * TC; it += SWEEP_THREADS) {
-        int l, t;
-        if (DIR == 0) { l = it / TC; t = it - l * TC; } else { t = it / TL; l = it - t * TL; }
-        if (l >= nl || t >= nc) continue;
-        const long long c = cell(l, c0 + t + NG);
-        R d[5];
-#pragma unroll
-        for (int n = 0; n < 5; n++) d[n] = sF[n * TL * NF + fidx(l, t)] - sF[n * TL * NF + fidx(l, t + 1)];
-        if (Fvr) {
-            // Fv index = full index - 2 in every dimension (viscous.jl:119, div.jl:14-39)
-            long long vi, vj, vk;
-            const int g = c0 + t + NG - 2;
-            if (DIR == 0) { vi = g; vj = l0 + l + NG - 2; vk = other + NG - 2; }
-            else if (DIR == 1) { vi = l0 + l + NG - 2; vj = g; vk = other + NG - 2; }
-            else { vi = l0 + l + NG - 2; vj = other + NG - 2; vk = g; }
-            const long long vc = vi + (long long)vxt * (vj + (long long)vyt * vk);
-            const long long vs = DIR == 0 ? 1 : (DIR == 1 ? (long long)vxt : (long long)vxt * vyt);
-            const R k1 = R(1) / R(12), k2 = R(-2) / R(3);
-#pragma unroll
-            for (int n = 0; n < 4; n++) {
-                const R* F = Fvr + n * vplane + vc;
-                d[n + 1] += k1 * (F[-2 * vs] - F[2 * vs]) + k2 * (F[-vs] - F[vs]);
-            }
-        }
-        if (a.out_mode == OUT_SET) {
-#pragma unroll
-            for (int n = 0; n < 5; n++) acc[c + n * pl] = d[n];
-        } else if (a.out_mode == OUT_ADD) {
-#pragma unroll
-            for (int n = 0; n < 5; n++) acc[c + n * pl] += d[n];
-        } else if (a.out_mode == OUT_RHS) {
-            const double Jc = a.J[c];
-#pragma unroll
-            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * (double)(acc[c + n * pl] + d[n]);
-        } else {  // OUT_STAGE: RK state accumulation in FP64
-            const double Jact = a.J[c] * a.dt;
-#pragma unroll
-            for (int n = 0; n < 5; n++) {
-                const double u = a.U[c + n * pl];
-                if (a.stage1_copy) a.Un[c + n * pl] = u;
-                double un = u + (double)(acc[c + n * pl] + d[n]) * Jact;
-                if (a.combine) un = un * a.ca + a.Un[c + n * pl] * a.cb;
-                a.U[c + n * pl] = un;
-            }
-        }
-    }
+    // ---- Phase C: differences, viscous terms and the accumulation of out_mode.
+    sweep_epilogue<DIR, TL, TC, SWEEP_THREADS, R>(a, sF, c0, l0, other, nc, nl, cell, fidx);
 }
 
 template <int DIR, bool CHAR, class R> static cudaError_t configure_dir() {

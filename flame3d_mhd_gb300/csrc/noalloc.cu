@@ -67,6 +67,10 @@ extern "C" int f3d_rhs_noalloc(const f3d_params* p, const double* const metrics[
         std::fprintf(stderr, "f3d_rhs_noalloc: %s\n", why.c_str());
         return rc;
     }
+    if (p->scheme != F3D_SCHEME_FDM) {
+        std::fprintf(stderr, "f3d_rhs_noalloc: the finite-volume schemes need a context (coordinates)\n");
+        return F3D_ERR_UNSUPPORTED;
+    }
     for (int f = 0; f < 6; f++)
         if (p->bc[f].kind == F3D_BC_INFLOW_PROFILE) {
             std::fprintf(stderr, "f3d_rhs_noalloc: inflow-profile faces need a context\n");

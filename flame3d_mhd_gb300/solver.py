@@ -118,6 +118,12 @@ class Flame3D:
         self._check(self.lib.f3d_set_metrics(self._h, arr, self._ptr(J, 1), self._stream()))
         self.metrics, self.J = list(metrics), J  # keep the borrowed arrays alive
 
+    def set_coordinates(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor):
+        """Ghost-filled cell-centre coordinates for the finite-volume schemes: face normals
+        and areas (FVM.jl:16-29) are computed from them once (a no-op for the FDM scheme)."""
+        self._check(self.lib.f3d_set_coordinates(self._h, self._ptr(x, 1), self._ptr(y, 1), self._ptr(z, 1),
+                                                 self._stream()))
+
     def profile_shape(self, face: int) -> tuple[int, int, int]:
         """(5, Tb, Ta) of an inflow-profile face: its transverse extent including ghosts."""
         nxt, nyt, nzt = self.shape3[2], self.shape3[1], self.shape3[0]

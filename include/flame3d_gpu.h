@@ -48,6 +48,14 @@ extern "C" {
 #define F3D_SPLIT_VL 2   /* van Leer, split.jl:110-183      */
 #define F3D_SPLIT_AUSM 3 /* AUSM, split.jl:185-255          */
 
+/* right-hand-side family (run.jl:64-65 finite_volume / eigen_reconstruction) */
+#define F3D_SCHEME_FDM 0       /* flux splitting + hybrid reconstruction of the split fluxes
+                                  (split.jl, schemes.jl): the finite-difference path       */
+#define F3D_SCHEME_FVM_EIGEN 1 /* finite volume: Roe-averaged characteristic reconstruction
+                                  of U + HLLC (FVM.jl Eigen_reconstruct_*, HLLC_Flux)      */
+#define F3D_SCHEME_FVM_CONS 2  /* finite volume: component-wise reconstruction of U + HLLC
+                                  (FVM.jl Conser_reconstruct_*)                            */
+
 /* arithmetic of the flux kernels */
 #define F3D_PREC_FP64 0  /* everything in FP64: the drop-in, parity at 1e-12             */
 #define F3D_PREC_MIXED 1 /* FP32 split/reconstruction/weights/viscous; FP64 state, EOS,
@@ -90,6 +98,8 @@ typedef struct f3d_params {
     int32_t viscous;        /* 1: add viscous and heat fluxes (viscous.jl)               */
     int32_t precision;      /* F3D_PREC_*                                                */
     f3d_bc bc[6];           /* x-, x+, y-, y+, z-, z+                                    */
+    int32_t scheme;         /* F3D_SCHEME_*; the finite-volume schemes are FP64 only       */
+    int32_t pad2_;
 } f3d_params;
 
 typedef struct f3d_ctx f3d_ctx;
@@ -123,6 +133,13 @@ int f3d_scratch_bytes(const f3d_ctx* ctx, size_t* bytes);
 int f3d_set_metrics(f3d_ctx* ctx, const double* const metrics[9], const double* jac,
                     f3d_stream stream);
 
+/* Cell-centre coordinates (Nxt,Nyt,Nzt each, ghost layers filled as solver.jl:682-829
+ * extrapolates them) for the finite-volume schemes: the unit normal and area of every face
+ * (FVM.jl:16-29) are computed once here, in FP64, and kept in the context. Required before
+ * any call that needs the metrics when params.scheme is a finite-volume scheme (else
+ * F3D_ERR_STATE); a no-op for F3D_SCHEME_FDM. The arrays are read during this call only. */
+int f3d_set_coordinates(f3d_ctx* ctx, const double* x, const double* y, const double* z, f3d_stream stream);
+
 /* Compute metrics and J from coordinates x,y,z (Nxt,Nyt,Nzt with ghost coordinates) with
  * the CD6 / one-sided CD2 formulas of parse_mesh.jl:139-248, in FP64 on the device. */
 int f3d_compute_metrics(f3d_ctx* ctx, const double* x, const double* y, const double* z,
@@ -146,7 +163,9 @@ int f3d_fill_ghosts(f3d_ctx* ctx, double* Q, double* U, f3d_stream stream);
 /* dUdt = L(U) at interior cells (dUdt has the U layout; ghosts are not written) from a
  * ghost-filled Q: shock sensor, flux splitting and hybrid reconstruction in xi, eta,
  * zeta, viscous fluxes and the flux divergence (div.jl:1-50 without the dt factor).
- * Equals (U_after_div - U_before)/dt of one reference stage. */
+ * Equals (U_after_div - U_before)/dt of one reference stage. The finite-volume schemes
+ * reconstruct the conserved variables; here they take U = prim2c(Q) at every cell (the
+ * stage entries use the state U itself). */
 int f3d_rhs(f3d_ctx* ctx, const double* Q, double* dUdt, f3d_stream stream);
 
 /* One SSP-RK3 stage (stage = 1,2,3) exactly as solver.jl:416-444: stage 1 copies U to

@@ -38,6 +38,11 @@ template <class T> inline T jmax(const T& a, const T& b) {
     if (b != b) return b;
     return (a < b) ? b : a;
 }
+template <class T> inline T jmin(const T& a, const T& b) {
+    if (a != a) return a;
+    if (b != b) return b;
+    return (b < a) ? b : a;
+}
 template <class T> inline T sq(const T& a) { return a * a; }
 
 // minmod, schemes.jl:26-28
@@ -219,6 +224,13 @@ void fill_ghost_cell(const f3d_params& P, const Consts<R>& C, const f3d_bc& bc, 
 inline const double*& inflow_profile(int face) {
     static const double* prof[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     return prof[face];
+}
+
+// Cell-centre coordinates (x, y, z with ghosts) for the finite-volume schemes, registered
+// by orc_set_coordinates; every Solver of a finite-volume scheme copies them in its type.
+inline const double** coordinates() {
+    static const double* xyz[3] = {nullptr, nullptr, nullptr};
+    return xyz;
 }
 
 // Source layer (1-based index along the direction) of ghost layer g for a face rule.
@@ -763,14 +775,21 @@ template <class R> void metric_norm(size_t nc, const R* a, const R* b, const R* 
     for (long i = 0; i < (long)nc; i++) s[i] = sqrt(a[i] * a[i] + b[i] * b[i] + c[i] * c[i]);
 }
 
+}  // namespace f3do
+#include "f3d_oracle_fvm.hpp"
+namespace f3do {
+
 // ---------------------------------------------------------------------------------
 // Workspace and the composed RHS / RK3 stage (solver.jl:416-444 with flowAdvance).
+// The finite-volume schemes (params.scheme) reconstruct U: the stage's state, or prim2c(Q)
+// for a bare RHS; they need the cell-centre coordinates (set_coordinates).
 template <class R, class W> struct Solver {
     f3d_params P;
     Grid g;
     const R* m[9];
     const R* J;
-    std::vector<R> S[3], phi, Fp, Fm, F[3], Fv[3];
+    const R *xs = nullptr, *ys = nullptr, *zs = nullptr;
+    std::vector<R> S[3], phi, Fp, Fm, F[3], Fv[3], Uq, xyz[3];
     std::vector<int8_t> branch[3];
     bool record_branch = false;
 
@@ -787,13 +806,35 @@ template <class R, class W> struct Solver {
             branch[d].assign(nf, 0);
         }
         phi.assign(nc, R(0));  // CUDA.zeros: cells 1 and Nt are never written
+        if (P.scheme != F3D_SCHEME_FDM && coordinates()[0]) {
+            for (int a = 0; a < 3; a++) xyz[a].assign(coordinates()[a], coordinates()[a] + nc);
+            set_coordinates(xyz[0].data(), xyz[1].data(), xyz[2].data());
+        }
         Fp.assign(nc * 5, R(0));
         Fm.assign(nc * 5, R(0));
     }
 
+    void set_coordinates(const R* x, const R* y, const R* z) {
+        xs = x;
+        ys = y;
+        zs = z;
+    }
+
     // shockSensor + the flux part of flowAdvance: fills F[0..2] and Fv[0..2].
-    void fluxes(const R* Q) {
+    void fluxes(const R* Q, const R* U = nullptr) {
         sensor<R>(P, Q, phi.data());
+        if (P.scheme != F3D_SCHEME_FDM) {  // FVM.jl (solver.jl:21-31)
+            if (!U) {
+                Uq.assign(g.ncell() * 5, R(0));
+                prim2c<R>(P, Q, Uq.data());
+                U = Uq.data();
+            }
+            for (int d = 0; d < 3; d++)
+                fvm_face_flux<R>(P, d, P.scheme == F3D_SCHEME_FVM_EIGEN, phi.data(), S[d].data(), Q, U, xs, ys, zs,
+                                 F[d].data(), record_branch ? branch[d].data() : nullptr);
+            if (P.viscous) viscous<R>(P, Q, m, J, Fv[0].data(), Fv[1].data(), Fv[2].data());
+            return;
+        }
         for (int d = 0; d < 3; d++) {
             split<R>(P, Q, m[3 * d], m[3 * d + 1], m[3 * d + 2], S[d].data(), Fp.data(), Fm.data());
             face_flux<R, W>(P, d, phi.data(), S[d].data(), Fp.data(), Fm.data(), Q, m[3 * d], m[3 * d + 1],
@@ -813,7 +854,7 @@ template <class R, class W> struct Solver {
     void rk3_stage(int stage, R dt, R* U, R* Un, R* Q) {
         const size_t n5 = g.ncell() * 5;
         if (stage == 1) std::memcpy(Un, U, n5 * sizeof(R));
-        fluxes(Q);
+        fluxes(Q, U);
         const bool v = P.viscous != 0;
         divergence<R>(P, F[0].data(), F[1].data(), F[2].data(), v ? Fv[0].data() : nullptr,
                       v ? Fv[1].data() : nullptr, v ? Fv[2].data() : nullptr, J, dt, U, nullptr);

@@ -37,7 +37,34 @@ def lib() -> C.CDLL:
         _lib.orc_set_threads.argtypes = [C.c_int]
         _lib.orc_set_inflow_profile.restype = None
         _lib.orc_set_inflow_profile.argtypes = [C.c_int, C.c_void_p]
+        _lib.orc_set_coordinates.restype = None
+        _lib.orc_set_coordinates.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     return _lib
+
+
+_coords: list = []
+
+
+def set_coordinates(x: np.ndarray | None, y: np.ndarray | None = None, z: np.ndarray | None = None) -> None:
+    """Register the ghost-filled cell-centre coordinates the finite-volume schemes take
+    their face geometry from (every later oracle call of such a scheme); None clears them."""
+    if x is None:
+        _coords.clear()
+        lib().orc_set_coordinates(None, None, None)
+        return
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z)]
+    _coords[:] = arrs
+    lib().orc_set_coordinates(*[a.ctypes.data for a in arrs])
+
+
+def fvm_face_flux(P, d, eigen, phi, S, Q, U, x, y, z, with_branch=False):
+    """FVM.jl face fluxes of direction d in the Fx/Fy/Fz shape."""
+    F = np.zeros((5, *face_shape(P, d)))
+    br = np.zeros(face_shape(P, d), dtype=np.int8) if with_branch else None
+    xs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z)]
+    lib().orc_fvm_face_flux(C.byref(P), C.c_int(d), C.c_int(int(eigen)), _p(phi), _p(S), _p(Q), _p(U),
+                            _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(F), _p(br))
+    return (F, br) if with_branch else F
 
 
 _profiles: dict = {}

@@ -21,6 +21,21 @@ int orc_set_threads(int n) {
     return omp_get_max_threads();
 }
 
+// Register (or clear, with nullptrs) the cell-centre coordinates the finite-volume schemes
+// take their face geometry from.
+void orc_set_coordinates(const double* x, const double* y, const double* z) {
+    coordinates()[0] = x;
+    coordinates()[1] = y;
+    coordinates()[2] = z;
+}
+
+// FVM.jl face fluxes of direction dir (Fx/Fy/Fz shape) from ghost-filled Q and U.
+void orc_fvm_face_flux(const f3d_params* P, int dir, int eigen, const double* phi, const double* S, const double* Q,
+                       const double* U, const double* x, const double* y, const double* z, double* F,
+                       int8_t* branch) {
+    fvm_face_flux<double>(*P, dir, eigen != 0, phi, S, Q, U, x, y, z, F, branch);
+}
+
 // Register (or clear, with nullptr) the state array of an inflow-profile face.
 void orc_set_inflow_profile(int face, const double* prof) {
     if (face >= 0 && face < 6) inflow_profile(face) = prof;
