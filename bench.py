@@ -157,6 +157,20 @@ def cpu_sample(target_s: float = 12.0, max_steps: int = 8) -> dict:
                       f"{WORKLOAD['nz']} workload after 1 untimed step, {dt:.1f} s"}
 
 
+def workload_flops_per_cell() -> float:
+    """Floating-point operations of one RHS per interior cell on the workload, counted
+    exactly by the oracle's counting number type (add + mul + div + sqrt, an FMA counting
+    as two), with this workload's own branch mix."""
+    from flame3d_mhd_gb300 import cases
+    from oracle import oracle as orc
+    c = cases.sod(**WORKLOAD)
+    P = c["params"]
+    m, J, Q, _ = orc.prepare(P, c["Q"], c["x"], c["y"], c["z"])
+    oc = orc.rhs_opcount(P, Q, m, J)
+    cells = WORKLOAD["nx"] * WORKLOAD["ny"] * WORKLOAD["nz"]
+    return float(oc["add"] + oc["mul"] + oc["div"] + oc["sqrt"]) / cells
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -404,8 +418,19 @@ def run_ours(args):
         "clocks": clocks,
         "state_finite": bool(ok),
     }
+    # the FP64 form's binding roof is the FP64 pipe: achieved flop rate of the whole RHS
+    # against the FMA-chain peak measured on this GPU now
+    from flame3d_mhd_gb300.solver import measure_pipes
+    fp64_peak, fp32_peak = measure_pipes()
+    line["roofline_fp64_pipe"] = {"bound": "fp64", "peak": fp64_peak, "unit": "TFLOP/s", "fp32_peak": fp32_peak,
+                                  "achieved": None, "frac": None, "flops_per_cell_rhs": None,
+                                  "note": "flops from the oracle's exact op count (CPU leg); GPU divides "
+                                          "and square roots cost ~10 FMA slots each but count as 1"}
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample()
+        f = workload_flops_per_cell()
+        ach = f * value * 1e6 / ws / 1e12
+        line["roofline_fp64_pipe"].update(achieved=ach, frac=ach / fp64_peak, flops_per_cell_rhs=f)
     if rank == 0:
         print(json.dumps(line), flush=True)
     s.close()
