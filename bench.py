@@ -55,6 +55,11 @@ KERNEL_BYTES_PER_CELL = {
 # one RK3 step of the whole RHS: 3 x (U + 9 metrics + J read, U written) + 2 x Un read
 STEP_BYTES_PER_CELL = 3 * 160 + 2 * 40
 
+# DRAM bytes per interior cell of one launch in an RK3 stage, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on this workload: the stage-mode table of
+# profiles/k_sweep_fp64_sod256x64x64_full.md
+KERNEL_TRAFFIC_PER_CELL = {"sweep_xi": 135.2, "sweep_eta": 191.8, "sweep_zeta": 291.4}
+
 
 def load_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
@@ -369,7 +374,9 @@ def run_ours(args):
     alg = KERNEL_BYTES_PER_CELL[top] * cells
     achieved = alg / (top_avg_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": top,
+                "frac": achieved / peaks["hbm_gbs"],
+                "traffic": KERNEL_TRAFFIC_PER_CELL[top] * cells if top in KERNEL_TRAFFIC_PER_CELL else None,
+                "traffic_source": "ncu DRAM bytes per cell of the stage-mode sweep on this workload", "kernel": top,
                 "peak_source": peaks["source"],
                 "alg_bytes_per_launch": alg, "avg_launch_ms": top_avg_ms,
                 "shares": {k: round(v[0] / total_ms, 4) for k, v in sorted(prof.items())}}

@@ -205,6 +205,11 @@ def rhs_ld(P, Q, m, J):
     return out, scale
 
 
+def rk3_ld(P, nsteps, dt, U, Un, Q, m, J):
+    """nsteps SSP-RK3 steps in extended precision (in place, rounded back to FP64)."""
+    lib().orcld_rk3(C.byref(P), C.c_int(nsteps), C.c_double(dt), _p(U), _p(Un), _p(Q), _pp(m), _p(J))
+
+
 def rk3(P, nsteps, dt, U, Un, Q, m, J):
     lib().orc_rk3(C.byref(P), C.c_int(nsteps), C.c_double(dt), _p(U), _p(Un), _p(Q), _pp(m), _p(J))
 

@@ -160,6 +160,29 @@ void orcld_rhs(const f3d_params* P, const double* Q, const double* const m[9], c
 }
 
 // ---- the reference's own precision: Float32 state, Float64 WENO7 alphas -------------
+// nsteps SSP-RK3 steps in long double from FP64 inputs (the yardstick for the rounding of
+// FP64 trajectories); U, Un, Q updated in place (rounded back to FP64).
+void orcld_rk3(const f3d_params* P, int nsteps, double dt, double* U, double* Un, double* Q,
+               const double* const m[9], const double* J) {
+    Grid g(*P);
+    const size_t nc = g.ncell();
+    using L = long double;
+    std::vector<L> Ul(U, U + nc * 5), Unl(Un, Un + nc * 5), Ql(Q, Q + nc * 6), ml[9], Jl(J, J + nc);
+    const L* mp[9];
+    for (int a = 0; a < 9; a++) {
+        ml[a].assign(m[a], m[a] + nc);
+        mp[a] = ml[a].data();
+    }
+    Solver<L, L> s(*P, mp, Jl.data());
+    for (int t = 0; t < nsteps; t++)
+        for (int st = 1; st <= 3; st++) s.rk3_stage(st, L(dt), Ul.data(), Unl.data(), Ql.data());
+    for (size_t i = 0; i < nc * 5; i++) {
+        U[i] = (double)Ul[i];
+        Un[i] = (double)Unl[i];
+    }
+    for (size_t i = 0; i < nc * 6; i++) Q[i] = (double)Ql[i];
+}
+
 void orc32_rhs(const f3d_params* P, const float* Q, const float* const m[9], const float* J, float* dUdt) {
     Solver<float, double> s(*P, m, J);
     s.rhs(Q, dUdt);

@@ -130,10 +130,20 @@ def test_fvm_sod_reference_bcs_steps(gpu_lib):
     try:
         Uo, Uno, Qo = U.copy(), np.zeros_like(U), Q.copy()
         orc.rk3(P, 10, c["dt"], Uo, Uno, Qo, m, J)
+        Ul, Unl, Ql = U.copy(), np.zeros_like(U), Q.copy()
+        orc.rk3_ld(P, 10, c["dt"], Ul, Unl, Ql, m, J)
     finally:
         orc.set_coordinates(None)
-    assert np.isfinite(host(Ud)).all()
-    assert rel_linf(host(Ud)[I], Uo[I], per_var=False) <= 1e-12
+    Ug = host(Ud)
+    assert np.isfinite(Ug).all()
+    # across the shock the FP64 trajectory itself drifts from the extended-precision one;
+    # the GPU must be as close to that as the FP64 oracle is
+    gpu_ld = rel_linf(Ug[I], Ul[I], per_var=False)
+    orc_ld = rel_linf(Uo[I], Ul[I], per_var=False)
+    plain = rel_linf(Ug[I], Uo[I], per_var=False)
+    msg = f"plain {plain:.2e} gpu-vs-ld {gpu_ld:.2e} oracle-vs-ld {orc_ld:.2e}"
+    assert gpu_ld <= max(1e-12, 3.0 * orc_ld), msg
+    assert plain <= max(1e-12, 4.0 * orc_ld), msg
     s.close()
 
 
