@@ -55,9 +55,10 @@ KERNEL_BYTES_PER_CELL = {
 # one RK3 step of the whole RHS: 3 x (U + 9 metrics + J read, U written) + 2 x Un read
 STEP_BYTES_PER_CELL = 3 * 160 + 2 * 40
 
-# DRAM bytes per interior cell of one launch in an RK3 stage, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum) on this workload: the stage-mode table of
-# profiles/k_sweep_fp64_sod256x64x64_full.md
+# DRAM bytes per interior cell of one launch in an RK3 stage on this workload, measured by
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_sweep
+#       python -m flame3d_mhd_gb300.profile --case sod --nx 256 --ny 64 --nz 64 --reps 2 --step
+# (read + write bytes of each sweep divided by the interior cell count)
 KERNEL_TRAFFIC_PER_CELL = {"sweep_xi": 135.2, "sweep_eta": 191.8, "sweep_zeta": 291.4}
 
 
