@@ -357,6 +357,19 @@ def run_ours(args):
              "shares": {k: round(v[0] / tot_m, 4) for k, v in sorted(prof_m.items())},
              "step_hbm_frac": STEP_BYTES_PER_CELL * cells / (ms_mixed / args.steps / 1e3) / 1e9 / load_peaks()["hbm_gbs"]}
     sm.close()
+
+    # the reference's default scheme (run.jl:64-65: finite volume, eigen reconstruction,
+    # HLLC) on the same workload and step count, FP64
+    from flame3d_mhd_gb300.abi import SCHEME_FVM_EIGEN
+    sf = Flame3D(params_copy(P, scheme=SCHEME_FVM_EIGEN))
+    sf.set_metrics(ms, J)
+    sf.set_coordinates(dev(c["x"]), dev(c["y"]), dev(c["z"]))
+    Uf, Unf, Qf = U0.clone(), torch.zeros_like(U0), Q0.clone()
+    ms_fvm, _, _ = timed_steps(sf, Uf, Unf, Qf, args.steps, args.warmup)
+    fvm = {"value": ws * cells * 3 * args.steps / (ms_fvm / 1e3) / 1e6, "unit": UNIT,
+           "ms_per_step": ms_fvm / args.steps, "scheme": "finite volume, Roe-characteristic WENO7/WENO5/minmod "
+           "of U + HLLC (FVM.jl)", "state_finite": bool(sf.check_finite(Uf))}
+    sf.close()
     adjoint = adjoint_cost(args)
 
     # per-kernel device times of single steps (events between launches, outside the timed loop)
@@ -422,6 +435,7 @@ def run_ours(args):
                           "frac": step_gbs / peaks["hbm_gbs"], "alg_bytes_per_cell_step": STEP_BYTES_PER_CELL},
         "mcell_updates_per_s": value / 3,
         "mixed": mixed,
+        "fvm": fvm,
         "adjoint": adjoint,
         "clocks": clocks,
         "state_finite": bool(ok),

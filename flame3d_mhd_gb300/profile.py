@@ -24,7 +24,7 @@ from . import cases
 from .solver import Flame3D
 
 
-def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: int = 0):
+def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: int = 0, scheme: int = 0):
     if case == "sod":
         c = cases.sod(nx, ny, nz, character=character)
     elif case == "tgv_viscous":
@@ -35,10 +35,13 @@ def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: i
         raise ValueError(case)
     P = c["params"]
     P.precision = precision
+    P.scheme = scheme
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     s = Flame3D(P)
     ms, J = s.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
     s.set_metrics(ms, J)
+    xyz = [dev(c[k]) for k in ("x", "y", "z")]
+    s.set_coordinates(*xyz)
     Q = dev(c["Q"])
     U = s.field(5)
     s.prim2c(U, Q)
@@ -54,13 +57,14 @@ def main(argv=None):
     ap.add_argument("--nz", type=int, default=64)
     ap.add_argument("--character", type=int, default=1)
     ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--scheme", type=int, default=0, help="0 FDM, 1 FVM eigen, 2 FVM component-wise")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--step", action="store_true", help="profile_step instead of rhs (per-kernel event times)")
     ap.add_argument("--adjoint", action="store_true", help="RK3 step VJPs on the viscous curvilinear TGV")
     a = ap.parse_args(argv)
     if a.adjoint:
         a.case = "tgv_viscous"
-    s, c, U, Q = setup(a.case, a.nx, a.ny, a.nz, a.character, a.precision)
+    s, c, U, Q = setup(a.case, a.nx, a.ny, a.nz, a.character, a.precision, a.scheme)
     out = s.field(5)
     torch.cuda.synchronize()
     t0 = time.perf_counter()

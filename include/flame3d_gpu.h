@@ -137,7 +137,8 @@ int f3d_set_metrics(f3d_ctx* ctx, const double* const metrics[9], const double* 
  * extrapolates them) for the finite-volume schemes: the unit normal and area of every face
  * (FVM.jl:16-29) are computed once here, in FP64, and kept in the context. Required before
  * any call that needs the metrics when params.scheme is a finite-volume scheme (else
- * F3D_ERR_STATE); a no-op for F3D_SCHEME_FDM. The arrays are read during this call only. */
+ * F3D_ERR_STATE); a no-op for F3D_SCHEME_FDM. The arrays are read only by the work this
+ * call queues on the stream. */
 int f3d_set_coordinates(f3d_ctx* ctx, const double* x, const double* y, const double* z, f3d_stream stream);
 
 /* Compute metrics and J from coordinates x,y,z (Nxt,Nyt,Nzt with ghost coordinates) with
