@@ -23,6 +23,8 @@ SPLIT_SW, SPLIT_LF, SPLIT_VL, SPLIT_AUSM = 0, 1, 2, 3
 SPLIT_NAMES = {"SW": SPLIT_SW, "LF": SPLIT_LF, "VL": SPLIT_VL, "AUSM": SPLIT_AUSM}
 PREC_FP64, PREC_MIXED = 0, 1
 SCHEME_FDM, SCHEME_FVM_EIGEN, SCHEME_FVM_CONS = 0, 1, 2
+FILTER_NONE, FILTER_LINEAR, FILTER_NONLINEAR = 0, 1, 2
+LES_NONE, LES_SMAGORINSKY, LES_WALE = 0, 1, 2
 BC_PERIODIC, BC_DIRICHLET, BC_ZERO_GRADIENT, BC_WALL_ADIABATIC, BC_WALL_ISOTHERMAL = 0, 1, 2, 3, 4
 BC_INFLOW_PROFILE = 5
 
@@ -40,7 +42,9 @@ class F3DParams(C.Structure):
                 ("t_s", C.c_double), ("pr", C.c_double), ("phi1", C.c_double), ("phi2", C.c_double),
                 ("phi3", C.c_double), ("linear_phi", C.c_double), ("clamp_eps", C.c_double),
                 ("split_method", C.c_int32), ("character", C.c_int32), ("viscous", C.c_int32),
-                ("precision", C.c_int32), ("bc", F3DBc * 6), ("scheme", C.c_int32), ("pad2_", C.c_int32)]
+                ("precision", C.c_int32), ("bc", F3DBc * 6), ("scheme", C.c_int32), ("pad2_", C.c_int32),
+                ("lts", C.c_int32), ("filter", C.c_int32), ("filter_interval", C.c_int32), ("les", C.c_int32),
+                ("lts_cfl", C.c_double), ("filter_s0", C.c_double), ("filter_rth", C.c_double)]
 
 
 def params_to_dict(p: F3DParams) -> dict:
@@ -62,6 +66,7 @@ def make_params(nx: int, ny: int, nz: int, **kw) -> F3DParams:
     p.gamma, p.rg, p.cp, p.c_s, p.t_s, p.pr = 1.4, 287.0, 0.0, 1.458e-6, 110.4, 0.72
     p.phi1, p.phi2, p.phi3, p.linear_phi, p.clamp_eps = 0.05, 1.0, 10.0, 1.0, 0.0
     p.split_method, p.character, p.viscous, p.precision = SPLIT_SW, 1, 1, PREC_FP64
+    p.lts_cfl, p.filter_interval, p.filter_rth, p.filter_s0 = 0.5, 100, 1e-5, 1.0  # run.jl:22, 52-54
     fs = dict(kind=BC_DIRICHLET, rho=1.0, u=0.5, v=0.0, w=0.0, p=1.0 / 1.4)
     bcs = [fs, dict(kind=BC_ZERO_GRADIENT), dict(kind=BC_WALL_ADIABATIC), fs,
            dict(kind=BC_PERIODIC), dict(kind=BC_PERIODIC)]
@@ -126,6 +131,8 @@ def load() -> C.CDLL:
         "f3d_rk3_step_vjp": (ip, [vp, C.c_double, vp, vp, vp, vp]),
         "f3d_set_inflow_profile": (ip, [vp, ip, vp, vp]),
         "f3d_set_coordinates": (ip, [vp, vp, vp, vp, vp]),
+        "f3d_filter": (ip, [vp, vp, vp, vp, vp]),
+        "f3d_local_dt": (ip, [vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -142,7 +149,7 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_check_finite", "f3d_debug_sensor", "f3d_debug_split", "f3d_debug_face_flux",
             "f3d_debug_viscous", "f3d_div", "f3d_measure_pipes", "f3d_kernel_count", "f3d_kernel_name",
             "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp", "f3d_set_inflow_profile",
-            "f3d_set_coordinates"]
+            "f3d_set_coordinates", "f3d_filter", "f3d_local_dt"]
 
 
 class F3DError(RuntimeError):

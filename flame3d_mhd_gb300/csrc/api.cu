@@ -43,6 +43,11 @@ int validate_params(const f3d_params& p, std::string& why) {
     if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
     if (p.scheme < F3D_SCHEME_FDM || p.scheme > F3D_SCHEME_FVM_CONS) { why = "unknown scheme"; return F3D_ERR_ARG; }
+    if (p.lts != 0 && p.lts != 1) { why = "lts must be 0 or 1"; return F3D_ERR_ARG; }
+    if (p.lts && !(p.lts_cfl > 0.0)) { why = "lts_cfl must be > 0"; return F3D_ERR_ARG; }
+    if (p.filter < F3D_FILTER_NONE || p.filter > F3D_FILTER_NONLINEAR) { why = "unknown filter"; return F3D_ERR_ARG; }
+    if (p.filter && p.filter_interval < 1) { why = "filter_interval must be >= 1"; return F3D_ERR_ARG; }
+    if (p.les < F3D_LES_NONE || p.les > F3D_LES_WALE) { why = "unknown les model"; return F3D_ERR_ARG; }
     if (p.scheme != F3D_SCHEME_FDM && p.precision != F3D_PREC_FP64) {
         why = "the finite-volume schemes are built for FP64";
         return F3D_ERR_UNSUPPORTED;
@@ -87,6 +92,8 @@ DevParams make_dev_params(const f3d_params& p) {
     for (int m = 0; m < 7; m++) d.lin[m] = up7[m] * p.linear_phi + cd6[m] * (1.0 - p.linear_phi);
     d.split = p.split_method; d.character = p.character; d.viscous = p.viscous;
     d.precision = p.precision;
+    d.lts = p.lts;
+    d.les = p.les;
     d.fixed_branch = fixed_branch_of(p);
     const double th[3] = {p.phi1, p.phi2, p.phi3};
     for (int k = 0; k < 3; k++) {
@@ -148,6 +155,12 @@ struct f3d_ctx {
     double* geo[12] = {};
     double* Ufv = nullptr;
     bool coords_set = false;
+    // local time step (lts) and the shock-capturing filter's sensor; steps done by
+    // f3d_rk3_steps (the filter runs after every filter_interval-th)
+    double* dtl = nullptr;
+    double* sc = nullptr;
+    long long tt = 0;
+    void* extra = nullptr;
     // mixed precision: FP32 copies and FP32 intermediates
     float* Q32 = nullptr;
     MetricPtrs32 m32 = {};
@@ -291,7 +304,7 @@ int run_rhs_fvm(f3d_ctx* ctx, const double* Q, double* acc, const SweepArgs& las
     }
     if (stage)
         F3D_CUDA(ctx, launch_stage_update(P, acc, ctx->J, last.dt, last.U, last.Un, last.stage1_copy, last.combine,
-                                          last.ca, last.cb, st));
+                                          last.ca, last.cb, st, last.dtl));
     return F3D_OK;
 }
 
@@ -342,6 +355,7 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
             a.cb = last.cb;
             a.combine = last.combine;
             a.stage1_copy = last.stage1_copy;
+            a.dtl = last.dtl;
         }
         F3D_CUDA(ctx, launch_sweep(d, a, st));
         mark(ctx, K_SWEEP_X + d, st);
@@ -361,6 +375,10 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
     last.combine = stage != 1;
     last.ca = stage == 2 ? 0.25 : 2.0 / 3.0;  // utils.jl:57-70 via solver.jl:433-435
     last.cb = stage == 2 ? 0.75 : 1.0 / 3.0;
+    if (ctx->params.lts) {  // compute_dt before flowAdvance (solver.jl:419-420), div_LTS after
+        F3D_CUDA(ctx, launch_local_dt(ctx->dp, Q, ctx->m, ctx->J, ctx->params.lts_cfl, ctx->dtl, st));
+        last.dtl = ctx->dtl;
+    }
     int rc = run_rhs(ctx, Q, ctx->acc, last, st, q32_current);
     if (rc) return rc;
     F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 0, st, mixed(ctx) ? ctx->Q32 : nullptr));
@@ -369,8 +387,22 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
 }
 
 // ---- discrete adjoint ------------------------------------------------------------------
+// The explicit filters after every filter_interval-th step (solver.jl:446-470): per
+// direction Un = U, then U = filter(Un) at interior cells. Q is left as it is, as the
+// reference leaves it until the next stage recomputes it.
+int apply_filter(f3d_ctx* ctx, double* U, double* Un, const double* Q, cudaStream_t st) {
+    const f3d_params& p = ctx->params;
+    for (int d = 0; d < 3; d++) {
+        F3D_CUDA(ctx, cudaMemcpyAsync(Un, U, (size_t)ctx->dp.plane * 5 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        F3D_CUDA(ctx, launch_filter_dir(ctx->dp, d, p.filter, p.filter_s0, p.filter_rth, Q, U, Un, ctx->sc, st));
+    }
+    return F3D_OK;
+}
+
 int adjoint_supported(f3d_ctx* ctx) {
     if (mixed(ctx)) return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for the FP64 form");
+    if (ctx->params.lts || ctx->params.filter || ctx->params.les)
+        return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint has no local time stepping, filters or LES");
     if (ctx->params.scheme != F3D_SCHEME_FDM)
         return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for the finite-difference scheme");
     if (ctx->params.character) return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for component-wise reconstruction");
@@ -480,6 +512,8 @@ int f3d_default_params(int nx, int ny, int nz, f3d_params* p) {
     p->clamp_eps = 0.0;
     p->split_method = F3D_SPLIT_SW; p->character = 1; p->viscous = 1;                            // run.jl:61,68,69
     p->precision = F3D_PREC_FP64;
+    p->lts_cfl = 0.5;                                                                           // run.jl:22
+    p->filter_interval = 100; p->filter_rth = 1e-5; p->filter_s0 = 1.0;                          // run.jl:52-54
     // boundary.jl: Dirichlet free stream inlet, zero-gradient outlet, adiabatic no-slip wall,
     // Dirichlet far field, periodic span.
     f3d_bc fs;
@@ -507,6 +541,18 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     ctx->params = *p;
     ctx->dp = make_dev_params(*p);
     if (cudaGetDevice(&ctx->device) != cudaSuccess) { delete ctx; return F3D_ERR_CUDA; }
+    const size_t nplane = (size_t)ctx->dp.plane;
+    if (p->lts || p->filter == F3D_FILTER_NONLINEAR) {  // local dt, filter sensor (zero outside the interior)
+        const size_t eb = nplane * sizeof(double) * 2;
+        if (cudaMalloc(&ctx->extra, eb) != cudaSuccess || cudaMemset(ctx->extra, 0, eb) != cudaSuccess) {
+            if (ctx->extra) cudaFree(ctx->extra);
+            delete ctx;
+            std::fprintf(stderr, "f3d_create: cudaMalloc of the step-component scratch failed\n");
+            return F3D_ERR_CUDA;
+        }
+        ctx->dtl = (double*)ctx->extra;
+        ctx->sc = ctx->dtl + nplane;
+    }
     const size_t nc = (size_t)ctx->dp.plane;
     const size_t nv = (size_t)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -520,6 +566,7 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     }
     cudaError_t e = cudaMalloc(&ctx->slab, total);
     if (e != cudaSuccess) {
+        if (ctx->extra) cudaFree(ctx->extra);
         delete ctx;
         std::fprintf(stderr, "f3d_create: cudaMalloc(%zu) failed: %s\n", total, cudaGetErrorString(e));
         return F3D_ERR_CUDA;
@@ -559,6 +606,7 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     if ((e = cudaMemset(mx ? (void*)ctx->phi32 : (void*)ctx->phi, 0, phi_bytes)) != cudaSuccess ||
         (e = sweep_configure()) != cudaSuccess || (fvm && (e = fvm_configure()) != cudaSuccess)) {
         cudaFree(ctx->slab);
+        if (ctx->extra) cudaFree(ctx->extra);
         delete ctx;
         std::fprintf(stderr, "f3d_create: %s\n", cudaGetErrorString(e));
         return F3D_ERR_CUDA;
@@ -572,6 +620,7 @@ int f3d_destroy(f3d_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
     if (ctx->adj_slab) cudaFree(ctx->adj_slab);
+    if (ctx->extra) cudaFree(ctx->extra);
     cudaError_t e = cudaFree(ctx->slab);
     delete ctx;
     return e == cudaSuccess ? F3D_OK : F3D_ERR_CUDA;
@@ -676,10 +725,17 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
     // fill rewrites it, so the stages inside the step (and the graph) skip the conversion.
     const bool mx = mixed(ctx);
     if (mx && nsteps > 0) F3D_CUDA(ctx, launch_to_f32(Q, ctx->Q32, 6 * ctx->dp.plane, st));
+    const int filt = ctx->params.filter, every = ctx->params.filter_interval;
+    auto after_step = [&]() {  // solver.jl:446-470: filter after every `every`-th step
+        ctx->tt++;
+        return (filt && ctx->tt % every == 0) ? apply_filter(ctx, U, Un, Q, st) : F3D_OK;
+    };
     if (st == nullptr) {  // the legacy stream cannot be captured: plain launches
-        for (int t = 0; t < nsteps; t++)
+        for (int t = 0; t < nsteps; t++) {
             for (int s = 1; s <= 3; s++)
                 if ((rc = run_stage(ctx, s, dt, U, Un, Q, st, mx))) return rc;
+            if ((rc = after_step())) return rc;
+        }
         return F3D_OK;
     }
     const void* key[4] = {U, Un, Q, st};
@@ -703,7 +759,25 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
         for (int n = 0; n < 4; n++) ctx->g_key[n] = key[n];
         ctx->g_dt = dt;
     }
-    for (int t = 0; t < nsteps; t++) F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
+    for (int t = 0; t < nsteps; t++) {
+        F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
+        if ((rc = after_step())) return rc;
+    }
+    return F3D_OK;
+}
+
+int f3d_filter(f3d_ctx* ctx, double* U, double* Un, const double* Q, f3d_stream stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
+    if (!ctx->params.filter) return fail(ctx, F3D_ERR_ARG, "params.filter is F3D_FILTER_NONE");
+    return apply_filter(ctx, U, Un, Q, (cudaStream_t)stream);
+}
+
+int f3d_local_dt(f3d_ctx* ctx, const double* Q, double* dt, f3d_stream stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {Q, dt}))) return rc;
+    F3D_CUDA(ctx, launch_local_dt(ctx->dp, Q, ctx->m, ctx->J,
+                                  ctx->params.lts_cfl > 0.0 ? ctx->params.lts_cfl : 0.5, dt, (cudaStream_t)stream));
     return F3D_OK;
 }
 

@@ -55,6 +55,8 @@ struct DevParams {
     unsigned long long phib[3];
     Cst<double> cd;
     Cst<float> cf;
+    int lts;            // local time stepping: per-cell dt in the stage update
+    int les;            // F3D_LES_* in the viscous fluxes
     BcDev bc[6];
     const double* prof[6];  // F3D_BC_INFLOW_PROFILE states (5 x Ta x Tb), borrowed
 };

@@ -30,6 +30,7 @@ struct SweepArgs {
     double* Un;           // OUT_STAGE stage-start copy
     double* faces;        // OUT_FACES destination (Fx/Fy/Fz shape) or null
     double dt, ca, cb;    // OUT_STAGE: U = ca*(U + dt J acc) + cb*Un when combine
+    const double* dtl;    // OUT_STAGE with local time stepping: per-cell dt replacing dt
     int out_mode;
     int combine;
     int stage1_copy;      // OUT_STAGE of stage 1: Un = U before the update
@@ -75,7 +76,15 @@ cudaError_t launch_face_geometry(const DevParams& P, const double* x, const doub
 cudaError_t launch_fvm_sweep(int dir, bool eigen, const SweepArgs& a, const double* U, const double* const geo[12],
                              cudaStream_t st);
 cudaError_t launch_stage_update(const DevParams& P, const double* acc, const double* J, double dt, double* U,
-                                double* Un, int stage1_copy, int combine, double ca, double cb, cudaStream_t st);
+                                double* Un, int stage1_copy, int combine, double ca, double cb, cudaStream_t st,
+                                const double* dtl = nullptr);
+
+// step components beside the stage (k_step_extras.cu): local time step of every interior
+// cell (utils.jl:73-99) and the explicit filters of U (utils.jl:102-315)
+cudaError_t launch_local_dt(const DevParams& P, const double* Q, const double* const m[9], const double* J,
+                            double lts_cfl, double* dt, cudaStream_t st);
+cudaError_t launch_filter_dir(const DevParams& P, int dir, int mode, double s0, double rth, const double* Q,
+                              double* U, const double* Un, double* sc, cudaStream_t st);
 
 // metric pointer bundles (passed by value to kernels)
 struct MetricPtrs {

@@ -75,7 +75,7 @@ __device__ __forceinline__ void sweep_epilogue(const SweepArgs& a, const R* sF, 
 #pragma unroll
             for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * (double)(acc[c + n * pl] + d[n]);
         } else {  // OUT_STAGE: RK state accumulation in FP64
-            const double Jact = a.J[c] * a.dt;
+            const double Jact = a.J[c] * (a.dtl ? a.dtl[c] : a.dt);  // div_LTS: per-cell dt
 #pragma unroll
             for (int n = 0; n < 5; n++) {
                 const double u = a.U[c + n * pl];

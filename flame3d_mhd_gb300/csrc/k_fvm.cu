@@ -427,13 +427,14 @@ cudaError_t launch_fvm_sweep(int dir, bool eigen, const SweepArgs& a, const doub
 // ------------------------------------------------------------------------------------
 // RK update from the accumulated RHS (div.jl:1-50 fused with linComb, utils.jl:57-70)
 __global__ void k_stage_update(const DevParams P, const double* __restrict__ acc, const double* __restrict__ J,
-                               double dt, double* U, double* Un, int stage1_copy, int combine, double ca, double cb) {
+                               double dt, double* U, double* Un, int stage1_copy, int combine, double ca, double cb,
+                               const double* __restrict__ dtl) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = (long long)P.nx * P.ny * P.nz;
     if (t >= n) return;
     const int i = (int)(t % P.nx), j = (int)((t / P.nx) % P.ny), k = (int)(t / ((long long)P.nx * P.ny));
     const long long c = lin3(P, i + NG, j + NG, k + NG), pl = P.plane;
-    const double Jact = J[c] * dt;
+    const double Jact = J[c] * (dtl ? dtl[c] : dt);
 #pragma unroll
     for (int v = 0; v < 5; v++) {
         const double u = U[c + v * pl];
@@ -445,9 +446,10 @@ __global__ void k_stage_update(const DevParams P, const double* __restrict__ acc
 }
 
 cudaError_t launch_stage_update(const DevParams& P, const double* acc, const double* J, double dt, double* U,
-                                double* Un, int stage1_copy, int combine, double ca, double cb, cudaStream_t st) {
+                                double* Un, int stage1_copy, int combine, double ca, double cb, cudaStream_t st,
+                                const double* dtl) {
     const long long n = (long long)P.nx * P.ny * P.nz;
-    k_stage_update<<<cdiv(n, 256), 256, 0, st>>>(P, acc, J, dt, U, Un, stage1_copy, combine, ca, cb);
+    k_stage_update<<<cdiv(n, 256), 256, 0, st>>>(P, acc, J, dt, U, Un, stage1_copy, combine, ca, cb, dtl);
     return cudaGetLastError();
 }
 

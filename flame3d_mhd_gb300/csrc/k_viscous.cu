@@ -28,8 +28,8 @@ __global__ void __launch_bounds__(128) k_viscous(const DevParams P, const R* __r
     const R zx = m6[c], zy = m7[c], zz = m8[c];
     const R Jac = J[c];
     const R T = Q[c + 5 * pl];
-    const R mu = K.c_s * T * sqrt(T) / (T + K.t_s);
-    const R lam = mu * K.cp_pr;
+    R mu = K.c_s * T * sqrt(T) / (T + K.t_s);
+    R lam = mu * K.cp_pr;
     const R c1 = R(1) / R(12), c2 = R(-2) / R(3), c23 = R(2) / R(3);
     auto d4 = [&](int n, long long s) {
         const R* f = Q + n * pl + c;
@@ -53,6 +53,42 @@ __global__ void __launch_bounds__(128) k_viscous(const DevParams P, const R* __r
     const R dTdy = (Txi * xy + Tet * ey + Tze * zy) * Jac;
     const R dTdz = (Txi * xz + Tet * ez + Tze * zz) * Jac;
     const R dv = dudx + dvdy + dwdz;
+    if (P.les) {  // viscous.jl:66-106: eddy viscosity and conductivity, Pr_t = 0.9
+        const R rho = Q[c];
+        const R s12 = R(0.5) * (dudy + dvdx), s13 = R(0.5) * (dudz + dwdx), s23 = R(0.5) * (dvdz + dwdy);
+        const R sii = dudx * dudx + dvdy * dvdy + dwdz * dwdz;
+        const R sij = s12 * s12 + s13 * s13 + s23 * s23;
+        const R inv_d = R(1) / cbrt(Jac);  // 1 / Delta with Delta = J^(1/3) (cell size, J^-1 = volume)
+        R mut;
+        if (P.les == F3D_LES_SMAGORINSKY) {
+            const R Smag = sqrt(R(2) * (sii + R(2) * sij));  // sqrt(2) |S_ij|
+            const R cd = R(0.1) * inv_d;
+            mut = rho * cd * cd * Smag;
+        } else {  // WALE
+            const R S = sqrt(sii + R(2) * sij);
+            R d11 = dudx * dudx + dudy * dvdx + dudz * dwdx;
+            R d22 = dvdx * dudy + dvdy * dvdy + dvdz * dwdy;
+            R d33 = dwdx * dudz + dwdy * dvdz + dwdz * dwdz;
+            const R tr = R(1) / R(3) * (d11 + d22 + d33);
+            d11 -= tr;
+            d22 -= tr;
+            d33 -= tr;
+            const R d12 = R(0.5) * (dudx * dvdx + dvdx * dvdy + dwdx * dvdz + dudy * dudx + dvdy * dudy + dwdy * dudz);
+            const R d13 = R(0.5) * (dudx * dwdx + dvdx * dwdy + dwdx * dwdz + dudz * dudx + dvdz * dudy + dwdz * dudz);
+            const R d23 = R(0.5) * (dudy * dwdx + dvdy * dwdy + dwdy * dwdz + dudz * dvdx + dvdz * dvdy + dwdz * dvdz);
+            const R Sd = sqrt(d11 * d11 + d22 * d22 + d33 * d33 + R(2) * (d12 * d12 + d13 * d13 + d23 * d23));
+            const R S2 = S * S;
+            const R D = Sd * Sd * Sd / (S2 * S2 * S + Sd * Sd * sqrt(Sd));
+            const R cd = R(0.325) * inv_d;
+            mut = rho * cd * cd * D;
+        }
+        // min(mu_t, 2 mu) returning NaN when either is NaN, as Julia's min does (D = 0/0 where
+        // the velocity gradient vanishes)
+        const R lim = R(2) * mu;
+        mut = (mut != mut) ? mut : (lim < mut ? lim : mut);
+        mu += mut;
+        lam += K.cp * mut / R(0.9);
+    }
     const R t11 = mu * (R(2) * dudx - c23 * dv);
     const R t12 = mu * (dudy + dvdx);
     const R t13 = mu * (dudz + dwdx);

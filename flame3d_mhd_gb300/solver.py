@@ -118,6 +118,18 @@ class Flame3D:
         self._check(self.lib.f3d_set_metrics(self._h, arr, self._ptr(J, 1), self._stream()))
         self.metrics, self.J = list(metrics), J  # keep the borrowed arrays alive
 
+    def filter(self, U: torch.Tensor, Un: torch.Tensor, Q: torch.Tensor):
+        """One pass of the explicit filter of params.filter (linearFilter_x/y/z, or pre_x/y/z
+        and filter_x/y/z) over U; Un receives the per-direction copies (solver.jl:446-470)."""
+        self._check(self.lib.f3d_filter(self._h, self._ptr(U, 5), self._ptr(Un, 5), self._ptr(Q, 6), self._stream()))
+
+    def compute_dt(self, Q: torch.Tensor, dt: torch.Tensor | None = None) -> torch.Tensor:
+        """Local time step of every interior cell (utils.jl:73-99)."""
+        if dt is None:
+            dt = self.field(1)
+        self._check(self.lib.f3d_local_dt(self._h, self._ptr(Q, 6), self._ptr(dt, 1), self._stream()))
+        return dt
+
     def set_coordinates(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor):
         """Ghost-filled cell-centre coordinates for the finite-volume schemes: face normals
         and areas (FVM.jl:16-29) are computed from them once (a no-op for the FDM scheme)."""

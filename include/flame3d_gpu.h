@@ -61,6 +61,17 @@ extern "C" {
 #define F3D_PREC_MIXED 1 /* FP32 split/reconstruction/weights/viscous; FP64 state, EOS,
                             metrics/J, RK accumulation and reductions                   */
 
+/* explicit filters of U (utils.jl:102-315) */
+#define F3D_FILTER_NONE 0
+#define F3D_FILTER_LINEAR 1     /* 8th-order linear filter, linearFilter_x/y/z              */
+#define F3D_FILTER_NONLINEAR 2  /* shock-capturing filter: pressure sensor pre_x/y/z, then
+                                   the 4-point dissipative filter filter_x/y/z               */
+
+/* sub-grid models (viscous.jl:66-106) */
+#define F3D_LES_NONE 0
+#define F3D_LES_SMAGORINSKY 1   /* C_s = 0.1, Pr_t = 0.9                                     */
+#define F3D_LES_WALE 2          /* C_w = 0.325, Pr_t = 0.9                                   */
+
 /* ghost-cell rules, one per face (x-, x+, y-, y+, z-, z+). Faces are filled in the
  * order x, y, z over the full transverse extent including ghosts, which is the
  * order of fill_x, fill_y, fill_z in boundary.jl:151-156. */
@@ -100,6 +111,17 @@ typedef struct f3d_params {
     f3d_bc bc[6];           /* x-, x+, y-, y+, z-, z+                                    */
     int32_t scheme;         /* F3D_SCHEME_*; the finite-volume schemes are FP64 only       */
     int32_t pad2_;
+    /* step components beside the RK stage (run.jl:3-5, 21-22, 49-54; off by default)      */
+    int32_t lts;            /* 1: local time stepping: each stage advances every cell by its
+                               own dt = lts_cfl min_d(V/S_d/(u_d+c)) (utils.jl:73-99,
+                               div.jl:52-101); the dt argument of the stage entries is unused */
+    int32_t filter;         /* F3D_FILTER_*: applied to U after every filter_interval-th step
+                               of f3d_rk3_steps (solver.jl:446-470), or by f3d_filter          */
+    int32_t filter_interval;
+    int32_t les;            /* F3D_LES_*: eddy viscosity in the viscous fluxes (viscous.jl:66-106) */
+    double lts_cfl;         /* run.jl:22                                                   */
+    double filter_s0;       /* filter strength, run.jl:54                                  */
+    double filter_rth;      /* shock-capturing filter threshold, run.jl:53                 */
 } f3d_params;
 
 typedef struct f3d_ctx f3d_ctx;
@@ -213,6 +235,16 @@ int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream);
  * CuArrays (solver.jl:293-337). */
 int f3d_rhs_noalloc(const f3d_params* p, const double* const metrics[9], const double* jac,
                     const double* Q, double* dUdt, f3d_stream stream);
+
+/* One pass of the explicit filter of params.filter over U (interior cells), the three
+ * directions in turn, each from a copy Un of U made just before it (solver.jl:447-470);
+ * Q supplies the shock-capturing filter's pressure sensor and is not updated (as in the
+ * reference). f3d_rk3_steps applies it by itself after every filter_interval-th step. */
+int f3d_filter(f3d_ctx* ctx, double* U, double* Un, const double* Q, f3d_stream stream);
+
+/* Local time step of every interior cell (compute_dt, utils.jl:73-99) into dt (U-cell
+ * layout, ghosts untouched), with params.lts_cfl (0.5 when unset). */
+int f3d_local_dt(f3d_ctx* ctx, const double* Q, double* dt, f3d_stream stream);
 
 /* Borrow the state of an F3D_BC_INFLOW_PROFILE face (0..5 = x-, x+, y-, y+, z-, z+): a
  * device array of 5 x Ta x Tb doubles, variable-major (rho, u, v, w, p), each plane indexed

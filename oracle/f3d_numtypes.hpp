@@ -32,6 +32,10 @@ struct Dual {
     friend bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
     friend bool operator==(const Dual& a, const Dual& b) { return a.v == b.v; }
     friend Dual abs(const Dual& a) { return a.v >= 0.0 ? a : -a; }
+    friend Dual cbrt(const Dual& a) {
+        const double r = std::cbrt(a.v);
+        return Dual(r, a.d / (3.0 * r * r));
+    }
     friend Dual sqrt(const Dual& a) {
         double s = std::sqrt(a.v);
         return Dual(s, a.d / (2.0 * s));
@@ -71,6 +75,7 @@ struct Counted {
     friend bool operator==(const Counted& a, const Counted& b) { return a.v == b.v; }
     friend Counted abs(const Counted& a) { tick(OPC_CMP); return Counted(std::fabs(a.v)); }
     friend Counted sqrt(const Counted& a) { tick(OPC_SQRT); return Counted(std::sqrt(a.v)); }
+    friend Counted cbrt(const Counted& a) { tick(OPC_SQRT); return Counted(std::cbrt(a.v)); }
 };
 
 }  // namespace f3do

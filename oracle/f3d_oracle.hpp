@@ -31,6 +31,7 @@ namespace f3do {
 
 using std::abs;
 using std::sqrt;
+using std::cbrt;
 
 // NaN-propagating max/min like Julia's max/min on floats.
 template <class T> inline T jmax(const T& a, const T& b) {
@@ -693,6 +694,37 @@ void viscous(const f3d_params& P, const R* Qp, const R* const m[9], const R* Jp,
                 R dTdy = (Txi * xy + Teta * ey + Tze * zy) * Jac;
                 R dTdz = (Txi * xz + Teta * ez + Tze * zz) * Jac;
                 R dv = dudx + dvdy + dwdz;
+                if (P.les) {  // viscous.jl:66-106, Pr_t = 0.9
+                    const R rho = Q(i, j, k, 1);
+                    const R s12 = R(0.5) * (dudy + dvdx), s13 = R(0.5) * (dudz + dwdx), s23 = R(0.5) * (dvdz + dwdy);
+                    const R sii = dudx * dudx + dvdy * dvdy + dwdz * dwdz;
+                    const R sij = s12 * s12 + s13 * s13 + s23 * s23;
+                    const R J13 = cbrt(Jac);  // Jac^(1/3)
+                    R mut;
+                    if (P.les == F3D_LES_SMAGORINSKY) {  // viscous.jl:66-78
+                        const R Smag = sqrt(R(2) * (sii + R(2) * sij));
+                        const R cd = R(0.1) / J13;
+                        mut = jmin(rho * cd * cd * Smag, R(2) * mu);
+                    } else {  // WALE, viscous.jl:79-101
+                        const R S = sqrt(sii + R(2) * sij);
+                        R d11 = dudx * dudx + dudy * dvdx + dudz * dwdx;
+                        R d22 = dvdx * dudy + dvdy * dvdy + dvdz * dwdy;
+                        R d33 = dwdx * dudz + dwdy * dvdz + dwdz * dwdz;
+                        const R tr = R(1) / R(3) * (d11 + d22 + d33);
+                        d11 = d11 - tr;
+                        d22 = d22 - tr;
+                        d33 = d33 - tr;
+                        const R d12 = R(0.5) * (dudx * dvdx + dvdx * dvdy + dwdx * dvdz + dudy * dudx + dvdy * dudy + dwdy * dudz);
+                        const R d13 = R(0.5) * (dudx * dwdx + dvdx * dwdy + dwdx * dwdz + dudz * dudx + dvdz * dudy + dwdz * dudz);
+                        const R d23 = R(0.5) * (dudy * dwdx + dvdy * dwdy + dwdy * dwdz + dudz * dvdx + dvdz * dvdy + dwdz * dvdz);
+                        const R Sd = sqrt(d11 * d11 + d22 * d22 + d33 * d33 + R(2) * (d12 * d12 + d13 * d13 + d23 * d23));
+                        const R D = Sd * Sd * Sd / (S * S * S * S * S + Sd * Sd * sqrt(Sd));  // Sd^3/(S^5 + Sd^2.5)
+                        const R cd = R(0.325) / J13;
+                        mut = jmin(rho * cd * cd * D, R(2) * mu);
+                    }
+                    mu = mu + mut;
+                    lam = lam + C.cp * mut / R(0.9);
+                }
                 R t11 = mu * (R(2) * dudx - c23 * dv);
                 R t12 = mu * (dudy + dvdx);
                 R t13 = mu * (dudz + dwdx);
@@ -724,7 +756,7 @@ void viscous(const f3d_params& P, const R* Qp, const R* const m[9], const R* Jp,
 // (the right-hand side itself, the same two-term structure without dt).
 template <class R>
 void divergence(const f3d_params& P, const R* Fxp, const R* Fyp, const R* Fzp, const R* Fvxp,
-                const R* Fvyp, const R* Fvzp, const R* Jp, R dt, R* U_inout, R* dUdt) {
+                const R* Fvyp, const R* Fvzp, const R* Jp, R dt, R* U_inout, R* dUdt, const R* dtl = nullptr) {
     Grid g(P);
     const long NG = g.ng;
     const long Nx = g.nx, Ny = g.ny, Nz = g.nz;
@@ -740,7 +772,9 @@ void divergence(const f3d_params& P, const R* Fxp, const R* Fyp, const R* Fzp, c
         for (long j = 1; j <= Ny; j++)
             for (long i = 1; i <= Nx; i++) {
                 const R Jc = Jv(i + NG, j + NG, k + NG);
-                const R Jact = U_inout ? Jc * dt : Jc;
+                // div_LTS (div.jl:52-101) with a per-cell dt
+                const R dtc = dtl ? dtl[(i + NG - 1) + g.nxt * ((j + NG - 1) + g.nyt * (k + NG - 1))] : dt;
+                const R Jact = U_inout ? Jc * dtc : Jc;
                 R dv[5] = {R(0), R(0), R(0), R(0), R(0)};
                 if (visc) {
                     for (int n = 1; n <= 4; n++) {
@@ -775,6 +809,72 @@ template <class R> void metric_norm(size_t nc, const R* a, const R* b, const R* 
     for (long i = 0; i < (long)nc; i++) s[i] = sqrt(a[i] * a[i] + b[i] * b[i] + c[i] * c[i]);
 }
 
+// utils.jl:73-99 compute_dt: interior cells, LTS_CFL * min(V/S1/(u+c), V/S2/(v+c), V/S3/(w+c)).
+template <class R>
+void compute_dt(const f3d_params& P, const R* Qp, const R* Jp, const R* S1, const R* S2, const R* S3, R* dtp) {
+    Grid g(P);
+    Consts<R> C(P);
+    V4<const R> Q{Qp, g.nxt, g.nyt, g.nzt};
+    const R cfl = R(P.lts_cfl);
+#pragma omp parallel for schedule(static)
+    for (long k = g.ng + 1; k <= g.nz + g.ng; k++)
+        for (long j = g.ng + 1; j <= g.ny + g.ng; j++)
+            for (long i = g.ng + 1; i <= g.nx + g.ng; i++) {
+                const size_t c = Q.lin(i, j, k);
+                const R u = Q(i, j, k, 2), v = Q(i, j, k, 3), w = Q(i, j, k, 4), T = Q(i, j, k, 6);
+                const R V = R(1) / Jp[c];
+                const R cs = sqrt(C.gamma * C.rg * T);
+                const R dtx = V / S1[c] / (u + cs), dty = V / S2[c] / (v + cs), dtz = V / S3[c] / (w + cs);
+                dtp[c] = jmin(jmin(dtx, dty), dtz) * cfl;
+            }
+}
+
+// The explicit filters of one direction d over interior cells (utils.jl:102-315): the
+// shock-capturing pair pre_x/filter_x (nonlinear) or linearFilter_x, from Un into U.
+template <class R>
+void filter_dir(const f3d_params& P, int d, const R* Qp, R* Up, const R* Unp, R* scp) {
+    Grid g(P);
+    const long NG = g.ng, st = g.stride(d);
+    const size_t nc = g.ncell();
+    const R s0 = R(P.filter_s0), rth = R(P.filter_rth);
+    auto interior = [&](auto&& fn) {
+#pragma omp parallel for schedule(static)
+        for (long k = NG + 1; k <= g.nz + NG; k++)
+            for (long j = NG + 1; j <= g.ny + NG; j++)
+                for (long i = NG + 1; i <= g.nx + NG; i++) fn((size_t)((i - 1) + g.nxt * ((j - 1) + g.nyt * (k - 1))));
+    };
+    if (P.filter == F3D_FILTER_NONLINEAR) {
+        interior([&](size_t c) {  // pre_x, utils.jl:102-123
+            const R* p = Qp + 4 * nc + c;
+            const R p1 = p[-2 * st], p2 = p[-st], p3 = p[0], p4 = p[st], p5 = p[2 * st];
+            const R d0 = R(0.25) * (-p4 + R(2) * p3 - p2);
+            const R d1 = R(0.25) * (-p5 + R(2) * p4 - p3);
+            const R d2 = R(0.25) * (-p3 + R(2) * p2 - p1);
+            const R ri = R(0.5) * ((d0 - d1) * (d0 - d1) + (d0 - d2) * (d0 - d2)) / (p3 * p3) + R(1e-16);
+            scp[c] = R(0.5) * (R(1) - rth / ri + abs(R(1) - rth / ri));
+        });
+        interior([&](size_t c) {  // filter_x, utils.jl:171-193
+            const R c1 = R(-0.210383), c2 = R(0.039617);
+            const R sc1 = R(0.5) * (scp[c] + scp[c + st]), sc2 = R(0.5) * (scp[c] + scp[c - st]);
+            for (int n = 0; n < 5; n++) {
+                const R* f = Unp + n * nc + c;
+                Up[n * nc + c] = f[0] - s0 * (sc1 * (c1 * (f[st] - f[0]) + c2 * (f[2 * st] - f[-st])) -
+                                              sc2 * (c1 * (f[0] - f[-st]) + c2 * (f[st] - f[-2 * st])));
+            }
+        });
+    } else {
+        interior([&](size_t c) {  // linearFilter_x, utils.jl:243-266
+            const R d0 = R(0.243527493120), d1 = R(-0.204788880640), d2 = R(0.120007591680),
+                    d3 = R(-0.045211119360), d4 = R(0.008228661760);
+            for (int n = 0; n < 5; n++) {
+                const R* f = Unp + n * nc + c;
+                Up[n * nc + c] = f[0] - s0 * (d0 * f[0] + d1 * (f[-st] + f[st]) + d2 * (f[-2 * st] + f[2 * st]) +
+                                              d3 * (f[-3 * st] + f[3 * st]) + d4 * (f[-4 * st] + f[4 * st]));
+            }
+        });
+    }
+}
+
 }  // namespace f3do
 #include "f3d_oracle_fvm.hpp"
 namespace f3do {
@@ -789,7 +889,8 @@ template <class R, class W> struct Solver {
     const R* m[9];
     const R* J;
     const R *xs = nullptr, *ys = nullptr, *zs = nullptr;
-    std::vector<R> S[3], phi, Fp, Fm, F[3], Fv[3], Uq, xyz[3];
+    std::vector<R> S[3], phi, Fp, Fm, F[3], Fv[3], Uq, xyz[3], dtl, sc;
+    long tt = 0;  // steps done (the filter runs after every filter_interval-th)
     std::vector<int8_t> branch[3];
     bool record_branch = false;
 
@@ -854,14 +955,36 @@ template <class R, class W> struct Solver {
     void rk3_stage(int stage, R dt, R* U, R* Un, R* Q) {
         const size_t n5 = g.ncell() * 5;
         if (stage == 1) std::memcpy(Un, U, n5 * sizeof(R));
+        if (P.lts) {  // solver.jl:419-420: compute_dt before flowAdvance
+            dtl.assign(g.ncell(), R(0));
+            compute_dt<R>(P, Q, J, S[0].data(), S[1].data(), S[2].data(), dtl.data());
+        }
         fluxes(Q, U);
         const bool v = P.viscous != 0;
         divergence<R>(P, F[0].data(), F[1].data(), F[2].data(), v ? Fv[0].data() : nullptr,
-                      v ? Fv[1].data() : nullptr, v ? Fv[2].data() : nullptr, J, dt, U, nullptr);
+                      v ? Fv[1].data() : nullptr, v ? Fv[2].data() : nullptr, J, dt, U, nullptr,
+                      P.lts ? dtl.data() : nullptr);
         if (stage == 2) lincomb<R>(P, U, Un, R(0.25), R(0.75));
         if (stage == 3) lincomb<R>(P, U, Un, R(2) / R(3), R(1) / R(3));
         c2prim<R>(P, U, Q);
         fill_ghosts<R>(P, Q, U);
+    }
+
+    // solver.jl:446-470 after a step: the filter every filter_interval steps, each
+    // direction from a copy Un of U (Q unchanged).
+    void after_step(R* U, R* Un, const R* Q) {
+        tt++;
+        if (!P.filter || tt % P.filter_interval != 0) return;
+        if (sc.empty()) sc.assign(g.ncell(), R(0));
+        for (int d = 0; d < 3; d++) {
+            std::memcpy(Un, U, g.ncell() * 5 * sizeof(R));
+            filter_dir<R>(P, d, Q, U, Un, sc.data());
+        }
+    }
+
+    void rk3_step(R dt, R* U, R* Un, R* Q) {
+        for (int st = 1; st <= 3; st++) rk3_stage(st, dt, U, Un, Q);
+        after_step(U, Un, Q);
     }
 };
 

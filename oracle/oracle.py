@@ -205,6 +205,18 @@ def rhs_ld(P, Q, m, J):
     return out, scale
 
 
+def local_dt(P, Q, m, J):
+    """compute_dt (utils.jl:73-99) at interior cells (ghost cells 0)."""
+    dt = zeros(P)
+    lib().orc_local_dt(C.byref(P), _p(Q), _pp(m), _p(J), _p(dt))
+    return dt
+
+
+def filter_pass(P, U, Un, Q):
+    """One pass of params.filter over U in place (three directions, Un the per-direction copy)."""
+    lib().orc_filter(C.byref(P), _p(U), _p(Un), _p(Q))
+
+
 def rk3_ld(P, nsteps, dt, U, Un, Q, m, J):
     """nsteps SSP-RK3 steps in extended precision (in place, rounded back to FP64)."""
     lib().orcld_rk3(C.byref(P), C.c_int(nsteps), C.c_double(dt), _p(U), _p(Un), _p(Q), _pp(m), _p(J))

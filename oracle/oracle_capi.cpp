@@ -21,6 +21,20 @@ int orc_set_threads(int n) {
     return omp_get_max_threads();
 }
 
+// compute_dt (utils.jl:73-99) into dt at interior cells; one filter pass (3 directions).
+void orc_local_dt(const f3d_params* P, const double* Q, const double* const m[9], const double* J, double* dt) {
+    Solver<double, double> s(*P, m, J);
+    compute_dt<double>(*P, Q, J, s.S[0].data(), s.S[1].data(), s.S[2].data(), dt);
+}
+void orc_filter(const f3d_params* P, double* U, double* Un, const double* Q) {
+    Grid g(*P);
+    std::vector<double> sc(g.ncell(), 0.0);
+    for (int d = 0; d < 3; d++) {
+        std::memcpy(Un, U, g.ncell() * 5 * sizeof(double));
+        filter_dir<double>(*P, d, Q, U, Un, sc.data());
+    }
+}
+
 // Register (or clear, with nullptrs) the cell-centre coordinates the finite-volume schemes
 // take their face geometry from.
 void orc_set_coordinates(const double* x, const double* y, const double* z) {
@@ -95,7 +109,7 @@ void orc_rk3(const f3d_params* P, int nsteps, double dt, double* U, double* Un, 
              const double* const m[9], const double* J) {
     Solver<double, double> s(*P, m, J);
     for (int t = 0; t < nsteps; t++)
-        for (int st = 1; st <= 3; st++) s.rk3_stage(st, dt, U, Un, Q);
+        s.rk3_step(dt, U, Un, Q);
 }
 
 // Persistent workspace for timing: create once, step many times (allocation is set-up
@@ -106,7 +120,7 @@ void* orc_solver_create(const f3d_params* P, const double* const m[9], const dou
 void orc_solver_rk3(void* h, int nsteps, double dt, double* U, double* Un, double* Q) {
     auto* s = static_cast<Solver<double, double>*>(h);
     for (int t = 0; t < nsteps; t++)
-        for (int st = 1; st <= 3; st++) s->rk3_stage(st, dt, U, Un, Q);
+        s->rk3_step(dt, U, Un, Q);
 }
 void orc_solver_destroy(void* h) { delete static_cast<Solver<double, double>*>(h); }
 
@@ -175,7 +189,7 @@ void orcld_rk3(const f3d_params* P, int nsteps, double dt, double* U, double* Un
     }
     Solver<L, L> s(*P, mp, Jl.data());
     for (int t = 0; t < nsteps; t++)
-        for (int st = 1; st <= 3; st++) s.rk3_stage(st, L(dt), Ul.data(), Unl.data(), Ql.data());
+        s.rk3_step(L(dt), Ul.data(), Unl.data(), Ql.data());
     for (size_t i = 0; i < nc * 5; i++) {
         U[i] = (double)Ul[i];
         Un[i] = (double)Unl[i];
@@ -191,7 +205,7 @@ void orc32_rk3(const f3d_params* P, int nsteps, float dt, float* U, float* Un, f
                const float* J) {
     Solver<float, double> s(*P, m, J);
     for (int t = 0; t < nsteps; t++)
-        for (int st = 1; st <= 3; st++) s.rk3_stage(st, dt, U, Un, Q);
+        s.rk3_step(dt, U, Un, Q);
 }
 void orc32_c2prim(const f3d_params* P, const float* U, float* Q) { c2prim<float>(*P, U, Q); }
 void orc32_fill_ghosts(const f3d_params* P, float* Q, float* U) { fill_ghosts<float>(*P, Q, U); }
