@@ -34,7 +34,7 @@ int validate_params(const f3d_params& p, std::string& why) {
         why = "grid too large for the launch shape"; return F3D_ERR_ARG;
     }
     const long long cells = (long long)(p.nx + 8) * (p.ny + 8) * (p.nz + 8);
-    if (cells > (1LL << 34)) { why = "grid too large"; return F3D_ERR_ARG; }
+    if (cells >= (1LL << 31)) { why = "grid too large (cell indices are 31-bit)"; return F3D_ERR_ARG; }
     if (!(p.gamma > 1.0) || !(p.rg > 0.0) || !(p.pr > 0.0) || !(p.c_s >= 0.0) || !(p.t_s >= 0.0)) {
         why = "gas constants out of range"; return F3D_ERR_ARG;
     }
@@ -79,6 +79,9 @@ DevParams make_dev_params(const f3d_params& p) {
     d.nx = p.nx; d.ny = p.ny; d.nz = p.nz;
     d.nxt = p.nx + 2 * NG; d.nyt = p.ny + 2 * NG; d.nzt = p.nz + 2 * NG;
     d.plane = (long long)d.nxt * d.nyt * d.nzt;
+    d.dnxt = make_fastdiv((unsigned)d.nxt); d.dnyt = make_fastdiv((unsigned)d.nyt);
+    d.dnx = make_fastdiv((unsigned)p.nx); d.dny = make_fastdiv((unsigned)p.ny);
+    d.dvxt = make_fastdiv((unsigned)(d.nxt - 4)); d.dvyt = make_fastdiv((unsigned)(d.nyt - 4));
     d.gamma = p.gamma; d.rg = p.rg;
     d.cp = p.cp != 0.0 ? p.cp : p.rg * p.gamma / (p.gamma - 1.0);
     d.c_s = p.c_s; d.t_s = p.t_s; d.pr = p.pr;
@@ -764,6 +767,12 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
         if ((rc = after_step())) return rc;
     }
     return F3D_OK;
+}
+
+int f3d_debug_round_f32(const double* in, float* out, long long n, f3d_stream stream) {
+    if (!in || !out || n < 0) return F3D_ERR_ARG;
+    if (((uintptr_t)in & 15u) || ((uintptr_t)out & 7u)) return F3D_ERR_ALIGN;
+    return launch_to_f32(in, out, n, (cudaStream_t)stream) == cudaSuccess ? F3D_OK : F3D_ERR_CUDA;
 }
 
 int f3d_filter(f3d_ctx* ctx, double* U, double* Un, const double* Q, f3d_stream stream) {

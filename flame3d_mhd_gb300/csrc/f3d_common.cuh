@@ -35,6 +35,28 @@ template <class R> struct Cst {
 };
 
 // Runtime constants of one context, passed to every kernel by value.
+// Exact quotient of n < 2^32 by a divisor d > 1 fixed for the grid: q = mulhi64(M, n) with
+// M = ceil(2^64 / d) (Lemire, Kaser and Kurz, "Faster remainder by direct computation",
+// 2019). Cell indices are decomposed this way instead of with 64-bit / and %, which
+// compile to long emulated sequences.
+struct FastDiv {
+    unsigned long long M;
+    unsigned d;
+};
+inline FastDiv make_fastdiv(unsigned d) { return FastDiv{d > 1 ? ~0ull / d + 1ull : 0ull, d}; }
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv& f) {
+    return f.d > 1 ? (unsigned)__umul64hi(f.M, (unsigned long long)n) : n;
+}
+// t = a + na (b + nb c) -> (a, b, c) with na = fa.d, nb = fb.d
+__device__ __forceinline__ void split3(long long t, const FastDiv& fa, const FastDiv& fb, int& a, int& b, int& c) {
+    const unsigned tu = (unsigned)t;
+    const unsigned q = fdiv(tu, fa);
+    a = (int)(tu - q * fa.d);
+    const unsigned q2 = fdiv(q, fb);
+    b = (int)(q - q2 * fb.d);
+    c = (int)q2;
+}
+
 struct DevParams {
     int nx, ny, nz;     // interior
     int nxt, nyt, nzt;  // with ghosts
@@ -55,6 +77,9 @@ struct DevParams {
     unsigned long long phib[3];
     Cst<double> cd;
     Cst<float> cf;
+    FastDiv dnxt, dnyt;  // full-grid extents: cell index -> (i, j, k)
+    FastDiv dnx, dny;    // interior extents
+    FastDiv dvxt, dvyt;  // the viscous box (Nt - 4 per direction)
     int lts;            // local time stepping: per-cell dt in the stage update
     int les;            // F3D_LES_* in the viscous fluxes
     BcDev bc[6];
@@ -90,12 +115,52 @@ __device__ __forceinline__ void c2prim_cell(const DevParams& P, const double U[5
 }
 
 // The same recovery for the mixed-precision form: still FP64 (the pressure/temperature
-// recovery from total energy stays FP64), with T = p (1/rho)(1/Rg) instead of a second
-// division. FP64 divisions are ~10 FMA issue slots on GB300.
+// recovery from total energy stays FP64), with 1/rho by recip_nr and T = p (1/rho)(1/Rg)
+// instead of divisions: FP64 divisions are ~10 FMA issue slots on GB300.
+// ---- conversions and a reciprocal for the mixed form, off the FP64 pipe -----------------
+// On this GPU the double <-> float conversion instructions issue on the FP64 pipe, which
+// the mixed form needs for its FP64 state arithmetic. These work on the IEEE 754 binary64 /
+// binary32 bit layouts with integer operations in the binary32 normal range and use the
+// conversion instruction elsewhere (zeros, subnormal results, overflow, infinities, NaN).
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int hi = (unsigned int)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7ffu);  // biased binary64 exponent
+    if (e < 897 || e > 1150) return __double2float_rn(x);  // outside binary32 exponents 1..254
+    const unsigned int m23 = (unsigned int)((b >> 29) & 0x7fffffull);
+    const unsigned int rest = (unsigned int)(b & 0x1fffffffull);  // the 29 dropped bits
+    unsigned int f = (hi & 0x80000000u) | ((unsigned int)(e - 896) << 23) | m23;
+    // round to nearest, ties to even; a carry out of the mantissa moves to the next binade
+    // (and from the largest finite binade to infinity), as rounding requires
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m23 & 1u))) f += 1u;
+    return __uint_as_float(f);
+}
+__device__ __forceinline__ double f32_to_f64(float x) {  // exact
+    const unsigned int b = __float_as_uint(x);
+    const unsigned int e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const unsigned long long r = ((unsigned long long)(b & 0x80000000u) << 32) |
+                                 ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)r);
+}
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
+
+// 1/x: an FP32 reciprocal refined by two Newton-Raphson steps r <- r + r (1 - x r) in FP64
+// (quadratic convergence from 2^-24 to below FP64 rounding), within an ulp of the FP64
+// quotient; IEEE division outside 2^-120 < |x| < 2^120 (and for NaN).
+__device__ __forceinline__ double recip_nr(double x) {
+    const double ax = fabs(x);
+    if (!(ax > 7.52316384526264e-37 && ax < 1.329227995784916e36)) return 1.0 / x;
+    double r = f32_to_f64(__frcp_rn(f64_to_f32_rn(x)));
+    r = fma(r, fma(-x, r, 1.0), r);
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
 __device__ __forceinline__ void c2prim_cell_fast(const DevParams& P, const double U[5], double q[6]) {
     double rho = fmax(U[0], P.eps_clamp);
     if (U[0] != U[0]) rho = U[0];
-    const double rinv = 1.0 / rho;
+    const double rinv = recip_nr(rho);
     const double u = U[1] * rinv, v = U[2] * rinv, w = U[3] * rinv;
     const double eraw = U[4] - 0.5 * rho * (u * u + v * v + w * w);
     double ei = fmax(eraw, P.eps_clamp);

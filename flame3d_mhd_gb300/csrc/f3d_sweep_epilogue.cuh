@@ -73,14 +73,14 @@ __device__ __forceinline__ void sweep_epilogue(const SweepArgs& a, const R* sF, 
         } else if (a.out_mode == OUT_RHS) {
             const double Jc = a.J[c];
 #pragma unroll
-            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * (double)(acc[c + n * pl] + d[n]);
+            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * to_f64(acc[c + n * pl] + d[n]);
         } else {  // OUT_STAGE: RK state accumulation in FP64
             const double Jact = a.J[c] * (a.dtl ? a.dtl[c] : a.dt);  // div_LTS: per-cell dt
 #pragma unroll
             for (int n = 0; n < 5; n++) {
                 const double u = a.U[c + n * pl];
                 if (a.stage1_copy) a.Un[c + n * pl] = u;
-                double un = u + (double)(acc[c + n * pl] + d[n]) * Jact;
+                double un = u + to_f64(acc[c + n * pl] + d[n]) * Jact;
                 if (a.combine) un = un * a.ca + a.Un[c + n * pl] * a.cb;
                 a.U[c + n * pl] = un;
             }

@@ -230,7 +230,8 @@ __global__ void k_visc_fvb(const DevParams P, const double* __restrict__ Lb, con
     const long long vpl = (long long)vxt * vyt * vzt;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= vpl) return;
-    const int vi = (int)(t % vxt), vj = (int)((t / vxt) % vyt), vk = (int)(t / ((long long)vxt * vyt));
+    int vi, vj, vk;
+    split3(t, P.dvxt, P.dvyt, vi, vj, vk);
     const int gi = vi + 2, gj = vj + 2, gk = vk + 2;  // full cell index
     const double k1 = 1.0 / 12.0, k2 = -2.0 / 3.0;
     const int g[3] = {gi, gj, gk};
@@ -271,7 +272,8 @@ __global__ void k_visc_vjp(const DevParams P, const double* __restrict__ Q, cons
     const long long vpl = (long long)vxt * vyt * vzt;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= vpl) return;
-    const int vi = (int)(t % vxt), vj = (int)((t / vxt) % vyt), vk = (int)(t / ((long long)vxt * vyt));
+    int vi, vj, vk;
+    split3(t, P.dvxt, P.dvyt, vi, vj, vk);
     const long long c = lin3(P, vi + 2, vj + 2, vk + 2);
     const long long pl = P.plane, sy = P.nxt, sz = (long long)P.nxt * P.nyt;
     const double M[3][3] = {{m0[c], m1[c], m2[c]}, {m3[c], m4[c], m5[c]}, {m6[c], m7[c], m8[c]}};  // M[d][x]
@@ -359,7 +361,8 @@ __global__ void k_visc_vjp(const DevParams P, const double* __restrict__ Q, cons
 __global__ void k_visc_gather(const DevParams P, const double* __restrict__ gb, double* Qb) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
-    const int i = (int)(c % P.nxt), j = (int)((c / P.nxt) % P.nyt), k = (int)(c / ((long long)P.nxt * P.nyt));
+    int i, j, k;
+    split3(c, P.dnxt, P.dnyt, i, j, k);
     const int vxt = P.nxt - 4, vyt = P.nyt - 4, vzt = P.nzt - 4;
     const long long vpl = (long long)vxt * vyt * vzt;
     const double c1 = 1.0 / 12.0, c2 = -2.0 / 3.0;
@@ -398,7 +401,8 @@ __global__ void k_visc_gather(const DevParams P, const double* __restrict__ gb, 
 __global__ void k_fill_vjp(const DevParams P, const double* __restrict__ Q, double* Qb) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
-    const int i = (int)(c % P.nxt), j = (int)((c / P.nxt) % P.nyt), k = (int)(c / ((long long)P.nxt * P.nyt));
+    int i, j, k;
+    split3(c, P.dnxt, P.dnyt, i, j, k);
     if (i >= NG && i < P.nx + NG && j >= NG && j < P.ny + NG && k >= NG && k < P.nz + NG) return;
     const GhostChain ch = resolve_ghost(P, i, j, k);
     if (ch.dirichlet >= 0) return;
@@ -429,7 +433,8 @@ __global__ void k_c2prim_vjp(const DevParams P, const double* __restrict__ U, co
                              double* out, double alpha, double beta) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
-    const int i = (int)(c % P.nxt), j = (int)((c / P.nxt) % P.nyt), k = (int)(c / ((long long)P.nxt * P.nyt));
+    int i, j, k;
+    split3(c, P.dnxt, P.dnyt, i, j, k);
     if (!(i >= NG && i < P.nx + NG && j >= NG && j < P.ny + NG && k >= NG && k < P.nz + NG)) return;
     const long long pl = P.plane;
     double u[5], qb[6], ub[5];
@@ -446,7 +451,8 @@ __global__ void k_c2prim_vjp(const DevParams P, const double* __restrict__ U, co
 __global__ void k_axpby(const DevParams P, double* out, const double* x, double a, const double* y, double b) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
-    const int i = (int)(c % P.nxt), j = (int)((c / P.nxt) % P.nyt), k = (int)(c / ((long long)P.nxt * P.nyt));
+    int i, j, k;
+    split3(c, P.dnxt, P.dnyt, i, j, k);
     const bool in = i >= NG && i < P.nx + NG && j >= NG && j < P.ny + NG && k >= NG && k < P.nz + NG;
     for (int n = 0; n < 5; n++) {
         const long long o = c + n * P.plane;

@@ -432,7 +432,8 @@ __global__ void k_stage_update(const DevParams P, const double* __restrict__ acc
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = (long long)P.nx * P.ny * P.nz;
     if (t >= n) return;
-    const int i = (int)(t % P.nx), j = (int)((t / P.nx) % P.ny), k = (int)(t / ((long long)P.nx * P.ny));
+    int i, j, k;
+    split3(t, P.dnx, P.dny, i, j, k);
     const long long c = lin3(P, i + NG, j + NG, k + NG), pl = P.plane;
     const double Jact = J[c] * (dtl ? dtl[c] : dt);
 #pragma unroll

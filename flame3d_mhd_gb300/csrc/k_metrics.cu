@@ -27,7 +27,8 @@ __global__ void k_metrics(const DevParams P, const double* x, const double* y, c
                           double* m8, double* J) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
-    const int i = (int)(c % P.nxt), j = (int)((c / P.nxt) % P.nyt), k = (int)(c / ((long long)P.nxt * P.nyt));
+    int i, j, k;
+    split3(c, P.dnxt, P.dnyt, i, j, k);
     const long long sy = P.nxt, sz = (long long)P.nxt * P.nyt;
     const double xxi = dcoord(x, c, 1, i, P.nxt), yxi = dcoord(y, c, 1, i, P.nxt), zxi = dcoord(z, c, 1, i, P.nxt);
     const double xet = dcoord(x, c, sy, j, P.nyt), yet = dcoord(y, c, sy, j, P.nyt), zet = dcoord(z, c, sy, j, P.nyt);

@@ -13,10 +13,7 @@ static unsigned pw_blocks(long long n) {
 }
 
 __device__ __forceinline__ void cell_ijk(const DevParams& P, long long c, int& i, int& j, int& k) {
-    i = (int)(c % P.nxt);
-    long long r = c / P.nxt;
-    j = (int)(r % P.nyt);
-    k = (int)(r / P.nyt);
+    split3(c, P.dnxt, P.dnyt, i, j, k);
 }
 
 __device__ __forceinline__ bool is_interior(const DevParams& P, int i, int j, int k) {
@@ -86,7 +83,7 @@ __global__ void k_prim_fill(const DevParams P, const double* U, double* Q, doubl
     if (csnd) csnd[c] = sound_speed(P, q);
     if (Q32) {
 #pragma unroll
-        for (int n = 0; n < 6; n++) Q32[c + n * pl] = (float)q[n];
+        for (int n = 0; n < 6; n++) Q32[c + n * pl] = f64_to_f32_rn(q[n]);
     }
 }
 
@@ -101,9 +98,9 @@ __global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst
     long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
     if (i + 1 < n) {
         const double2 v = *reinterpret_cast<const double2*>(src + i);
-        *reinterpret_cast<float2*>(dst + i) = make_float2((float)v.x, (float)v.y);
+        *reinterpret_cast<float2*>(dst + i) = make_float2(f64_to_f32_rn(v.x), f64_to_f32_rn(v.y));
     } else if (i < n) {
-        dst[i] = (float)src[i];
+        dst[i] = f64_to_f32_rn(src[i]);
     }
 }
 cudaError_t launch_to_f32(const double* src, float* dst, long long n, cudaStream_t st) {
@@ -306,7 +303,8 @@ __global__ void k_div_ref(const DevParams P, double* U, const double* Fx, const 
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nint = (long long)P.nx * P.ny * P.nz;
     if (t >= nint) return;
-    const int i = (int)(t % P.nx), j = (int)((t / P.nx) % P.ny), k = (int)(t / ((long long)P.nx * P.ny));
+    int i, j, k;
+    split3(t, P.dnx, P.dny, i, j, k);
     const long long c = lin3(P, i + NG, j + NG, k + NG);
     const double Jact = J[c] * dt;
     const long long fx = P.nx + 1, fy = P.ny + 1, fz = P.nz + 1;

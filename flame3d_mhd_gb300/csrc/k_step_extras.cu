@@ -19,7 +19,8 @@ __global__ void k_local_dt(const DevParams P, const double* __restrict__ Q, Metr
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = (long long)P.nx * P.ny * P.nz;
     if (t >= n) return;
-    const int i = (int)(t % P.nx), j = (int)((t / P.nx) % P.ny), k = (int)(t / ((long long)P.nx * P.ny));
+    int i, j, k;
+    split3(t, P.dnx, P.dny, i, j, k);
     const long long c = lin3(P, i + NG, j + NG, k + NG), pl = P.plane;
     const double u = Q[c + pl], v = Q[c + 2 * pl], w = Q[c + 3 * pl], T = Q[c + 5 * pl];
     const double V = 1.0 / m.J[c];
@@ -49,7 +50,8 @@ __device__ __forceinline__ bool interior_cell(const DevParams& P, int dir, long 
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = (long long)P.nx * P.ny * P.nz;
     if (t >= n) return false;
-    const int i = (int)(t % P.nx), j = (int)((t / P.nx) % P.ny), k = (int)(t / ((long long)P.nx * P.ny));
+    int i, j, k;
+    split3(t, P.dnx, P.dny, i, j, k);
     c = lin3(P, i + NG, j + NG, k + NG);
     s = dir == 0 ? 1 : (dir == 1 ? (long long)P.nxt : (long long)P.nxt * P.nyt);
     return true;

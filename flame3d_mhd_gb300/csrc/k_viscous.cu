@@ -19,7 +19,8 @@ __global__ void __launch_bounds__(128) k_viscous(const DevParams P, const R* __r
     const long long vpl = (long long)vxt * vyt * vzt;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= vpl) return;
-    const int vi = (int)(t % vxt), vj = (int)((t / vxt) % vyt), vk = (int)(t / ((long long)vxt * vyt));
+    int vi, vj, vk;
+    split3(t, P.dvxt, P.dvyt, vi, vj, vk);
     const long long c = lin3(P, vi + 2, vj + 2, vk + 2);
     const long long pl = P.plane, sy = P.nxt, sz = (long long)P.nxt * P.nyt;
     const Cst<R>& K = cst<R>(P);

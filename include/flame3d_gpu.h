@@ -256,6 +256,12 @@ int f3d_local_dt(f3d_ctx* ctx, const double* Q, double* dt, f3d_stream stream);
  * kernels read it at each launch). */
 int f3d_set_inflow_profile(f3d_ctx* ctx, int face, const double* prof, f3d_stream stream);
 
+/* The rounding of FP64 values to FP32 the mixed form uses for its FP32 copies (integer
+ * operations on the IEEE 754 layouts, round to nearest even), on n device values; for
+ * checking it against the conversion instruction. No context; no counterpart in the
+ * reference. */
+int f3d_debug_round_f32(const double* in, float* out, long long n, f3d_stream stream);
+
 /* ---- discrete adjoint (FP64, component-wise reconstruction, SW or LF splitting) ---- */
 
 /* Ubar = (dL/dU)^T Lbar at interior cells (ghost cells of Ubar are zeroed), where

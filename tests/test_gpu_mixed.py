@@ -111,3 +111,33 @@ def test_mixed_wall_pressure_within_1e5(gpu_lib):
     pw32 = Q32[4, NG:-NG, NG, NG:-NG]
     assert float(np.abs(pw32 - pw64).max() / np.abs(pw64).max()) <= 1e-5
     assert abs(pw32.mean() - pw64.mean()) <= 1e-5 * abs(pw64.mean())
+
+
+def test_fp32_rounding_is_the_conversion_instruction(gpu_lib):
+    """The mixed form's FP32 copies round FP64 values with integer operations on the IEEE
+    layouts: bitwise equal to the conversion instruction (torch's .float()) on random values
+    over the whole binary32 range and beyond, exact ties (both parities), the largest finite
+    binade, subnormal results, zeros, infinities and NaN."""
+    import ctypes as C
+    rng = np.random.default_rng(17)
+    vals = [rng.standard_normal(2_000_000) * np.exp2(rng.integers(-160, 160, 2_000_000))]
+    # exact ties: 29 dropped bits = 1 followed by zeros, even and odd kept mantissas
+    m = rng.integers(0, 1 << 23, 200_000, dtype=np.int64)
+    e = rng.integers(897, 1151, 200_000, dtype=np.int64)
+    ties = ((e << 52) | (m << 29) | (1 << 28)).view(np.float64)
+    vals += [ties, -ties, np.nextafter(ties, 0), np.nextafter(ties, np.inf)]
+    fmax = float(np.finfo(np.float32).max)
+    vals.append(np.array([0.0, -0.0, np.inf, -np.inf, np.nan, fmax, -fmax, fmax * (1 + 2 ** -25),
+                          fmax * (1 + 2 ** -24), 2.0 ** -126, 2.0 ** -127, 2.0 ** -149, 2.0 ** -150,
+                          1.1754942e-38, 3.4e38, 1e-45, 1e300, -1e-300]))
+    x = np.concatenate(vals)
+    xd = torch.from_numpy(x).cuda()
+    out = torch.empty(x.size, dtype=torch.float32, device="cuda")
+    rc = gpu_lib.f3d_debug_round_f32(C.c_void_p(xd.data_ptr()), C.c_void_p(out.data_ptr()), x.size, None)
+    assert rc == 0
+    ref = xd.float()
+    torch.cuda.synchronize()
+    a, b = out.cpu().numpy().view(np.uint32), ref.cpu().numpy().view(np.uint32)
+    nan = np.isnan(ref.cpu().numpy())
+    assert np.array_equal(a[~nan], b[~nan])
+    assert np.isnan(out.cpu().numpy()[nan]).all()
