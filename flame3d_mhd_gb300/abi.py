@@ -134,6 +134,8 @@ def load() -> C.CDLL:
         "f3d_filter": (ip, [vp, vp, vp, vp, vp]),
         "f3d_local_dt": (ip, [vp, vp, vp, vp]),
         "f3d_debug_round_f32": (ip, [vp, vp, C.c_longlong, vp]),
+        "f3d_set_inflow_profile_cotangent": (ip, [vp, ip, vp, vp]),
+        "f3d_rk3_step_vjp_stages": (ip, [vp, C.c_double, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -150,7 +152,8 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_check_finite", "f3d_debug_sensor", "f3d_debug_split", "f3d_debug_face_flux",
             "f3d_debug_viscous", "f3d_div", "f3d_measure_pipes", "f3d_kernel_count", "f3d_kernel_name",
             "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp", "f3d_set_inflow_profile",
-            "f3d_set_coordinates", "f3d_filter", "f3d_local_dt", "f3d_debug_round_f32"]
+            "f3d_set_coordinates", "f3d_filter", "f3d_local_dt", "f3d_debug_round_f32",
+            "f3d_set_inflow_profile_cotangent", "f3d_rk3_step_vjp_stages"]
 
 
 class F3DError(RuntimeError):

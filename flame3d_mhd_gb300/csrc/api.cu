@@ -175,7 +175,7 @@ struct f3d_ctx {
     // adjoint scratch, allocated by the first VJP call
     void* adj_slab = nullptr;
     double *Qb = nullptr, *Lt = nullptr, *U1 = nullptr, *U2 = nullptr, *Xb = nullptr, *Yb = nullptr;
-    double *Qst[3] = {}, *cst_[3] = {}, *phst[3] = {};  // Q, sound speed and sensor of the 3 stage states
+    double *Qst[1] = {}, *cst_[1] = {}, *phst[1] = {};  // Q, sound speed and sensor of one stage state
     double *Fvb[3] = {}, *gb = nullptr;
     // CUDA graph of one RK3 step, keyed by its arguments
     cudaGraphExec_t step_graph = nullptr;
@@ -421,7 +421,7 @@ int adjoint_alloc(f3d_ctx* ctx) {
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t b1 = up(nc * 8);
     const size_t bv = up(nv * 8);
-    size_t total = b1 * (6 + 5 * 5 + 3 * 8) + (ctx->params.viscous ? bv * (12 + 12) : 0);
+    size_t total = b1 * (6 + 5 * 5 + 8) + (ctx->params.viscous ? bv * (12 + 12) : 0);
     cudaError_t e = cudaMalloc(&ctx->adj_slab, total);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc (adjoint scratch)");
     char* q = (char*)ctx->adj_slab;
@@ -431,11 +431,9 @@ int adjoint_alloc(f3d_ctx* ctx) {
     ctx->U2 = (double*)q; q += 5 * b1;
     ctx->Xb = (double*)q; q += 5 * b1;
     ctx->Yb = (double*)q; q += 5 * b1;
-    for (int k = 0; k < 3; k++) {
-        ctx->Qst[k] = (double*)q; q += 6 * b1;
-        ctx->cst_[k] = (double*)q; q += b1;
-        ctx->phst[k] = (double*)q; q += b1;
-    }
+    ctx->Qst[0] = (double*)q; q += 6 * b1;
+    ctx->cst_[0] = (double*)q; q += b1;
+    ctx->phst[0] = (double*)q; q += b1;
     if (ctx->params.viscous) {
         for (int d = 0; d < 3; d++) { ctx->Fvb[d] = (double*)q; q += 4 * bv; }
         ctx->gb = (double*)q;
@@ -495,7 +493,7 @@ int rhs_vjp_prepared(f3d_ctx* ctx, const double* U, const double* Q, const doubl
     }
     if (ctx->params.viscous)
         F3D_CUDA(ctx, launch_viscous_vjp(P, Q, ctx->m, ctx->J, Lb, ctx->Fvb, ctx->gb, ctx->Qb, st));
-    F3D_CUDA(ctx, launch_fill_vjp(P, Q, ctx->Qb, st));
+    F3D_CUDA(ctx, launch_fill_vjp(P, Q, ctx->Qb, alpha, st));
     F3D_CUDA(ctx, launch_c2prim_vjp(P, U, ctx->Qb, out, alpha, beta, st));
     return F3D_OK;
 }
@@ -800,6 +798,20 @@ int f3d_set_coordinates(f3d_ctx* ctx, const double* x, const double* y, const do
     return F3D_OK;
 }
 
+int f3d_set_inflow_profile_cotangent(f3d_ctx* ctx, int face, double* prof_bar, f3d_stream stream) {
+    (void)stream;
+    if (!ctx) return F3D_ERR_ARG;
+    if (face < 0 || face > 5) return fail(ctx, F3D_ERR_ARG, "face must be 0..5");
+    if (ctx->params.bc[face].kind != F3D_BC_INFLOW_PROFILE)
+        return fail(ctx, F3D_ERR_ARG, "face is not an F3D_BC_INFLOW_PROFILE face");
+    if (prof_bar) {
+        int rc = check_ptrs(ctx, {prof_bar});
+        if (rc) return rc;
+    }
+    ctx->dp.profb[face] = prof_bar;
+    return F3D_OK;
+}
+
 int f3d_set_inflow_profile(f3d_ctx* ctx, int face, const double* prof, f3d_stream stream) {
     (void)stream;
     if (!ctx) return F3D_ERR_ARG;
@@ -828,24 +840,40 @@ int f3d_rhs_vjp(f3d_ctx* ctx, const double* U, const double* Lbar, double* Ubar,
 // states are recomputed from U0, then the stages are reversed.
 int f3d_rk3_step_vjp(f3d_ctx* ctx, double dt, const double* U0, const double* Ubar_next, double* Ubar,
                      f3d_stream stream) {
+    return f3d_rk3_step_vjp_stages(ctx, dt, U0, Ubar_next, Ubar, nullptr, nullptr, stream);
+}
+
+// The same, also returning the three stage states V_s (U0, U1, U2) and the cotangents of
+// their RHS values L(V_s) (dt times the stage cotangents the step VJP applies).
+int f3d_rk3_step_vjp_stages(f3d_ctx* ctx, double dt, const double* U0, const double* Ubar_next, double* Ubar,
+                            double* Ustage, double* Lbar_stage, f3d_stream stream) {
     int rc = check_ctx(ctx, true);
     if (rc || (rc = check_ptrs(ctx, {U0, Ubar_next, Ubar}))) return rc;
     if (Ubar == Ubar_next || Ubar == U0) return fail(ctx, F3D_ERR_ARG, "Ubar must not alias U0 or Ubar_next");
+    for (double* o : {Ustage, Lbar_stage})
+        if (o && (rc = check_ptrs(ctx, {o}))) return rc;
     if ((rc = adjoint_supported(ctx)) || (rc = adjoint_alloc(ctx))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const DevParams& P = ctx->dp;
-    // forward recompute of the stage states, keeping what each stage's VJP needs
+    // forward recompute of the two intermediate stage states U1, U2
     const double* Us[3] = {U0, ctx->U1, ctx->U2};
     if ((rc = prep_state(ctx, U0, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
     if ((rc = rhs_prepared(ctx, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], ctx->Lt, st))) return rc;
     F3D_CUDA(ctx, launch_axpby(P, ctx->U1, U0, 1.0, ctx->Lt, dt, st));
-    if ((rc = prep_state(ctx, ctx->U1, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], st))) return rc;
-    if ((rc = rhs_prepared(ctx, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], ctx->Lt, st))) return rc;
+    if ((rc = prep_state(ctx, ctx->U1, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
+    if ((rc = rhs_prepared(ctx, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], ctx->Lt, st))) return rc;
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U1, 0.25, ctx->Lt, 0.25 * dt, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U2, 1.0, U0, 0.75, st));
-    if ((rc = prep_state(ctx, ctx->U2, ctx->Qst[2], ctx->cst_[2], ctx->phst[2], st))) return rc;
+    // one cache for a prepared stage state (Q, sound speed, sensor): each stage's VJP
+    // prepares its state again (c2Prim with the ghost fill, and the sensor) rather than
+    // keeping three copies (16 planes more)
+    const long long pl5 = 5 * P.plane;
+    if (Ustage)
+        for (int k = 0; k < 3; k++) F3D_CUDA(ctx, launch_axpby(P, Ustage + k * pl5, Us[k], 1.0, nullptr, 0.0, st));
     auto vjp = [&](int k, const double* Lb, double* out) {
-        return rhs_vjp_prepared(ctx, Us[k], ctx->Qst[k], ctx->cst_[k], ctx->phst[k], Lb, out, dt, 1.0, st);
+        if (Lbar_stage) F3D_CUDA(ctx, launch_axpby(P, Lbar_stage + k * pl5, Lb, dt, nullptr, 0.0, st));
+        int r = prep_state(ctx, Us[k], ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st);
+        return r ? r : rhs_vjp_prepared(ctx, Us[k], ctx->Qst[0], ctx->cst_[0], ctx->phst[0], Lb, out, dt, 1.0, st);
     };
     // stage 3: U3 = 1/3 U0 + 2/3 W, W = U2 + dt L(U2)
     F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar_next, 1.0 / 3.0, nullptr, 0.0, st));

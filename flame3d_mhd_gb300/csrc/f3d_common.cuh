@@ -84,6 +84,7 @@ struct DevParams {
     int les;            // F3D_LES_* in the viscous fluxes
     BcDev bc[6];
     const double* prof[6];  // F3D_BC_INFLOW_PROFILE states (5 x Ta x Tb), borrowed
+    double* profb[6];       // their cotangents, accumulated by the adjoint when set
 };
 
 template <class R> __host__ __device__ inline const Cst<R>& cst(const DevParams& P);

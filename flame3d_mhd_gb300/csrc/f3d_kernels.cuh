@@ -55,7 +55,7 @@ cudaError_t adjoint_configure();
 cudaError_t launch_sweep_vjp(int dir, const AdjArgs& a, cudaStream_t st);
 cudaError_t launch_viscous_vjp(const DevParams& P, const double* Q, const double* const m[9], const double* J,
                                const double* Lb, double* Fvb[3], double* gb, double* Qb, cudaStream_t st);
-cudaError_t launch_fill_vjp(const DevParams& P, const double* Q, double* Qb, cudaStream_t st);
+cudaError_t launch_fill_vjp(const DevParams& P, const double* Q, double* Qb, double pscale, cudaStream_t st);
 cudaError_t launch_c2prim_vjp(const DevParams& P, const double* U, const double* Qb, double* out, double alpha,
                               double beta, cudaStream_t st);
 cudaError_t launch_axpby(const DevParams& P, double* out, const double* x, double a, const double* y, double b,

@@ -398,18 +398,22 @@ __global__ void k_visc_gather(const DevParams P, const double* __restrict__ gb, 
 // Transpose of the composed ghost rules: a ghost cell's cotangent goes to its interior
 // source (copies and mirrors), nowhere for Dirichlet values; isothermal walls pass p, T
 // through T_g = 2 T_w - T_s and rho_g = p_s / (Rg T_g).
-__global__ void k_fill_vjp(const DevParams P, const double* __restrict__ Q, double* Qb) {
+// Inflow-profile cotangents (when a buffer is set) receive pscale times theirs: the RHS VJP
+// scales its state cotangent by alpha after c2Prim, and the profile enters before it.
+__global__ void k_fill_vjp(const DevParams P, const double* __restrict__ Q, double* Qb, double pscale) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
     int i, j, k;
     split3(c, P.dnxt, P.dnyt, i, j, k);
     if (i >= NG && i < P.nx + NG && j >= NG && j < P.ny + NG && k >= NG && k < P.nz + NG) return;
     const GhostChain ch = resolve_ghost(P, i, j, k);
-    if (ch.dirichlet >= 0) return;
+    const bool to_profile = ch.dirichlet >= 0 && P.bc[ch.dirichlet].kind == F3D_BC_INFLOW_PROFILE &&
+                            P.profb[ch.dirichlet] != nullptr;
+    if (ch.dirichlet >= 0 && !to_profile) return;  // a fixed state: no dependence
     const long long pl = P.plane;
     double gq[6];
     for (int n = 0; n < 6; n++) gq[n] = Qb[c + n * pl];
-    const long long s = lin3(P, ch.si, ch.sj, ch.sk);
+    const long long s = to_profile ? 0 : lin3(P, ch.si, ch.sj, ch.sk);
     double sq_[6] = {gq[0], gq[1], gq[2], gq[3], gq[4], gq[5]};
     if (ch.nmirror & 1) {
         sq_[1] = -gq[1];
@@ -424,6 +428,18 @@ __global__ void k_fill_vjp(const DevParams P, const double* __restrict__ Q, doub
         sq_[4] = gq[4] + rhob / (P.rg * Tg);
         const double Tgb = gq[5] - rhob * pg / (P.rg * Tg * Tg);
         sq_[5] = -Tgb;
+    }
+    if (to_profile) {
+        // the chain's first value is the profile state q = (rho, u, v, w, p, p / (rho Rg)) of
+        // its transverse point: pass the cotangent to (rho, u, v, w, p) of that point
+        const double* pr = P.prof[ch.dirichlet] + ch.poff;
+        double* pb = P.profb[ch.dirichlet] + ch.poff;
+        const double rho = pr[0], p = pr[4 * ch.pst];
+        const double T = p / (rho * P.rg);
+        const double b[5] = {sq_[0] - sq_[5] * T / rho, sq_[1], sq_[2], sq_[3], sq_[4] + sq_[5] / (rho * P.rg)};
+        for (int n = 0; n < 5; n++)
+            if (b[n] != 0.0) atomicAdd(&pb[n * ch.pst], pscale * b[n]);
+        return;
     }
     for (int n = 0; n < 6; n++)
         if (sq_[n] != 0.0) atomicAdd(&Qb[s + n * pl], sq_[n]);
@@ -502,8 +518,8 @@ cudaError_t launch_viscous_vjp(const DevParams& P, const double* Q, const double
     return cudaGetLastError();
 }
 
-cudaError_t launch_fill_vjp(const DevParams& P, const double* Q, double* Qb, cudaStream_t st) {
-    k_fill_vjp<<<blocks_for(P.plane, 256), 256, 0, st>>>(P, Q, Qb);
+cudaError_t launch_fill_vjp(const DevParams& P, const double* Q, double* Qb, double pscale, cudaStream_t st) {
+    k_fill_vjp<<<blocks_for(P.plane, 256), 256, 0, st>>>(P, Q, Qb, pscale);
     return cudaGetLastError();
 }
 

@@ -136,6 +136,19 @@ class Flame3D:
         self._check(self.lib.f3d_set_coordinates(self._h, self._ptr(x, 1), self._ptr(y, 1), self._ptr(z, 1),
                                                  self._stream()))
 
+    def set_inflow_profile_cotangent(self, face: int, prof_bar: torch.Tensor | None):
+        """Accumulate dJ/d(profile of face) into prof_bar during the adjoint calls (None stops)."""
+        if prof_bar is None:
+            self._check(self.lib.f3d_set_inflow_profile_cotangent(self._h, face, None, self._stream()))
+            return
+        if (tuple(prof_bar.shape) != self.profile_shape(face) or prof_bar.dtype != torch.float64
+                or not prof_bar.is_cuda or not prof_bar.is_contiguous()):
+            raise ValueError(f"expected a contiguous float64 CUDA tensor of shape {self.profile_shape(face)}")
+        self._check(self.lib.f3d_set_inflow_profile_cotangent(self._h, face, C.c_void_p(prof_bar.data_ptr()),
+                                                              self._stream()))
+        self._profile_bars = getattr(self, "_profile_bars", {})
+        self._profile_bars[face] = prof_bar
+
     def profile_shape(self, face: int) -> tuple[int, int, int]:
         """(5, Tb, Ta) of an inflow-profile face: its transverse extent including ghosts."""
         nxt, nyt, nzt = self.shape3[2], self.shape3[1], self.shape3[0]
@@ -236,13 +249,27 @@ class Flame3D:
         return Ubar
 
     def rk3_step_vjp(self, dt: float, U0: torch.Tensor, Ubar_next: torch.Tensor,
-                     Ubar: torch.Tensor | None = None) -> torch.Tensor:
-        """Cotangent of the state at the start of one SSP-RK3 step from the one at its end."""
+                     Ubar: torch.Tensor | None = None, Ustage: torch.Tensor | None = None,
+                     Lbar_stage: torch.Tensor | None = None) -> torch.Tensor:
+        """Cotangent of the state at the start of one SSP-RK3 step from the one at its end.
+        Ustage / Lbar_stage, shape (3, 5, Nzt, Nyt, Nxt) when given, receive the three stage
+        states and the cotangents of their RHS values (interior cells)."""
         if Ubar is None:
             Ubar = self.field(5)
-        self._check(self.lib.f3d_rk3_step_vjp(self._h, dt, self._ptr(U0, 5), self._ptr(Ubar_next, 5),
-                                              self._ptr(Ubar, 5), self._stream()))
+        if Ustage is None and Lbar_stage is None:
+            self._check(self.lib.f3d_rk3_step_vjp(self._h, dt, self._ptr(U0, 5), self._ptr(Ubar_next, 5),
+                                                  self._ptr(Ubar, 5), self._stream()))
+            return Ubar
+        opt = [None if t is None else C.c_void_p(self._stages_ptr(t)) for t in (Ustage, Lbar_stage)]
+        self._check(self.lib.f3d_rk3_step_vjp_stages(self._h, dt, self._ptr(U0, 5), self._ptr(Ubar_next, 5),
+                                                     self._ptr(Ubar, 5), opt[0], opt[1], self._stream()))
         return Ubar
+
+    def _stages_ptr(self, t: torch.Tensor) -> int:
+        want = (3, 5, *self.shape3)
+        if tuple(t.shape) != want or t.dtype != torch.float64 or not t.is_contiguous() or not t.is_cuda:
+            raise ValueError(f"expected a contiguous float64 CUDA tensor of shape {want}")
+        return t.data_ptr()
 
     def q_from_u(self, U: torch.Tensor, Q: torch.Tensor | None = None) -> torch.Tensor:
         """Q = c2Prim(U) with its ghost layers (and U's) filled: the stage input of solver.jl."""

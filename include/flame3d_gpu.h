@@ -264,6 +264,13 @@ int f3d_debug_round_f32(const double* in, float* out, long long n, f3d_stream st
 
 /* ---- discrete adjoint (FP64, component-wise reconstruction, SW or LF splitting) ---- */
 
+/* Let the adjoint calls of the context also accumulate the cotangent of an inflow-profile
+ * face's state (the same 5 x Ta x Tb layout as f3d_set_inflow_profile) into prof_bar: every
+ * f3d_rhs_vjp / f3d_rk3_step_vjp adds its share, so after a backward pass prof_bar holds
+ * dJ/d(profile) (the caller zeroes it first). nullptr stops the accumulation. No counterpart
+ * in the reference. */
+int f3d_set_inflow_profile_cotangent(f3d_ctx* ctx, int face, double* prof_bar, f3d_stream stream);
+
 /* Ubar = (dL/dU)^T Lbar at interior cells (ghost cells of Ubar are zeroed), where
  * L(U) = RHS(ghost-filled c2Prim(U)) is the right-hand side as a function of the interior
  * conserved state. Branches (hybrid scheme choice, minmod, sign splits, c2Prim clamps)
@@ -278,6 +285,14 @@ int f3d_rhs_vjp(f3d_ctx* ctx, const double* U, const double* Lbar, double* Ubar,
  * (flame3d_mhd_gb300/adjoint.py). */
 int f3d_rk3_step_vjp(f3d_ctx* ctx, double dt, const double* U0, const double* Ubar_next, double* Ubar,
                      f3d_stream stream);
+
+/* f3d_rk3_step_vjp that also writes, when non-null, the step's three stage states
+ * V_0 = U0, V_1 = U1, V_2 = U2 into Ustage (3 x 5 planes) and the cotangents of their RHS
+ * values L(V_s) into Lbar_stage (3 x 5 planes; dt times the stage cotangent), interior cells
+ * (ghost cells zero). With these a caller forms the gradient with respect to any parameter
+ * theta of the RHS: the step contributes sum_s <Lbar_s, dL/dtheta at V_s>. */
+int f3d_rk3_step_vjp_stages(f3d_ctx* ctx, double dt, const double* U0, const double* Ubar_next, double* Ubar,
+                            double* Ustage, double* Lbar_stage, f3d_stream stream);
 
 /* ---- stage-by-stage intermediates in the reference's own array shapes ----------- */
 

@@ -165,6 +165,27 @@ template <class R> void lincomb(const f3d_params& P, R* Up, const R* Unp, R a, R
                 for (long i = NG + 1; i <= g.nx + NG; i++) U(i, j, k, n) = U(i, j, k, n) * a + Un(i, j, k, n) * b;
 }
 
+// The Dirichlet ghost state (rho, u, v, w, p) with T = p / (rho Rg) and its conserved form.
+template <class R>
+void set_dirichlet(const Consts<R>& C, R rho, R u, R v, R w, R p, V4<R>& Q, V4<R>& U, long gi, long gj, long gk) {
+    R T = p / (rho * C.rg);
+    Q(gi, gj, gk, 1) = rho;
+    Q(gi, gj, gk, 2) = u;
+    Q(gi, gj, gk, 3) = v;
+    Q(gi, gj, gk, 4) = w;
+    Q(gi, gj, gk, 5) = p;
+    Q(gi, gj, gk, 6) = T;
+    U(gi, gj, gk, 1) = rho;
+    U(gi, gj, gk, 2) = rho * u;
+    U(gi, gj, gk, 3) = rho * v;
+    U(gi, gj, gk, 4) = rho * w;
+    U(gi, gj, gk, 5) = p / (C.gamma - R(1)) + R(0.5) * rho * (u * u + v * v + w * w);
+}
+
+// A value of type R seeded with a tangent: only dual numbers carry it.
+template <class R> inline R seeded(double v, double) { return R(v); }
+template <> inline Dual seeded<Dual>(double v, double d) { return Dual(v, d); }
+
 // ---------------------------------------------------------------------------------
 // Ghost fill: mpi.jl:2-103 (periodic exchange with self) and boundary.jl:1-156
 // (fill_x, fill_y, fill_z), applied in the order x, y, z over the full transverse
@@ -178,22 +199,9 @@ void fill_ghost_cell(const f3d_params& P, const Consts<R>& C, const f3d_bc& bc, 
         for (int n = 1; n <= 6; n++) Q(gi, gj, gk, n) = Q(si, sj, sk, n);
         for (int n = 1; n <= 5; n++) U(gi, gj, gk, n) = U(si, sj, sk, n);
         break;
-    case F3D_BC_DIRICHLET: {  // boundary.jl:12-38 and 98-118
-        R rho = R(bc.rho), u = R(bc.u), v = R(bc.v), w = R(bc.w), p = R(bc.p);
-        R T = p / (rho * C.rg);
-        Q(gi, gj, gk, 1) = rho;
-        Q(gi, gj, gk, 2) = u;
-        Q(gi, gj, gk, 3) = v;
-        Q(gi, gj, gk, 4) = w;
-        Q(gi, gj, gk, 5) = p;
-        Q(gi, gj, gk, 6) = T;
-        U(gi, gj, gk, 1) = rho;
-        U(gi, gj, gk, 2) = rho * u;
-        U(gi, gj, gk, 3) = rho * v;
-        U(gi, gj, gk, 4) = rho * w;
-        U(gi, gj, gk, 5) = p / (C.gamma - R(1)) + R(0.5) * rho * (u * u + v * v + w * w);
+    case F3D_BC_DIRICHLET:  // boundary.jl:12-38 and 98-118
+        set_dirichlet(C, R(bc.rho), R(bc.u), R(bc.v), R(bc.w), R(bc.p), Q, U, gi, gj, gk);
         break;
-    }
     case F3D_BC_WALL_ADIABATIC:
     case F3D_BC_WALL_ISOTHERMAL: {  // boundary.jl:67-93 (mirror about the wall)
         R rho = Q(si, sj, sk, 1), p = Q(si, sj, sk, 5), T = Q(si, sj, sk, 6);
@@ -225,6 +233,13 @@ void fill_ghost_cell(const f3d_params& P, const Consts<R>& C, const f3d_bc& bc, 
 inline const double*& inflow_profile(int face) {
     static const double* prof[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     return prof[face];
+}
+
+// Optional tangent of an inflow profile (same layout): dual-number runs seed the profile's
+// ghost states with it (forward-mode derivative with respect to the profile).
+inline const double*& inflow_profile_tangent(int face) {
+    static const double* dprof[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return dprof[face];
 }
 
 // Cell-centre coordinates (x, y, z with ghosts) for the finite-volume schemes, registered
@@ -270,16 +285,13 @@ template <class R> void fill_ghosts(const f3d_params& P, R* Qp, R* Up) {
                         if (bc.kind == F3D_BC_INFLOW_PROFILE) {
                             // the inlet of boundary.jl:10-38 with the state of this point
                             const double* pr = inflow_profile(2 * d + side);
+                            const double* dp = inflow_profile_tangent(2 * d + side);
                             const long st = ta * tb, off = (a - 1) + ta * (b - 1);
-                            f3d_bc pb = bc;
-                            pb.kind = F3D_BC_DIRICHLET;
-                            if (pr) {
-                                pb.rho = pr[off]; pb.u = pr[off + st]; pb.v = pr[off + 2 * st];
-                                pb.w = pr[off + 3 * st]; pb.p = pr[off + 4 * st];
-                            } else {  // not registered: poison the ghosts so the caller sees it
-                                pb.rho = pb.u = pb.v = pb.w = pb.p = std::numeric_limits<double>::quiet_NaN();
-                            }
-                            fill_ghost_cell(P, C, pb, Q, U, gi, gj, gk, si, sj, sk);
+                            R q[5];
+                            for (int n = 0; n < 5; n++)  // not registered: NaN ghosts, for the caller to see
+                                q[n] = seeded<R>(pr ? pr[off + n * st] : std::numeric_limits<double>::quiet_NaN(),
+                                                 dp ? dp[off + n * st] : 0.0);
+                            set_dirichlet(C, q[0], q[1], q[2], q[3], q[4], Q, U, gi, gj, gk);
                             continue;
                         }
                         fill_ghost_cell(P, C, bc, Q, U, gi, gj, gk, si, sj, sk);

@@ -37,6 +37,8 @@ def lib() -> C.CDLL:
         _lib.orc_set_threads.argtypes = [C.c_int]
         _lib.orc_set_inflow_profile.restype = None
         _lib.orc_set_inflow_profile.argtypes = [C.c_int, C.c_void_p]
+        _lib.orc_set_inflow_profile_tangent.restype = None
+        _lib.orc_set_inflow_profile_tangent.argtypes = [C.c_int, C.c_void_p]
         _lib.orc_set_coordinates.restype = None
         _lib.orc_set_coordinates.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     return _lib
@@ -80,6 +82,18 @@ def set_inflow_profile(face: int, prof: np.ndarray | None) -> None:
     a = np.ascontiguousarray(prof, dtype=np.float64)
     _profiles[face] = a  # keep it alive while registered
     lib().orc_set_inflow_profile(face, a.ctypes.data)
+
+
+def set_inflow_profile_tangent(face: int, dprof: np.ndarray | None) -> None:
+    """Register the tangent of an inflow profile (same layout) for the dual-number JVPs
+    (rhs_jvp_u, rk3_jvp_u); None clears it."""
+    if dprof is None:
+        _profiles.pop(("d", face), None)
+        lib().orc_set_inflow_profile_tangent(face, None)
+        return
+    a = np.ascontiguousarray(dprof, dtype=np.float64)
+    _profiles[("d", face)] = a
+    lib().orc_set_inflow_profile_tangent(face, a.ctypes.data)
 
 
 def set_threads(n: int) -> int:

@@ -55,6 +55,11 @@ void orc_set_inflow_profile(int face, const double* prof) {
     if (face >= 0 && face < 6) inflow_profile(face) = prof;
 }
 
+// Register (or clear) the tangent of an inflow profile for the dual-number entries.
+void orc_set_inflow_profile_tangent(int face, const double* dprof) {
+    if (face >= 0 && face < 6) inflow_profile_tangent(face) = dprof;
+}
+
 void orc_c2prim(const f3d_params* P, const double* U, double* Q) { c2prim<double>(*P, U, Q); }
 void orc_prim2c(const f3d_params* P, const double* Q, double* U) { prim2c<double>(*P, Q, U); }
 void orc_lincomb(const f3d_params* P, double* U, const double* Un, double a, double b) {
