@@ -11,7 +11,8 @@ import numpy as np
 NG = 4
 
 
-def extend_ghosts(x: np.ndarray, y: np.ndarray, z: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+def extend_ghosts(x: np.ndarray, y: np.ndarray, z: np.ndarray,
+                  dtype=np.float64) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Fill the ghost layers of interior coordinates as SCU-benchmark/readfort.jl:34-95 does.
 
     Point reflection about the first / last interior cell (x_g = 2 x_b - x_mirror) on the
@@ -19,9 +20,10 @@ def extend_ghosts(x: np.ndarray, y: np.ndarray, z: np.ndarray) -> tuple[np.ndarr
     the eta faces (readfort.jl:48-58); parallelogram completion x = x[i, b] + x[b, j] - x[b, b]
     in the four xi-eta edge regions (readfort.jl:61-83); then point reflection on the zeta
     faces over the full xi-eta extent (readfort.jl:85-95). Interior values are untouched.
-    Returns new arrays; inputs are (Nz+8, Ny+8, Nx+8) with the interior filled.
+    Returns new arrays of `dtype` (arithmetic in that type: np.float32 repeats the Float32
+    arrays of readfort.jl); inputs are (Nz+8, Ny+8, Nx+8) with the interior filled.
     """
-    X, Y, Z = (np.array(a, dtype=np.float64, copy=True) for a in (x, y, z))
+    X, Y, Z = (np.array(a, dtype=dtype, copy=True) for a in (x, y, z))
     nzt, nyt, nxt = X.shape
     nx, ny = nxt - 2 * NG, nyt - 2 * NG
     ki = slice(NG, nzt - NG)  # interior k
@@ -110,3 +112,61 @@ def compression_ramp_grid(nx: int, ny: int, nz: int, angle_deg: float = 24.0, x_
     z[I] = zs[:, None, None]
     x, y, z = extend_ghosts(x, y, z)
     return x, y, z, beta
+
+
+# ---- the mesh file of the reference's grid generator -----------------------------------
+# SCU-benchmark/swept-compression-ramp.c:451-560 writes OCFD3d-Mesh.dat as Fortran
+# unformatted sequential records: for x, then y, then z, one record per zeta plane k, each
+# a 4-byte length nx*ny*8, the nx*ny doubles of the plane (xi fastest) and the length again.
+# readfort.jl:14-33 reads it plane by plane into Float32 arrays.
+
+def write_ocfd_mesh(path: str, x: np.ndarray, y: np.ndarray, z: np.ndarray) -> None:
+    """Write interior coordinates ((Nz, Ny, Nx) each) in the OCFD3d-Mesh.dat record layout."""
+    shape = x.shape
+    if y.shape != shape or z.shape != shape or len(shape) != 3:
+        raise ValueError("x, y, z must be (Nz, Ny, Nx) arrays of one shape")
+    nz, ny, nx = shape
+    mark = np.array([nx * ny * 8], dtype="<i4").tobytes()
+    with open(path, "wb") as f:
+        for a in (x, y, z):
+            a = np.ascontiguousarray(a, dtype="<f8")
+            for k in range(nz):
+                f.write(mark)
+                f.write(a[k].tobytes())
+                f.write(mark)
+
+
+def read_ocfd_mesh(path: str, nx: int, ny: int, nz: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Interior coordinates ((Nz, Ny, Nx) float64 each) from an OCFD3d-Mesh.dat file; every
+    record length is checked (a file of other dimensions or a damaged file raises)."""
+    rec = nx * ny * 8
+    want = 3 * nz * (rec + 8)
+    raw = np.fromfile(path, dtype=np.uint8)
+    if raw.size != want:
+        raise ValueError(f"{path}: {raw.size} bytes, expected {want} for {nx}x{ny}x{nz}")
+    recs = raw.reshape(3, nz, rec + 8)
+    heads = recs[:, :, :4].copy().view("<i4").reshape(3, nz)
+    tails = recs[:, :, rec + 4:].copy().view("<i4").reshape(3, nz)
+    if not ((heads == rec).all() and (tails == rec).all()):
+        raise ValueError(f"{path}: record markers do not match {nx}x{ny} planes")
+    data = recs[:, :, 4:rec + 4].copy().view("<f8").reshape(3, nz, ny, nx).astype(np.float64)
+    return data[0], data[1], data[2]
+
+
+def mesh_from_ocfd(path: str, nx: int, ny: int, nz: int, divisor: float = 1000.0,
+                   dtype=np.float32) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """readfort.jl's generateXYZ (:14-100): the mesh file's planes into (Nz+8, Ny+8, Nx+8)
+    arrays of `dtype` (Float32 there), the ghost layers by extend_ghosts, then every
+    coordinate divided by `divisor` in that type (./= 1000.f0 there: millimetres to metres).
+    Pass dtype=np.float64 to keep the file's FP64 coordinates for f3d_compute_metrics."""
+    xi, yi, zi = read_ocfd_mesh(path, nx, ny, nz)
+    shape = (nz + 2 * NG, ny + 2 * NG, nx + 2 * NG)
+    I = (slice(NG, NG + nz), slice(NG, NG + ny), slice(NG, NG + nx))
+    out = []
+    for a in (xi, yi, zi):
+        A = np.zeros(shape, dtype=dtype)
+        A[I] = a.astype(dtype)
+        out.append(A)
+    X, Y, Z = extend_ghosts(*out, dtype=dtype)
+    d = np.dtype(dtype).type(divisor)
+    return X / d, Y / d, Z / d
