@@ -42,13 +42,13 @@ class F3DParams(C.Structure):
                 ("t_s", C.c_double), ("pr", C.c_double), ("phi1", C.c_double), ("phi2", C.c_double),
                 ("phi3", C.c_double), ("linear_phi", C.c_double), ("clamp_eps", C.c_double),
                 ("split_method", C.c_int32), ("character", C.c_int32), ("viscous", C.c_int32),
-                ("precision", C.c_int32), ("bc", F3DBc * 6), ("scheme", C.c_int32), ("pad2_", C.c_int32),
+                ("precision", C.c_int32), ("bc", F3DBc * 6), ("scheme", C.c_int32), ("adjoint_lean", C.c_int32),
                 ("lts", C.c_int32), ("filter", C.c_int32), ("filter_interval", C.c_int32), ("les", C.c_int32),
                 ("lts_cfl", C.c_double), ("filter_s0", C.c_double), ("filter_rth", C.c_double)]
 
 
 def params_to_dict(p: F3DParams) -> dict:
-    d = {f: getattr(p, f) for f, _ in F3DParams._fields_ if f not in ("bc", "pad2_")}
+    d = {f: getattr(p, f) for f, _ in F3DParams._fields_ if f != "bc"}
     d["bc"] = [{f: getattr(b, f) for f, _ in F3DBc._fields_ if f != "pad_"} for b in p.bc]
     return d
 

@@ -44,6 +44,7 @@ int validate_params(const f3d_params& p, std::string& why) {
     if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
     if (p.scheme < F3D_SCHEME_FDM || p.scheme > F3D_SCHEME_FVM_CONS) { why = "unknown scheme"; return F3D_ERR_ARG; }
     if (p.lts != 0 && p.lts != 1) { why = "lts must be 0 or 1"; return F3D_ERR_ARG; }
+    if (p.adjoint_lean != 0 && p.adjoint_lean != 1) { why = "adjoint_lean must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.lts && !(p.lts_cfl > 0.0)) { why = "lts_cfl must be > 0"; return F3D_ERR_ARG; }
     if (p.filter < F3D_FILTER_NONE || p.filter > F3D_FILTER_NONLINEAR) { why = "unknown filter"; return F3D_ERR_ARG; }
     if (p.filter && p.filter_interval < 1) { why = "filter_interval must be >= 1"; return F3D_ERR_ARG; }
@@ -175,7 +176,7 @@ struct f3d_ctx {
     // adjoint scratch, allocated by the first VJP call
     void* adj_slab = nullptr;
     double *Qb = nullptr, *Lt = nullptr, *U1 = nullptr, *U2 = nullptr, *Xb = nullptr, *Yb = nullptr;
-    double *Qst[1] = {}, *cst_[1] = {}, *phst[1] = {};  // Q, sound speed and sensor of one stage state
+    double *Qst[3] = {}, *cst_[3] = {}, *phst[3] = {};  // Q, sound speed and sensor of the stage states
     double *Fvb[3] = {}, *gb = nullptr;
     // CUDA graph of one RK3 step, keyed by its arguments
     cudaGraphExec_t step_graph = nullptr;
@@ -421,7 +422,8 @@ int adjoint_alloc(f3d_ctx* ctx) {
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t b1 = up(nc * 8);
     const size_t bv = up(nv * 8);
-    size_t total = b1 * (6 + 5 * 5 + 8) + (ctx->params.viscous ? bv * (12 + 12) : 0);
+    const int ncache = ctx->params.adjoint_lean ? 1 : 3;
+    size_t total = b1 * (6 + 5 * 5 + 8 * ncache) + (ctx->params.viscous ? bv * (12 + 12) : 0);
     cudaError_t e = cudaMalloc(&ctx->adj_slab, total);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc (adjoint scratch)");
     char* q = (char*)ctx->adj_slab;
@@ -431,9 +433,15 @@ int adjoint_alloc(f3d_ctx* ctx) {
     ctx->U2 = (double*)q; q += 5 * b1;
     ctx->Xb = (double*)q; q += 5 * b1;
     ctx->Yb = (double*)q; q += 5 * b1;
-    ctx->Qst[0] = (double*)q; q += 6 * b1;
-    ctx->cst_[0] = (double*)q; q += b1;
-    ctx->phst[0] = (double*)q; q += b1;
+    for (int k = 0; k < 3; k++) {  // lean: the three stages share one cache
+        if (k < ncache) {
+            ctx->Qst[k] = (double*)q; q += 6 * b1;
+            ctx->cst_[k] = (double*)q; q += b1;
+            ctx->phst[k] = (double*)q; q += b1;
+        } else {
+            ctx->Qst[k] = ctx->Qst[0]; ctx->cst_[k] = ctx->cst_[0]; ctx->phst[k] = ctx->phst[0];
+        }
+    }
     if (ctx->params.viscous) {
         for (int d = 0; d < 3; d++) { ctx->Fvb[d] = (double*)q; q += 4 * bv; }
         ctx->gb = (double*)q;
@@ -860,20 +868,22 @@ int f3d_rk3_step_vjp_stages(f3d_ctx* ctx, double dt, const double* U0, const dou
     if ((rc = prep_state(ctx, U0, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
     if ((rc = rhs_prepared(ctx, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], ctx->Lt, st))) return rc;
     F3D_CUDA(ctx, launch_axpby(P, ctx->U1, U0, 1.0, ctx->Lt, dt, st));
-    if ((rc = prep_state(ctx, ctx->U1, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
-    if ((rc = rhs_prepared(ctx, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], ctx->Lt, st))) return rc;
+    if ((rc = prep_state(ctx, ctx->U1, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], st))) return rc;
+    if ((rc = rhs_prepared(ctx, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], ctx->Lt, st))) return rc;
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U1, 0.25, ctx->Lt, 0.25 * dt, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U2, 1.0, U0, 0.75, st));
-    // one cache for a prepared stage state (Q, sound speed, sensor): each stage's VJP
-    // prepares its state again (c2Prim with the ghost fill, and the sensor) rather than
-    // keeping three copies (16 planes more)
+    // each stage's VJP needs its prepared state (Q, sound speed, sensor): kept from the
+    // recompute, or, with adjoint_lean (one shared cache), prepared again (c2Prim with the
+    // ghost fill, and the sensor) for stages 1 and 0
+    const bool lean = ctx->params.adjoint_lean != 0;
+    if ((rc = prep_state(ctx, ctx->U2, ctx->Qst[2], ctx->cst_[2], ctx->phst[2], st))) return rc;
     const long long pl5 = 5 * P.plane;
     if (Ustage)
         for (int k = 0; k < 3; k++) F3D_CUDA(ctx, launch_axpby(P, Ustage + k * pl5, Us[k], 1.0, nullptr, 0.0, st));
     auto vjp = [&](int k, const double* Lb, double* out) {
         if (Lbar_stage) F3D_CUDA(ctx, launch_axpby(P, Lbar_stage + k * pl5, Lb, dt, nullptr, 0.0, st));
-        int r = prep_state(ctx, Us[k], ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st);
-        return r ? r : rhs_vjp_prepared(ctx, Us[k], ctx->Qst[0], ctx->cst_[0], ctx->phst[0], Lb, out, dt, 1.0, st);
+        int r = (lean && k < 2) ? prep_state(ctx, Us[k], ctx->Qst[k], ctx->cst_[k], ctx->phst[k], st) : 0;
+        return r ? r : rhs_vjp_prepared(ctx, Us[k], ctx->Qst[k], ctx->cst_[k], ctx->phst[k], Lb, out, dt, 1.0, st);
     };
     // stage 3: U3 = 1/3 U0 + 2/3 W, W = U2 + dt L(U2)
     F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar_next, 1.0 / 3.0, nullptr, 0.0, st));

@@ -81,6 +81,8 @@ class RampAdjoint:
                                            character=0)
         if a.branch == "weno5":  # thresholds that leave the sensor no choice: WENO5 at every face
             self.case["params"] = params_copy(self.case["params"], phi1=0.0, phi2=0.0, phi3=5.0)
+        # one prepared stage state in the step VJP: 16 grid-sized arrays more for trajectory states
+        self.case["params"] = params_copy(self.case["params"], adjoint_lean=1)
         P = self.case["params"]
         self.gamma = P.gamma
         self.to = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(dev)

@@ -110,7 +110,8 @@ typedef struct f3d_params {
     int32_t precision;      /* F3D_PREC_*                                                */
     f3d_bc bc[6];           /* x-, x+, y-, y+, z-, z+                                    */
     int32_t scheme;         /* F3D_SCHEME_*; the finite-volume schemes are FP64 only       */
-    int32_t pad2_;
+    int32_t adjoint_lean;   /* 1: the step VJP keeps one prepared stage state instead of three
+                               (16 grid-sized arrays less, two more preparations per step) */
     /* step components beside the RK stage (run.jl:3-5, 21-22, 49-54; off by default)      */
     int32_t lts;            /* 1: local time stepping: each stage advances every cell by its
                                own dt = lts_cfl min_d(V/S_d/(u_d+c)) (utils.jl:73-99,

@@ -195,3 +195,19 @@ def test_windowed_wall_force_gradient_vs_central_differences(gpu_lib):
                              "--fd-angle-h", "1e-3", "--eta", "1e-3", "--mixed", "0"])
     (ch,) = out["checks"]
     assert ch["param"] == "theta_deg" and ch["rel_diff"] <= 1e-5, ch
+
+
+def test_lean_stage_cache_gives_the_same_step_vjp(gpu_lib, ramp):
+    """adjoint_lean = 1 (one prepared stage state, re-prepared per stage) against the
+    default three caches: the same VJP up to the order of FP64 atomics."""
+    from flame3d_mhd_gb300.cases import params_copy
+    c, m, J, U = ramp
+    s, keep = _solver(c, m, J)
+    cl = dict(c, params=params_copy(c["params"], adjoint_lean=1))
+    sl, keepl = _solver(cl, m, J)
+    Ud, Ub = dev(U), dev(_interior_random(U.shape, 9))
+    g = host(s.rk3_step_vjp(c["dt"], Ud, Ub))
+    gl = host(sl.rk3_step_vjp(c["dt"], Ud, Ub))
+    assert np.abs(g[I] - gl[I]).max() <= 1e-14 * np.abs(g[I]).max()
+    s.close()
+    sl.close()
