@@ -181,7 +181,18 @@ template <int DIR> struct FTile;
 template <> struct FTile<0> { static constexpr int TL = 8, TC = 32; };
 template <> struct FTile<1> { static constexpr int TL = 16, TC = 16; };
 template <> struct FTile<2> { static constexpr int TL = 16, TC = 16; };
-constexpr int FVM_THREADS = 256;
+// Threads and resident blocks per SM of a sweep: the characteristic form holds ~250
+// registers a thread, the component-wise one ~120. Small blocks let several blocks share an
+// SM, so one block's barrier waits overlap another's face work.
+#ifndef FVM_E_THREADS
+#define FVM_E_THREADS 64
+#define FVM_E_BLOCKS 4
+#define FVM_C_THREADS 128
+#define FVM_C_BLOCKS 2
+#endif
+template <bool EIGEN> struct FvmLaunch;
+template <> struct FvmLaunch<true> { static constexpr int NT = FVM_E_THREADS, MINB = FVM_E_BLOCKS; };
+template <> struct FvmLaunch<false> { static constexpr int NT = FVM_C_THREADS, MINB = FVM_C_BLOCKS; };
 
 template <int DIR> constexpr size_t fvm_smem_bytes() {
     constexpr int TL = FTile<DIR>::TL, TC = FTile<DIR>::TC, NP = TC + 8, NF = TC + 1;
@@ -189,10 +200,11 @@ template <int DIR> constexpr size_t fvm_smem_bytes() {
 }
 
 template <int DIR, bool EIGEN>
-__global__ void __launch_bounds__(FVM_THREADS) k_fvm_sweep(const SweepArgs a, const double* __restrict__ Ur,
+__global__ void __launch_bounds__(FvmLaunch<EIGEN>::NT, FvmLaunch<EIGEN>::MINB) k_fvm_sweep(const SweepArgs a, const double* __restrict__ Ur,
                                                            const double* __restrict__ gnx, const double* __restrict__ gny,
                                                            const double* __restrict__ gnz, const double* __restrict__ gar) {
     constexpr int TL = FTile<DIR>::TL, TC = FTile<DIR>::TC, NP = TC + 8, NF = TC + 1;
+    constexpr int FVM_THREADS = FvmLaunch<EIGEN>::NT;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -413,7 +425,7 @@ static cudaError_t fvm_launch_dir(const SweepArgs& a, const double* U, const dou
     else if (DIR == 1) grid = dim3(cdiv(P.nx, TL), cdiv(P.ny, TC), P.nz);
     else grid = dim3(cdiv(P.nx, TL), cdiv(P.nz, TC), P.ny);
     const double* const* g = geo + 4 * DIR;
-    k_fvm_sweep<DIR, EIGEN><<<grid, FVM_THREADS, fvm_smem_bytes<DIR>(), st>>>(a, U, g[0], g[1], g[2], g[3]);
+    k_fvm_sweep<DIR, EIGEN><<<grid, FvmLaunch<EIGEN>::NT, fvm_smem_bytes<DIR>(), st>>>(a, U, g[0], g[1], g[2], g[3]);
     return cudaGetLastError();
 }
 
