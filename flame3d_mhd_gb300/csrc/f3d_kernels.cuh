@@ -7,8 +7,6 @@
 
 namespace f3d {
 
-constexpr int SWEEP_THREADS = 256;
-
 enum OutMode { OUT_SET = 0, OUT_ADD = 1, OUT_RHS = 2, OUT_STAGE = 3, OUT_FACES = 4 };
 
 // Arguments of one sweep. The field pointers are typed by the sweep's arithmetic: double

@@ -19,15 +19,29 @@
 
 namespace f3d {
 
-template <int DIR> struct Tile;
-template <> struct Tile<0> { static constexpr int TL = 8, TC = 64; };
-template <> struct Tile<1> { static constexpr int TL = 16, TC = 32; };
-template <> struct Tile<2> { static constexpr int TL = 16, TC = 32; };
+// Tile (lines TL x cells TC), threads and resident blocks per SM of a sweep, by type. FP64:
+// 128 threads and half-height tiles, so four blocks (~40 KB of shared memory each) share an
+// SM and one block's barrier waits overlap the others' work (1.5-2% over 256-thread blocks
+// of twice the lines on the 256x64x64 shock tube and the viscous vortex; 64-thread blocks
+// of quarter tiles were 6-13% slower).
+#ifndef SW_D_THREADS
+#define SW_D_THREADS 128
+#define SW_D_BLOCKS 4
+#define SW_D_TL0 4
+#define SW_D_TL12 8
+#endif
+template <int DIR, class R> struct Tile;
+template <> struct Tile<0, float> { static constexpr int TL = 8, TC = 64, NT = 256, MINB = 3; };
+template <> struct Tile<1, float> { static constexpr int TL = 16, TC = 32, NT = 256, MINB = 3; };
+template <> struct Tile<2, float> { static constexpr int TL = 16, TC = 32, NT = 256, MINB = 3; };
+template <> struct Tile<0, double> { static constexpr int TL = SW_D_TL0, TC = 64, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
+template <> struct Tile<1, double> { static constexpr int TL = SW_D_TL12, TC = 32, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
+template <> struct Tile<2, double> { static constexpr int TL = SW_D_TL12, TC = 32, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
 
 template <int DIR, class R> constexpr size_t sweep_smem_bytes(bool hybrid) {
-    return sizeof(R) * ((size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 8) * (10 + (hybrid ? 1 : 0)) +
-                        (size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 1) * 5) +
-           sizeof(int) * (2 * (size_t)Tile<DIR>::TL * (Tile<DIR>::TC + 1) + 4);
+    using T = Tile<DIR, R>;
+    return sizeof(R) * ((size_t)T::TL * (T::TC + 8) * (10 + (hybrid ? 1 : 0)) + (size_t)T::TL * (T::TC + 1) * 5) +
+           sizeof(int) * (2 * (size_t)T::TL * (T::TC + 1) + 4);
 }
 
 // Face flux of one face from the split fluxes of the 8 cells around it, positions
@@ -164,8 +178,9 @@ template <> __device__ __forceinline__ float split_sound<float>(const DevParams&
 }
 
 template <int DIR, bool CHAR, class R>
-__global__ void __launch_bounds__(SWEEP_THREADS, (sizeof(R) == 4 ? 3 : 2)) k_sweep(const SweepArgs a) {
-    constexpr int TL = Tile<DIR>::TL, TC = Tile<DIR>::TC, NP = TC + 8, NF = TC + 1;
+__global__ void __launch_bounds__(Tile<DIR, R>::NT, Tile<DIR, R>::MINB) k_sweep(const SweepArgs a) {
+    constexpr int TL = Tile<DIR, R>::TL, TC = Tile<DIR, R>::TC, NP = TC + 8, NF = TC + 1;
+    constexpr int SWEEP_THREADS = Tile<DIR, R>::NT;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -311,14 +326,14 @@ cudaError_t sweep_configure() {
 }
 
 template <int DIR, bool CHAR, class R> static cudaError_t launch_dir(const SweepArgs& a, cudaStream_t st) {
-    constexpr int TL = Tile<DIR>::TL, TC = Tile<DIR>::TC;
+    constexpr int TL = Tile<DIR, R>::TL, TC = Tile<DIR, R>::TC;
     const DevParams& P = a.P;
     const size_t smem = sweep_smem_bytes<DIR, R>(true);
     dim3 grid;
     if (DIR == 0) grid = dim3(cdiv(P.nx, TC), cdiv(P.ny, TL), P.nz);
     else if (DIR == 1) grid = dim3(cdiv(P.nx, TL), cdiv(P.ny, TC), P.nz);
     else grid = dim3(cdiv(P.nx, TL), cdiv(P.nz, TC), P.ny);
-    k_sweep<DIR, CHAR, R><<<grid, SWEEP_THREADS, smem, st>>>(a);
+    k_sweep<DIR, CHAR, R><<<grid, Tile<DIR, R>::NT, smem, st>>>(a);
     return cudaGetLastError();
 }
 
