@@ -19,11 +19,12 @@
 
 namespace f3d {
 
-// Tile (lines TL x cells TC), threads and resident blocks per SM of a sweep, by type. FP64:
-// 128 threads and half-height tiles, so four blocks (~40 KB of shared memory each) share an
-// SM and one block's barrier waits overlap the others' work (1.5-2% over 256-thread blocks
-// of twice the lines on the 256x64x64 shock tube and the viscous vortex; 64-thread blocks
-// of quarter tiles were 6-13% slower).
+// Tile (lines TL x cells TC), threads and resident blocks per SM of a sweep, by type: 128
+// threads on tiles of 4 x 64 (xi) or 8 x 32 (eta, zeta), so several blocks share an SM and
+// one block's barrier waits overlap the others' work. FP64: four blocks (~40 KB of shared
+// memory each), 1.5-2% over 256-thread blocks of twice the lines on the 256x64x64 shock tube
+// and the viscous vortex (64-thread blocks of quarter tiles were 6-13% slower); FP32: six
+// blocks (~20 KB), 1.5-6% over three 256-thread blocks.
 #ifndef SW_D_THREADS
 #define SW_D_THREADS 128
 #define SW_D_BLOCKS 4
@@ -31,9 +32,15 @@ namespace f3d {
 #define SW_D_TL12 8
 #endif
 template <int DIR, class R> struct Tile;
-template <> struct Tile<0, float> { static constexpr int TL = 8, TC = 64, NT = 256, MINB = 3; };
-template <> struct Tile<1, float> { static constexpr int TL = 16, TC = 32, NT = 256, MINB = 3; };
-template <> struct Tile<2, float> { static constexpr int TL = 16, TC = 32, NT = 256, MINB = 3; };
+#ifndef SW_F_THREADS
+#define SW_F_THREADS 128
+#define SW_F_BLOCKS 6
+#define SW_F_TL0 4
+#define SW_F_TL12 8
+#endif
+template <> struct Tile<0, float> { static constexpr int TL = SW_F_TL0, TC = 64, NT = SW_F_THREADS, MINB = SW_F_BLOCKS; };
+template <> struct Tile<1, float> { static constexpr int TL = SW_F_TL12, TC = 32, NT = SW_F_THREADS, MINB = SW_F_BLOCKS; };
+template <> struct Tile<2, float> { static constexpr int TL = SW_F_TL12, TC = 32, NT = SW_F_THREADS, MINB = SW_F_BLOCKS; };
 template <> struct Tile<0, double> { static constexpr int TL = SW_D_TL0, TC = 64, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
 template <> struct Tile<1, double> { static constexpr int TL = SW_D_TL12, TC = 32, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
 template <> struct Tile<2, double> { static constexpr int TL = SW_D_TL12, TC = 32, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
