@@ -19,11 +19,22 @@
 namespace f3d {
 
 // Tile of TL lines x TC cells; NT threads cover the TL x (TC + 8) stencil positions of
-// phases A and C in whole rounds (one block per SM: about 160 registers a thread).
+// phases A and C in whole rounds. About 150 registers a thread: xi 4 x 64 on 96 threads,
+// four blocks per SM; eta / zeta 8 x 64 on 192 threads, two blocks per SM (97 KB of shared
+// memory each). Several blocks per SM overlap one block's barrier waits with the others'
+// work: 2.7% per step VJP over one block of 288 / 384 threads and twice the lines.
+#ifndef V_TL0
+#define V_TL0 4
+#define V_NT0 96
+#define V_MB0 4
+#define V_TL12 8
+#define V_NT12 192
+#define V_MB12 2
+#endif
 template <int DIR> struct VTile;
-template <> struct VTile<0> { static constexpr int TL = 4, TC = 64, NT = 288; };
-template <> struct VTile<1> { static constexpr int TL = 16, TC = 64, NT = 384; };
-template <> struct VTile<2> { static constexpr int TL = 16, TC = 64, NT = 384; };
+template <> struct VTile<0> { static constexpr int TL = V_TL0, TC = 64, NT = V_NT0, MINB = V_MB0; };
+template <> struct VTile<1> { static constexpr int TL = V_TL12, TC = 64, NT = V_NT12, MINB = V_MB12; };
+template <> struct VTile<2> { static constexpr int TL = V_TL12, TC = 64, NT = V_NT12, MINB = V_MB12; };
 
 template <int DIR> constexpr size_t vjp_smem_bytes() {
     return sizeof(double) * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 8) * 21 +
@@ -31,7 +42,7 @@ template <int DIR> constexpr size_t vjp_smem_bytes() {
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(VTile<DIR>::NT) k_sweep_vjp(const AdjArgs a) {
+__global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(const AdjArgs a) {
     constexpr int TL = VTile<DIR>::TL, TC = VTile<DIR>::TC, NP = TC + 8, NT = VTile<DIR>::NT;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;
