@@ -914,7 +914,9 @@ int f3d_profile_step(f3d_ctx* ctx, double dt, double* U, double* Un, double* Q, 
     for (int i = 0; i < Prof::kMax; i++) F3D_CUDA(ctx, cudaEventCreate(&prof.ev[i]));
     ctx->prof = &prof;
     mark(ctx, -1, st);
-    for (int s = 1; s <= 3 && !rc; s++) rc = run_stage(ctx, s, dt, U, Un, Q, st);
+    // as inside f3d_rk3_steps, the mixed form's FP32 copy of Q is made before the first stage
+    // only: every stage's primitive fill rewrites it
+    for (int s = 1; s <= 3 && !rc; s++) rc = run_stage(ctx, s, dt, U, Un, Q, st, mixed(ctx) && s > 1);
     ctx->prof = nullptr;
     cudaError_t e = cudaStreamSynchronize(st);
     for (int k = 0; k < K_NKIND; k++) {
