@@ -134,6 +134,7 @@ struct Prof {
     static constexpr int kMax = 64;
     cudaEvent_t ev[kMax];
     int kind[kMax];
+    int nl[kMax];  // kernels launched since the previous mark
     int n = 0;
 };
 
@@ -186,14 +187,16 @@ struct f3d_ctx {
 
 namespace {
 
-enum KernelKind { K_SOUND = 0, K_SENSOR, K_VISCOUS, K_SWEEP_X, K_SWEEP_Y, K_SWEEP_Z, K_PRIM_FILL, K_NKIND };
+enum KernelKind { K_SOUND = 0, K_SENSOR, K_VISCOUS, K_SWEEP_X, K_SWEEP_Y, K_SWEEP_Z, K_PRIM_FILL, K_STAGE_UPDATE,
+                  K_NKIND };
 const char* kKernelNames[K_NKIND] = {"sound_speed", "shock_sensor", "viscous_flux", "sweep_xi",
-                                     "sweep_eta", "sweep_zeta", "prim_ghost_fill"};
+                                     "sweep_eta", "sweep_zeta", "prim_ghost_fill", "stage_update"};
 
-void mark(f3d_ctx* ctx, int kind, cudaStream_t st) {
+void mark(f3d_ctx* ctx, int kind, cudaStream_t st, int launches = 1) {
     Prof* p = ctx->prof;
     if (p && p->n < Prof::kMax) {
         cudaEventRecord(p->ev[p->n], st);
+        p->nl[p->n] = launches;
         p->kind[p->n++] = kind;
     }
 }
@@ -306,9 +309,11 @@ int run_rhs_fvm(f3d_ctx* ctx, const double* Q, double* acc, const SweepArgs& las
         F3D_CUDA(ctx, launch_fvm_sweep(d, eigen, a, U, ctx->geo, st));
         mark(ctx, K_SWEEP_X + d, st);
     }
-    if (stage)
+    if (stage) {
         F3D_CUDA(ctx, launch_stage_update(P, acc, ctx->J, last.dt, last.U, last.Un, last.stage1_copy, last.combine,
                                           last.ca, last.cb, st, last.dtl));
+        mark(ctx, K_STAGE_UPDATE, st);
+    }
     return F3D_OK;
 }
 
@@ -386,7 +391,7 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
     int rc = run_rhs(ctx, Q, ctx->acc, last, st, q32_current);
     if (rc) return rc;
     F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 0, st, mixed(ctx) ? ctx->Q32 : nullptr));
-    mark(ctx, K_PRIM_FILL, st);
+    mark(ctx, K_PRIM_FILL, st, 2);  // interior and ghost passes
     return F3D_OK;
 }
 
@@ -928,7 +933,7 @@ int f3d_profile_step(f3d_ctx* ctx, double dt, double* U, double* Un, double* Q, 
             float ms = 0.f;
             cudaEventElapsedTime(&ms, prof.ev[i - 1], prof.ev[i]);
             ms_out[prof.kind[i]] += ms;
-            launches_out[prof.kind[i]] += 1;
+            launches_out[prof.kind[i]] += prof.nl[i];
         }
     }
     for (int i = 0; i < Prof::kMax; i++) cudaEventDestroy(prof.ev[i]);

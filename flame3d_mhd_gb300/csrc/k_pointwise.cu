@@ -25,59 +25,65 @@ __device__ __forceinline__ double sound_speed(const DevParams& P, const double q
     return P.split == F3D_SPLIT_SW ? sqrt(__dmul_rn(P.grg, q[5])) : sqrt(__dmul_rn(P.gamma, q[4]) / q[0]);
 }
 
-// c2Prim at interior cells and the composed ghost rules everywhere else, in one pass.
-// A ghost cell recomputes c2Prim at its interior source cell, which is bitwise what
-// c2Prim followed by the reference's copies produces.
-__global__ void k_prim_fill(const DevParams P, const double* U, double* Q, double* Ug, double* csnd, float* Q32,
-                            int from_q) {
+// c2Prim at interior cells (k_prim_interior), then the composed ghost rules (k_prim_ghost):
+// a ghost cell reads the FP64 primitive state its chain starts from, which the first pass
+// has just written — bitwise what c2Prim followed by the reference's copies produces —
+// instead of recomputing c2Prim there (a quarter of the cells of a 256x64x64 grid are
+// ghosts). from_q: Q's interior is given (fillGhost); the first pass then only derives the
+// sound speed and the FP32 copy when they are asked for.
+__global__ void k_prim_interior(const DevParams P, const double* U, double* Q, double* csnd, float* Q32,
+                                int from_q) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)P.nx * P.ny * P.nz) return;
+    int i, j, k;
+    split3(t, P.dnx, P.dny, i, j, k);
+    const long long c = lin3(P, i + NG, j + NG, k + NG), pl = P.plane;
+    double q[6];
+    if (from_q) {
+#pragma unroll
+        for (int n = 0; n < 6; n++) q[n] = Q[c + n * pl];
+    } else {
+        double u[5];
+#pragma unroll
+        for (int n = 0; n < 5; n++) u[n] = U[c + n * pl];
+        if (Q32) c2prim_cell_fast(P, u, q);  // mixed precision
+        else c2prim_cell(P, u, q);
+#pragma unroll
+        for (int n = 0; n < 6; n++) Q[c + n * pl] = q[n];
+    }
+    if (csnd) csnd[c] = sound_speed(P, q);
+    if (Q32) {
+#pragma unroll
+        for (int n = 0; n < 6; n++) Q32[c + n * pl] = f64_to_f32_rn(q[n]);
+    }
+}
+
+__global__ void k_prim_ghost(const DevParams P, const double* U, double* Q, double* Ug, double* csnd, float* Q32) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
     const long long pl = P.plane;
     int i, j, k;
     cell_ijk(P, c, i, j, k);
+    if (is_interior(P, i, j, k)) return;
     double q[6];
-    if (is_interior(P, i, j, k)) {
-        if (from_q) {
-            if (!csnd && !Q32) return;
+    const GhostChain ch = resolve_ghost(P, i, j, k);
+    const long long s = lin3(P, ch.si, ch.sj, ch.sk);
+    if (ch.dirichlet < 0) {
 #pragma unroll
-            for (int n = 0; n < 6; n++) q[n] = Q[c + n * pl];
-        } else {
+        for (int n = 0; n < 6; n++) q[n] = Q[s + n * pl];
+    }
+    apply_chain(P, ch, q);
+#pragma unroll
+    for (int n = 0; n < 6; n++) Q[c + n * pl] = q[n];
+    if (Ug) {
+        if (ch.nontrivial) {
             double u[5];
+            prim2c_cell(P, q, u);
 #pragma unroll
-            for (int n = 0; n < 5; n++) u[n] = U[c + n * pl];
-            if (Q32) c2prim_cell_fast(P, u, q);  // mixed precision
-            else c2prim_cell(P, u, q);
+            for (int n = 0; n < 5; n++) Ug[c + n * pl] = u[n];
+        } else {
 #pragma unroll
-            for (int n = 0; n < 6; n++) Q[c + n * pl] = q[n];
-        }
-    } else {
-        const GhostChain ch = resolve_ghost(P, i, j, k);
-        const long long s = lin3(P, ch.si, ch.sj, ch.sk);
-        if (ch.dirichlet < 0) {
-            if (from_q) {
-#pragma unroll
-                for (int n = 0; n < 6; n++) q[n] = Q[s + n * pl];
-            } else {
-                double u[5];
-#pragma unroll
-                for (int n = 0; n < 5; n++) u[n] = U[s + n * pl];
-                if (Q32) c2prim_cell_fast(P, u, q);
-                else c2prim_cell(P, u, q);
-            }
-        }
-        apply_chain(P, ch, q);
-#pragma unroll
-        for (int n = 0; n < 6; n++) Q[c + n * pl] = q[n];
-        if (Ug) {
-            if (ch.nontrivial) {
-                double u[5];
-                prim2c_cell(P, q, u);
-#pragma unroll
-                for (int n = 0; n < 5; n++) Ug[c + n * pl] = u[n];
-            } else {
-#pragma unroll
-                for (int n = 0; n < 5; n++) Ug[c + n * pl] = U[s + n * pl];
-            }
+            for (int n = 0; n < 5; n++) Ug[c + n * pl] = U[s + n * pl];
         }
     }
     if (csnd) csnd[c] = sound_speed(P, q);
@@ -89,7 +95,9 @@ __global__ void k_prim_fill(const DevParams P, const double* U, double* Q, doubl
 
 cudaError_t launch_prim_fill(const DevParams& P, const double* U, double* Q, double* Ug, double* csnd, int from_q,
                              cudaStream_t st, float* Q32) {
-    k_prim_fill<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, U, Q, Ug, csnd, Q32, from_q);
+    const long long ni = (long long)P.nx * P.ny * P.nz;
+    if (!from_q || csnd || Q32) k_prim_interior<<<pw_blocks(ni), PW_THREADS, 0, st>>>(P, U, Q, csnd, Q32, from_q);
+    k_prim_ghost<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, U, Q, Ug, csnd, Q32);
     return cudaGetLastError();
 }
 

@@ -19,17 +19,18 @@
 
 namespace f3d {
 
-// Tile (lines TL x cells TC), threads and resident blocks per SM of a sweep, by type: 128
-// threads on tiles of 4 x 64 (xi) or 8 x 32 (eta, zeta), so several blocks share an SM and
-// one block's barrier waits overlap the others' work. FP64: four blocks (~40 KB of shared
-// memory each), 1.5-2% over 256-thread blocks of twice the lines on the 256x64x64 shock tube
-// and the viscous vortex (64-thread blocks of quarter tiles were 6-13% slower); FP32: six
-// blocks (~20 KB), 1.5-6% over three 256-thread blocks.
+// Tile (lines TL x cells TC), threads and resident blocks per SM of a sweep, by type.
+// FP64: 8 x 64 (xi) and 16 x 32 (eta, zeta) on 256 threads, two blocks per SM (~75 KB of
+// shared memory each); half-height tiles on 128 threads, four per SM, timed 3% slower per
+// RK3 step on the 256x64x64 shock tube (quarter tiles on 64 threads slower still). FP32:
+// half-height tiles on 128 threads, six blocks per SM (~20 KB each): the same step time as
+// three 256-thread blocks on that tube, 6% less per RHS on the component-wise tube and on
+// the viscous vortex.
 #ifndef SW_D_THREADS
-#define SW_D_THREADS 128
-#define SW_D_BLOCKS 4
-#define SW_D_TL0 4
-#define SW_D_TL12 8
+#define SW_D_THREADS 256
+#define SW_D_BLOCKS 2
+#define SW_D_TL0 8
+#define SW_D_TL12 16
 #endif
 template <int DIR, class R> struct Tile;
 #ifndef SW_F_THREADS
