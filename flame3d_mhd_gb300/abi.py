@@ -21,7 +21,7 @@ NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 
 SPLIT_SW, SPLIT_LF, SPLIT_VL, SPLIT_AUSM = 0, 1, 2, 3
 SPLIT_NAMES = {"SW": SPLIT_SW, "LF": SPLIT_LF, "VL": SPLIT_VL, "AUSM": SPLIT_AUSM}
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_REF32 = 0, 1, 2
 SCHEME_FDM, SCHEME_FVM_EIGEN, SCHEME_FVM_CONS = 0, 1, 2
 FILTER_NONE, FILTER_LINEAR, FILTER_NONLINEAR = 0, 1, 2
 LES_NONE, LES_SMAGORINSKY, LES_WALE = 0, 1, 2
@@ -136,6 +136,13 @@ def load() -> C.CDLL:
         "f3d_debug_round_f32": (ip, [vp, vp, C.c_longlong, vp]),
         "f3d_set_inflow_profile_cotangent": (ip, [vp, ip, vp, vp]),
         "f3d_rk3_step_vjp_stages": (ip, [vp, C.c_double, vp, vp, vp, vp, vp, vp]),
+        "f3d_set_metrics_f32": (ip, [vp, vp * 9, vp, vp]),
+        "f3d_c2prim_f32": (ip, [vp, vp, vp, vp]),
+        "f3d_prim2c_f32": (ip, [vp, vp, vp, vp]),
+        "f3d_fill_ghosts_f32": (ip, [vp, vp, vp, vp]),
+        "f3d_rhs_f32": (ip, [vp, vp, vp, vp]),
+        "f3d_rk3_stage_f32": (ip, [vp, ip, C.c_float, vp, vp, vp, vp]),
+        "f3d_rk3_steps_f32": (ip, [vp, ip, C.c_float, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -153,7 +160,9 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_debug_viscous", "f3d_div", "f3d_measure_pipes", "f3d_kernel_count", "f3d_kernel_name",
             "f3d_profile_step", "f3d_rhs_noalloc", "f3d_rhs_vjp", "f3d_rk3_step_vjp", "f3d_set_inflow_profile",
             "f3d_set_coordinates", "f3d_filter", "f3d_local_dt", "f3d_debug_round_f32",
-            "f3d_set_inflow_profile_cotangent", "f3d_rk3_step_vjp_stages"]
+            "f3d_set_inflow_profile_cotangent", "f3d_rk3_step_vjp_stages", "f3d_set_metrics_f32",
+            "f3d_c2prim_f32", "f3d_prim2c_f32", "f3d_fill_ghosts_f32", "f3d_rhs_f32", "f3d_rk3_stage_f32",
+            "f3d_rk3_steps_f32"]
 
 
 class F3DError(RuntimeError):

@@ -41,7 +41,11 @@ int validate_params(const f3d_params& p, std::string& why) {
     if (p.split_method < 0 || p.split_method > 3) { why = "unknown split_method"; return F3D_ERR_ARG; }
     if (p.character != 0 && p.character != 1) { why = "character must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
-    if (p.precision != F3D_PREC_FP64 && p.precision != F3D_PREC_MIXED) { why = "unknown precision"; return F3D_ERR_ARG; }
+    if (p.precision < F3D_PREC_FP64 || p.precision > F3D_PREC_REF32) { why = "unknown precision"; return F3D_ERR_ARG; }
+    if (p.precision == F3D_PREC_REF32 && (p.lts || p.filter || p.les)) {
+        why = "the Float32 reference form has no local time stepping, filters or LES";
+        return F3D_ERR_UNSUPPORTED;
+    }
     if (p.scheme < F3D_SCHEME_FDM || p.scheme > F3D_SCHEME_FVM_CONS) { why = "unknown scheme"; return F3D_ERR_ARG; }
     if (p.lts != 0 && p.lts != 1) { why = "lts must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.adjoint_lean != 0 && p.adjoint_lean != 1) { why = "adjoint_lean must be 0 or 1"; return F3D_ERR_ARG; }
@@ -57,6 +61,10 @@ int validate_params(const f3d_params& p, std::string& why) {
     for (int d = 0; d < 3; d++) {
         const f3d_bc &lo = p.bc[2 * d], &hi = p.bc[2 * d + 1];
         for (const f3d_bc* b : {&lo, &hi}) {
+            if (b->kind == F3D_BC_INFLOW_PROFILE && p.precision == F3D_PREC_REF32) {
+                why = "inflow-profile faces take FP64 profiles; the Float32 reference form has none";
+                return F3D_ERR_UNSUPPORTED;
+            }
             if (b->kind < 0 || b->kind > 5) { why = "unknown boundary kind"; return F3D_ERR_ARG; }
             if (b->kind == F3D_BC_DIRICHLET && !(b->rho > 0.0 && b->p > 0.0)) {
                 why = "Dirichlet state needs rho > 0 and p > 0"; return F3D_ERR_ARG;
@@ -117,6 +125,22 @@ DevParams make_dev_params(const f3d_params& p) {
     };
     fill(d.cd);
     fill(d.cf);
+    d.ref32 = p.precision == F3D_PREC_REF32;
+    d.g32 = (float)p.gamma;
+    d.rg32 = (float)p.rg;
+    d.gm1_32 = d.g32 - 1.0f;
+    d.eps32 = (float)d.eps_clamp;
+    if (d.ref32) {  // the reference's Float32 constants, derived in Float32 as its code does
+        Cst<float>& c = d.cf;
+        const float g = d.g32, rg = d.rg32, gm1 = d.gm1_32;
+        c.gamma = g; c.rg = rg; c.gm1 = gm1; c.grg = g * rg;
+        c.inv_gm1 = 1.0f / gm1; c.inv_2g = 1.0f / (2.0f * g); c.two_gm1 = 2.0f * gm1;
+        c.w2c = (3.0f - g) / (2.0f * gm1);
+        c.cp = p.cp != 0.0 ? (float)p.cp : rg * g / gm1;
+        c.cp_pr = c.cp / c.pr;
+        const float lp = (float)p.linear_phi;
+        for (int m = 0; m < 7; m++) c.lin[m] = (float)up7[m] * lp + (float)cd6[m] * (1.0f - lp);
+    }
     for (int f = 0; f < 6; f++) {
         const f3d_bc& b = p.bc[f];
         d.bc[f].kind = b.kind;
@@ -226,9 +250,15 @@ int check_ptrs(f3d_ctx* ctx, std::initializer_list<const void*> ps) {
     return F3D_OK;
 }
 
-// need_state: a compute call (metrics set, and every inflow-profile face has its profile)
-int check_ctx(f3d_ctx* ctx, bool need_state) {
+// need_state: a compute call (metrics set, and every inflow-profile face has its profile).
+// The FP64-array entries refuse an F3D_PREC_REF32 context (its arrays are Float32: the
+// *_f32 entries), and those refuse the other contexts (check_ctx32).
+int check_ctx(f3d_ctx* ctx, bool need_state, bool f32_entry = false) {
     if (!ctx) return F3D_ERR_ARG;
+    if (ctx->dp.ref32 && !f32_entry)
+        return fail(ctx, F3D_ERR_ARG, "an F3D_PREC_REF32 context takes Float32 arrays: use the _f32 entries");
+    if (!ctx->dp.ref32 && f32_entry)
+        return fail(ctx, F3D_ERR_ARG, "the _f32 entries need an F3D_PREC_REF32 context");
     if (need_state && !ctx->metrics_set) return fail(ctx, F3D_ERR_STATE, "metrics not set (call f3d_set_metrics)");
     if (need_state && ctx->params.scheme != F3D_SCHEME_FDM && !ctx->coords_set)
         return fail(ctx, F3D_ERR_STATE, "coordinates not set (call f3d_set_coordinates)");
@@ -240,6 +270,7 @@ int check_ctx(f3d_ctx* ctx, bool need_state) {
 }
 
 bool mixed(const f3d_ctx* ctx) { return ctx->dp.precision == F3D_PREC_MIXED; }
+int check_ctx32(f3d_ctx* ctx, bool need_state) { return check_ctx(ctx, need_state, true); }
 
 // Forget the captured RK3 step: its kernels hold pointers and parameters by value.
 void drop_step_graph(f3d_ctx* ctx) {
@@ -247,14 +278,15 @@ void drop_step_graph(f3d_ctx* ctx) {
     ctx->step_graph = nullptr;
 }
 
-SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const double* phi_override = nullptr) {
+SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const double* phi_override = nullptr,
+                     const float* Q32 = nullptr) {
     SweepArgs a;
     std::memset(&a, 0, sizeof(a));
     a.P = ctx->dp;
     a.J = ctx->J;
-    if (mixed(ctx)) {
+    if (mixed(ctx) || ctx->dp.ref32) {
         a.fp32 = 1;
-        a.Q = ctx->Q32;
+        a.Q = ctx->dp.ref32 ? Q32 : ctx->Q32;
         for (int n = 0; n < 3; n++) {
             a.A[n] = ctx->m32.A[3 * dir + n];
             a.Ah[n] = ctx->m32.H[3 * dir + n];
@@ -511,6 +543,62 @@ int rhs_vjp_prepared(f3d_ctx* ctx, const double* U, const double* Q, const doubl
     return F3D_OK;
 }
 
+// ---- F3D_PREC_REF32: the reference's Float32 form on the caller's Float32 arrays ----------
+// Sensor, viscous fluxes and the three FP32 sweeps from the Float32 Q; the last sweep
+// writes the Float32 RHS (OUT_RHS) or applies the Float32 RK update (OUT_STAGE).
+int run_rhs32(f3d_ctx* ctx, const float* Q, const SweepArgs& last, cudaStream_t st) {
+    const DevParams& P = ctx->dp;
+    const bool hybrid = P.fixed_branch < 0;
+    if (hybrid) {
+        F3D_CUDA(ctx, launch_sensor32(P, Q, ctx->phi32, st));
+        mark(ctx, K_SENSOR, st);
+    }
+    if (ctx->params.viscous) {
+        const float* m32[9];
+        for (int n = 0; n < 9; n++) m32[n] = ctx->m32.A[n];
+        F3D_CUDA(ctx, launch_viscous32(P, Q, m32, ctx->m32.J, ctx->Fv32[0], ctx->Fv32[1], ctx->Fv32[2], st));
+        mark(ctx, K_VISCOUS, st);
+    }
+    for (int d = 0; d < 3; d++) {
+        SweepArgs a = sweep_args(ctx, d, nullptr, hybrid, nullptr, Q);
+        a.acc = ctx->acc32;
+        a.out_mode = d == 0 ? OUT_SET : (d == 1 ? OUT_ADD : last.out_mode);
+        if (d == 2) {
+            a.J32 = ctx->m32.J;
+            a.out32 = last.out32;
+            a.U32 = last.U32;
+            a.Un32 = last.Un32;
+            a.dt32 = last.dt32;
+            a.ca32 = last.ca32;
+            a.cb32 = last.cb32;
+            a.combine = last.combine;
+            a.stage1_copy = last.stage1_copy;
+        }
+        F3D_CUDA(ctx, launch_sweep(d, a, st));
+        mark(ctx, K_SWEEP_X + d, st);
+    }
+    return F3D_OK;
+}
+
+// solver.jl:416-444 in Float32: U += dt J L, linComb, c2Prim, ghost fill
+int run_stage32(f3d_ctx* ctx, int stage, float dt, float* U, float* Un, float* Q, cudaStream_t st) {
+    SweepArgs last;
+    std::memset(&last, 0, sizeof(last));
+    last.out_mode = OUT_STAGE;
+    last.U32 = U;
+    last.Un32 = Un;
+    last.dt32 = dt;
+    last.stage1_copy = stage == 1;
+    last.combine = stage != 1;
+    last.ca32 = stage == 2 ? 0.25f : 2.0f / 3.0f;  // the Float32 weights of utils.jl:57-70
+    last.cb32 = stage == 2 ? 0.75f : 1.0f / 3.0f;
+    int rc = run_rhs32(ctx, Q, last, st);
+    if (rc) return rc;
+    F3D_CUDA(ctx, launch_prim_fill32(ctx->dp, U, Q, U, 0, st));
+    mark(ctx, K_PRIM_FILL, st, 2);
+    return F3D_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -570,13 +658,14 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     const size_t nc = (size_t)ctx->dp.plane;
     const size_t nv = (size_t)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const bool mx = p->precision == F3D_PREC_MIXED;
+    const bool mx = p->precision != F3D_PREC_FP64;  // FP32 sweeps: the mixed and reference forms
+    const bool r32 = p->precision == F3D_PREC_REF32;
     size_t total = 256;
     const bool fvm = p->scheme != F3D_SCHEME_FDM;
     if (!mx) {  // S(3) + A/|A|(9) + sound speed + phi + acc(5) [+ viscous 12] [+ FVM 12 + 5]
         total += up(nc * 8) * (3 + 9 + 1 + 1 + 5 + (fvm ? 17 : 0)) + (p->viscous ? 3 * up(nv * 4 * 8) : 0);
-    } else {    // Q32(6) + A32(9) + H32(9) + S32(3) + J32 + phi32 + acc32(5) [+ viscous 12]
-        total += up(nc * 4) * (6 + 9 + 9 + 3 + 1 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 4) : 0);
+    } else {    // [Q32(6) + A32(9) + J32, mixed only] + H32(9) + S32(3) + phi32 + acc32(5) [+ viscous 12]
+        total += up(nc * 4) * ((r32 ? 0 : 16) + 9 + 3 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 4) : 0);
     }
     cudaError_t e = cudaMalloc(&ctx->slab, total);
     if (e != cudaSuccess) {
@@ -604,11 +693,13 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
         phi_bytes = b1;
     } else {
         const size_t b1 = up(nc * 4);
-        ctx->Q32 = (float*)q; q += 6 * b1;
-        for (int n = 0; n < 9; n++) { ctx->m32.A[n] = (float*)q; q += b1; }
+        if (!r32) {  // the reference form reads the caller's Float32 Q, metrics and J
+            ctx->Q32 = (float*)q; q += 6 * b1;
+            for (int n = 0; n < 9; n++) { ctx->m32.A[n] = (float*)q; q += b1; }
+            ctx->m32.J = (float*)q; q += b1;
+        }
         for (int n = 0; n < 9; n++) { ctx->m32.H[n] = (float*)q; q += b1; }
         for (int d = 0; d < 3; d++) { ctx->m32.S[d] = (float*)q; q += b1; }
-        ctx->m32.J = (float*)q; q += b1;
         ctx->phi32 = (float*)q; q += b1;
         ctx->acc32 = (float*)q; q += 5 * b1;
         if (p->viscous)
@@ -777,6 +868,93 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
         F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
         if ((rc = after_step())) return rc;
     }
+    return F3D_OK;
+}
+
+// ---- F3D_PREC_REF32 entries (Float32 arrays) ---------------------------------------------
+int f3d_set_metrics_f32(f3d_ctx* ctx, const float* const metrics[9], const float* jac, f3d_stream stream) {
+    int rc = check_ctx32(ctx, false);
+    if (rc) return rc;
+    if (!metrics) return fail(ctx, F3D_ERR_ARG, "null metrics array");
+    if ((rc = check_ptrs(ctx, {metrics[0], metrics[1], metrics[2], metrics[3], metrics[4], metrics[5], metrics[6],
+                              metrics[7], metrics[8], jac})))
+        return rc;
+    for (int n = 0; n < 9; n++) ctx->m32.A[n] = const_cast<float*>(metrics[n]);  // read only
+    ctx->m32.J = const_cast<float*>(jac);
+    drop_step_graph(ctx);
+    F3D_CUDA(ctx, launch_metric_prep_ref32(ctx->dp, ctx->m32, (cudaStream_t)stream));
+    ctx->metrics_set = true;
+    return F3D_OK;
+}
+
+int f3d_c2prim_f32(f3d_ctx* ctx, const float* U, float* Q, f3d_stream stream) {
+    int rc = check_ctx32(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;
+    F3D_CUDA(ctx, launch_prim_fill32(ctx->dp, U, Q, nullptr, 2, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_prim2c_f32(f3d_ctx* ctx, const float* Q, float* U, f3d_stream stream) {
+    int rc = check_ctx32(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;
+    F3D_CUDA(ctx, launch_prim2c32(ctx->dp, Q, U, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_fill_ghosts_f32(f3d_ctx* ctx, float* Q, float* U, f3d_stream stream) {
+    int rc = check_ctx32(ctx, false);
+    if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;
+    F3D_CUDA(ctx, launch_prim_fill32(ctx->dp, U, Q, U, 1, (cudaStream_t)stream));
+    return F3D_OK;
+}
+
+int f3d_rhs_f32(f3d_ctx* ctx, const float* Q, float* dUdt, f3d_stream stream) {
+    int rc = check_ctx32(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {Q, dUdt}))) return rc;
+    SweepArgs last;
+    std::memset(&last, 0, sizeof(last));
+    last.out_mode = OUT_RHS;
+    last.out32 = dUdt;
+    return run_rhs32(ctx, Q, last, (cudaStream_t)stream);
+}
+
+int f3d_rk3_stage_f32(f3d_ctx* ctx, int stage, float dt, float* U, float* Un, float* Q, f3d_stream stream) {
+    int rc = check_ctx32(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
+    if (stage < 1 || stage > 3) return fail(ctx, F3D_ERR_ARG, "stage must be 1, 2 or 3");
+    return run_stage32(ctx, stage, dt, U, Un, Q, (cudaStream_t)stream);
+}
+
+int f3d_rk3_steps_f32(f3d_ctx* ctx, int nsteps, float dt, float* U, float* Un, float* Q, f3d_stream stream) {
+    int rc = check_ctx32(ctx, true);
+    if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
+    if (nsteps < 0) return fail(ctx, F3D_ERR_ARG, "nsteps must be >= 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (st == nullptr) {  // the legacy stream cannot be captured
+        for (int t = 0; t < nsteps; t++)
+            for (int s = 1; s <= 3; s++)
+                if ((rc = run_stage32(ctx, s, dt, U, Un, Q, st))) return rc;
+        return F3D_OK;
+    }
+    const void* key[4] = {U, Un, Q, st};
+    bool hit = ctx->step_graph && ctx->g_dt == (double)dt;
+    for (int n = 0; n < 4 && hit; n++) hit = ctx->g_key[n] == key[n];
+    if (!hit) {
+        drop_step_graph(ctx);
+        cudaGraph_t g;
+        F3D_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int src = F3D_OK;
+        for (int s = 1; s <= 3 && !src; s++) src = run_stage32(ctx, s, dt, U, Un, Q, st);
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (src) return src;
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&ctx->step_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaGraphInstantiate");
+        for (int n = 0; n < 4; n++) ctx->g_key[n] = key[n];
+        ctx->g_dt = (double)dt;
+    }
+    for (int t = 0; t < nsteps; t++) F3D_CUDA(ctx, cudaGraphLaunch(ctx->step_graph, st));
     return F3D_OK;
 }
 

@@ -69,7 +69,9 @@ struct DevParams {
     double phi1, phi2, phi3;
     double lin[7];       // run.jl:75-77
     int split, character, viscous;
-    int precision;       // F3D_PREC_FP64 or F3D_PREC_MIXED
+    int precision;       // F3D_PREC_*
+    int ref32;           // F3D_PREC_REF32: Float32 arrays and the reference's Float32 arithmetic
+    float g32, rg32, gm1_32, eps32;  // its Float32 constants: gamma, Rg, gamma - 1, the clamp
     int fixed_branch;    // -1: per-face hybrid switch; 0..3: every face takes that branch
     // FP64 sensor thresholds as bit patterns: for phi >= 0 (or NaN) the comparison
     // phi < t of the reference equals bits(phi) < phib (thresholds <= 0 or NaN map to 0,

@@ -181,6 +181,53 @@ template <class R> __device__ __forceinline__ R weno5(R V1, R V2, R V3, R V4, R 
 }
 
 // WENO7 of one side, schemes.jl:153-185: 12x the reconstructed value.
+template <class R>
+__device__ __forceinline__ void weno7_parts(R V1, R V2, R V3, R V4, R V5, R V6, R V7, R q[4], R Is[4]) {
+    q[0] = R(-3) * V1 + R(13) * V2 - R(23) * V3 + R(25) * V4;
+    q[1] = V2 - R(5) * V3 + R(13) * V4 + R(3) * V5;
+    q[2] = -V3 + R(7) * V4 + R(7) * V5 - V6;
+    q[3] = R(3) * V4 + R(13) * V5 - R(5) * V6 + V7;
+    Is[0] = V1 * (R(547) * V1 - R(3882) * V2 + R(4642) * V3 - R(1854) * V4) +
+            V2 * (R(7043) * V2 - R(17246) * V3 + R(7042) * V4) + V3 * (R(11003) * V3 - R(9402) * V4) +
+            V4 * (R(2107) * V4);
+    Is[1] = V2 * (R(267) * V2 - R(1642) * V3 + R(1602) * V4 - R(494) * V5) +
+            V3 * (R(2843) * V3 - R(5966) * V4 + R(1922) * V5) + V4 * (R(3443) * V4 - R(2522) * V5) +
+            V5 * (R(547) * V5);
+    Is[2] = V3 * (R(547) * V3 - R(2522) * V4 + R(1922) * V5 - R(494) * V6) +
+            V4 * (R(3443) * V4 - R(5966) * V5 + R(1602) * V6) + V5 * (R(2843) * V5 - R(1642) * V6) +
+            V6 * (R(267) * V6);
+    Is[3] = V4 * (R(2107) * V4 - R(9402) * V5 + R(7042) * V6 - R(1854) * V7) +
+            V5 * (R(11003) * V5 - R(17246) * V6 + R(4642) * V7) + V6 * (R(7043) * V6 - R(3882) * V7) +
+            V7 * (R(547) * V7);
+}
+
+// The reference's own Float32 forms (F3D_PREC_REF32). WENO7: smoothness indicators and
+// stencil values in Float32, the alphas d_k / (1e-20 + IS_k s0)^2 and their normalised
+// combination in FP64 (schemes.jl:178-185 promotes them); returns 12x the value in FP64.
+__device__ __forceinline__ double weno7_ref32(float V1, float V2, float V3, float V4, float V5, float V6, float V7,
+                                              float s0) {
+    float q[4], Is[4];
+    weno7_parts<float>(V1, V2, V3, V4, V5, V6, V7, q, Is);
+    const double e1 = 1e-20;
+    const double a1 = 1.0 / sq(e1 + (double)(Is[0] * s0)), a2 = 12.0 / sq(e1 + (double)(Is[1] * s0));
+    const double a3 = 18.0 / sq(e1 + (double)(Is[2] * s0)), a4 = 4.0 / sq(e1 + (double)(Is[3] * s0));
+    const double invsum = 1.0 / (a1 + a2 + a3 + a4);
+    return invsum * (a1 * (double)q[0] + a2 * (double)q[1] + a3 * (double)q[2] + a4 * (double)q[3]);
+}
+// WENO5 in Float32 with one division per alpha and one for their sum (schemes.jl:233-252).
+__device__ __forceinline__ float weno5_ref32(float V1, float V2, float V3, float V4, float V5, float s0) {
+    float s11 = 13.f * sq(V1 - 2.f * V2 + V3) + 3.f * sq(V1 - 4.f * V2 + 3.f * V3);
+    float s22 = 13.f * sq(V2 - 2.f * V3 + V4) + 3.f * sq(V2 - V4);
+    float s33 = 13.f * sq(V3 - 2.f * V4 + V5) + 3.f * sq(3.f * V3 - 4.f * V4 + V5);
+    const float e2 = 1e-16f;
+    s11 = 1.f / sq(e2 + s11 * s0);
+    s22 = 6.f / sq(e2 + s22 * s0);
+    s33 = 3.f / sq(e2 + s33 * s0);
+    const float invsum = 1.f / (s11 + s22 + s33);
+    const float v1 = 2.f * V1 - 7.f * V2 + 11.f * V3, v2 = -V2 + 5.f * V3 + 2.f * V4, v3 = 2.f * V3 + 5.f * V4 - V5;
+    return invsum * (s11 * v1 + s22 * v2 + s33 * v3);
+}
+
 template <class R> __device__ __forceinline__ R weno7(R V1, R V2, R V3, R V4, R V5, R V6, R V7, R s0) {
     R q1 = R(-3) * V1 + R(13) * V2 - R(23) * V3 + R(25) * V4;
     R q2 = V2 - R(5) * V3 + R(13) * V4 + R(3) * V5;

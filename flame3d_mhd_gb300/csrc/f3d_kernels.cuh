@@ -33,6 +33,12 @@ struct SweepArgs {
     int combine;
     int stage1_copy;      // OUT_STAGE of stage 1: Un = U before the update
     int fp32;             // 1: the mixed-precision (FP32) sweep
+    // F3D_PREC_REF32 (the FP32 sweep on the caller's Float32 arrays): Float32 outputs
+    const float* J32;     // Jacobian
+    float* out32;         // OUT_RHS destination
+    float* U32;           // OUT_STAGE state
+    float* Un32;          // OUT_STAGE stage-start copy
+    float dt32, ca32, cb32;
 };
 
 // Arguments of one sweep VJP (k_adjoint.cu, FP64, component-wise reconstruction)
@@ -100,6 +106,10 @@ struct MetricPtrs32 {
 // Q at every cell from the interior of U (c2Prim) or of Q itself (from_q), with the
 // ghost layers produced by the composed boundary rules. U ghosts are written when
 // U_ghost_out is not null. csnd (optional) receives the split's sound speed.
+// F3D_PREC_REF32 pointwise kernels (k_ref32.cu)
+cudaError_t launch_metric_prep_ref32(const DevParams& P, const MetricPtrs32& m, cudaStream_t st);
+cudaError_t launch_prim_fill32(const DevParams& P, const float* U, float* Q, float* Ug, int mode, cudaStream_t st);
+cudaError_t launch_prim2c32(const DevParams& P, const float* Q, float* U, cudaStream_t st);
 cudaError_t launch_prim_fill(const DevParams& P, const double* U, double* Q, double* U_ghost_out, double* csnd,
                              int from_q, cudaStream_t st, float* Q32 = nullptr);
 cudaError_t launch_to_f32(const double* src, float* dst, long long n, cudaStream_t st);

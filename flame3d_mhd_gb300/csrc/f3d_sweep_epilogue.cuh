@@ -64,6 +64,28 @@ __device__ __forceinline__ void sweep_epilogue(const SweepArgs& a, const R* sF, 
                 d[n + 1] += k1 * (F[-2 * vs] - F[2 * vs]) + k2 * (F[-vs] - F[vs]);
             }
         }
+        if constexpr (sizeof(R) == 4) {
+            if (a.J32 && (a.out_mode == OUT_RHS || a.out_mode == OUT_STAGE)) {
+                // F3D_PREC_REF32: Float32 result, J dt L added to U and combined in Float32
+                // (div.jl:40-48, utils.jl:57-70)
+                if (a.out_mode == OUT_RHS) {
+                    const float Jc = a.J32[c];
+#pragma unroll
+                    for (int n = 0; n < 5; n++) a.out32[c + n * pl] = (acc[c + n * pl] + d[n]) * Jc;
+                } else {
+                    const float Jact = a.J32[c] * a.dt32;
+#pragma unroll
+                    for (int n = 0; n < 5; n++) {
+                        const float u = a.U32[c + n * pl];
+                        if (a.stage1_copy) a.Un32[c + n * pl] = u;
+                        float un = u + (acc[c + n * pl] + d[n]) * Jact;
+                        if (a.combine) un = un * a.ca32 + a.Un32[c + n * pl] * a.cb32;
+                        a.U32[c + n * pl] = un;
+                    }
+                }
+                continue;
+            }
+        }
         if (a.out_mode == OUT_SET) {
 #pragma unroll
             for (int n = 0; n < 5; n++) acc[c + n * pl] = d[n];

@@ -86,6 +86,24 @@ __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a
     if (!CHAR) {  // component-wise WENO7 (schemes.jl:143-230) / WENO5 (:231-276)
 #pragma unroll 1
         for (int n = 0; n < 5; n++) {
+            if constexpr (sizeof(R) == 4) {
+                if (P.ref32) {  // the reference's Float32 reconstruction
+                    if (br == 1) {
+                        const double fp = weno7_ref32(FP(n, p0), FP(n, p0 + 1), FP(n, p0 + 2), FP(n, p0 + 3),
+                                                      FP(n, p0 + 4), FP(n, p0 + 5), FP(n, p0 + 6), s0);
+                        const double fm = weno7_ref32(FM(n, p0 + 7), FM(n, p0 + 6), FM(n, p0 + 5), FM(n, p0 + 4),
+                                                      FM(n, p0 + 3), FM(n, p0 + 2), FM(n, p0 + 1), s0);
+                        out[n] = (float)((fp + fm) * (double)tmp1);
+                    } else {
+                        out[n] = (weno5_ref32(FP(n, p0 + 1), FP(n, p0 + 2), FP(n, p0 + 3), FP(n, p0 + 4),
+                                              FP(n, p0 + 5), s0) +
+                                  weno5_ref32(FM(n, p0 + 6), FM(n, p0 + 5), FM(n, p0 + 4), FM(n, p0 + 3),
+                                              FM(n, p0 + 2), s0)) *
+                                 tmp2;
+                    }
+                    continue;
+                }
+            }
             if (br == 1) {
                 R fp = weno7(FP(n, p0), FP(n, p0 + 1), FP(n, p0 + 2), FP(n, p0 + 3), FP(n, p0 + 4), FP(n, p0 + 5),
                              FP(n, p0 + 6), s0);
@@ -154,6 +172,24 @@ __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a
         auto projM = [&](int pos) {
             return FM(0, pos) * l0 + FM(1, pos) * l1 + FM(2, pos) * l2 + FM(3, pos) * l3 + FM(4, pos) * l4;
         };
+        if constexpr (sizeof(R) == 4) {
+            if (P.ref32) {  // the reference's Float32 reconstruction of the characteristic fields
+                if (br == 1) {
+                    const double fp = weno7_ref32(projP(p0), projP(p0 + 1), projP(p0 + 2), projP(p0 + 3),
+                                                  projP(p0 + 4), projP(p0 + 5), projP(p0 + 6), s0);
+                    const double fm = weno7_ref32(projM(p0 + 7), projM(p0 + 6), projM(p0 + 5), projM(p0 + 4),
+                                                  projM(p0 + 3), projM(p0 + 2), projM(p0 + 1), s0);
+                    flux[n] = (float)((fp + fm) * (double)tmp1);
+                } else {
+                    flux[n] = (weno5_ref32(projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4),
+                                           projP(p0 + 5), s0) +
+                               weno5_ref32(projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3),
+                                           projM(p0 + 2), s0)) *
+                              tmp2;
+                }
+                continue;
+            }
+        }
         if (br == 1) {
             R fp = weno7(projP(p0), projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5),
                          projP(p0 + 6), s0);

@@ -4,7 +4,8 @@ Method names and argument meaning follow the reference's Julia functions (solver
 utils.jl, boundary.jl, schemes.jl, div.jl): prim2c(U, Q), c2Prim(U, Q), linComb(U, Un, a, b),
 fillGhost(Q, U) (exchange_ghost + fillGhost), shockSensor(phi, Q), flowAdvance(Q),
 div(U, Fx, Fy, Fz, Fv_x, Fv_y, Fv_z, dt) and the RK3 loop of time_step. Arrays are torch
-float64 CUDA tensors whose memory is the reference's Julia layout: a tensor of shape
+float64 CUDA tensors (float32 for an F3D_PREC_REF32 context, the reference's own Float32
+arrays) whose memory is the reference's Julia layout: a tensor of shape
 (nvar, Nz+8, Ny+8, Nx+8) in C order is the Julia array (Nx+8, Ny+8, Nz+8, nvar).
 
 PyTorch only provides device memory and the stream here; every computation runs in the
@@ -49,6 +50,9 @@ class Flame3D:
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else
                                    torch.device(device).index or 0)
         self.params = params
+        # F3D_PREC_REF32: the reference's Float32 arrays (the *_f32 entries)
+        self.ref32 = params.precision == abi.PREC_REF32
+        self.dtype = torch.float32 if self.ref32 else torch.float64
         self.nx, self.ny, self.nz = params.nx, params.ny, params.nz
         self.shape3 = (self.nz + 2 * NG, self.ny + 2 * NG, self.nx + 2 * NG)
         self.metrics = None
@@ -71,8 +75,8 @@ class Flame3D:
     def _ptr(self, t: torch.Tensor | None, nvar: int | None = None) -> C.c_void_p | None:
         if t is None:
             return None
-        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
-            raise TypeError("arrays must be contiguous float64 CUDA tensors")
+        if not (t.is_cuda and t.dtype == self.dtype and t.is_contiguous()):
+            raise TypeError(f"arrays must be contiguous {str(self.dtype)[6:]} CUDA tensors")
         if nvar is not None and tuple(t.shape) != (nvar, *self.shape3) and not (
                 nvar == 1 and tuple(t.shape) == self.shape3):
             raise ValueError(f"expected shape {(nvar, *self.shape3)}, got {tuple(t.shape)}")
@@ -81,7 +85,7 @@ class Flame3D:
     def field(self, nvar: int) -> torch.Tensor:
         """Zero-initialised array in the reference layout with nvar variables."""
         shape = self.shape3 if nvar == 1 else (nvar, *self.shape3)
-        return torch.zeros(shape, dtype=torch.float64, device=self.device)
+        return torch.zeros(shape, dtype=self.dtype, device=self.device)
 
     def face_field(self, d: int) -> torch.Tensor:
         """Zero array shaped like the reference's Fx / Fy / Fz (solver.jl:298-300)."""
@@ -115,7 +119,8 @@ class Flame3D:
         if len(metrics) != 9:
             raise ValueError("need nine metric arrays")
         arr = (C.c_void_p * 9)(*[self._ptr(m, 1) for m in metrics])
-        self._check(self.lib.f3d_set_metrics(self._h, arr, self._ptr(J, 1), self._stream()))
+        fn = self.lib.f3d_set_metrics_f32 if self.ref32 else self.lib.f3d_set_metrics
+        self._check(fn(self._h, arr, self._ptr(J, 1), self._stream()))
         self.metrics, self.J = list(metrics), J  # keep the borrowed arrays alive
 
     def filter(self, U: torch.Tensor, Un: torch.Tensor, Q: torch.Tensor):
@@ -176,17 +181,20 @@ class Flame3D:
 
     # ---- utils.jl / boundary.jl ----------------------------------------------------------
     def prim2c(self, U: torch.Tensor, Q: torch.Tensor):
-        self._check(self.lib.f3d_prim2c(self._h, self._ptr(Q, 6), self._ptr(U, 5), self._stream()))
+        fn = self.lib.f3d_prim2c_f32 if self.ref32 else self.lib.f3d_prim2c
+        self._check(fn(self._h, self._ptr(Q, 6), self._ptr(U, 5), self._stream()))
 
     def c2Prim(self, U: torch.Tensor, Q: torch.Tensor):
-        self._check(self.lib.f3d_c2prim(self._h, self._ptr(U, 5), self._ptr(Q, 6), self._stream()))
+        fn = self.lib.f3d_c2prim_f32 if self.ref32 else self.lib.f3d_c2prim
+        self._check(fn(self._h, self._ptr(U, 5), self._ptr(Q, 6), self._stream()))
 
     def linComb(self, U: torch.Tensor, Un: torch.Tensor, a: float, b: float):
         self._check(self.lib.f3d_lincomb(self._h, self._ptr(U, 5), self._ptr(Un, 5), a, b, self._stream()))
 
     def fillGhost(self, Q: torch.Tensor, U: torch.Tensor):
         """exchange_ghost (periodic, one GPU) followed by fillGhost for Q and U."""
-        self._check(self.lib.f3d_fill_ghosts(self._h, self._ptr(Q, 6), self._ptr(U, 5), self._stream()))
+        fn = self.lib.f3d_fill_ghosts_f32 if self.ref32 else self.lib.f3d_fill_ghosts
+        self._check(fn(self._h, self._ptr(Q, 6), self._ptr(U, 5), self._stream()))
 
     # ---- schemes.jl / split.jl / viscous.jl / div.jl --------------------------------------
     def shockSensor(self, phi: torch.Tensor, Q: torch.Tensor):
@@ -227,17 +235,18 @@ class Flame3D:
         """L(U) at interior cells from a ghost-filled Q (fused sensor/split/reconstruction/divergence)."""
         if dUdt is None:
             dUdt = self.field(5)
-        self._check(self.lib.f3d_rhs(self._h, self._ptr(Q, 6), self._ptr(dUdt, 5), self._stream()))
+        fn = self.lib.f3d_rhs_f32 if self.ref32 else self.lib.f3d_rhs
+        self._check(fn(self._h, self._ptr(Q, 6), self._ptr(dUdt, 5), self._stream()))
         return dUdt
 
     def rk3_stage(self, stage: int, dt: float, U, Un, Q):
-        self._check(self.lib.f3d_rk3_stage(self._h, stage, dt, self._ptr(U, 5), self._ptr(Un, 5), self._ptr(Q, 6),
-                                           self._stream()))
+        fn = self.lib.f3d_rk3_stage_f32 if self.ref32 else self.lib.f3d_rk3_stage
+        self._check(fn(self._h, stage, dt, self._ptr(U, 5), self._ptr(Un, 5), self._ptr(Q, 6), self._stream()))
 
     def time_step(self, U, Un, Q, dt: float, nsteps: int):
         """nsteps SSP-RK3 steps (the hot loop of solver.jl:410-444)."""
-        self._check(self.lib.f3d_rk3_steps(self._h, nsteps, dt, self._ptr(U, 5), self._ptr(Un, 5),
-                                           self._ptr(Q, 6), self._stream()))
+        fn = self.lib.f3d_rk3_steps_f32 if self.ref32 else self.lib.f3d_rk3_steps
+        self._check(fn(self._h, nsteps, dt, self._ptr(U, 5), self._ptr(Un, 5), self._ptr(Q, 6), self._stream()))
 
     # ---- discrete adjoint ----------------------------------------------------------
     def rhs_vjp(self, U: torch.Tensor, Lbar: torch.Tensor, Ubar: torch.Tensor | None = None) -> torch.Tensor:

@@ -60,6 +60,10 @@ extern "C" {
 #define F3D_PREC_FP64 0  /* everything in FP64: the drop-in, parity at 1e-12             */
 #define F3D_PREC_MIXED 1 /* FP32 split/reconstruction/weights/viscous; FP64 state, EOS,
                             metrics/J, RK accumulation and reductions                   */
+#define F3D_PREC_REF32 2 /* the reference's own arithmetic on its Float32 arrays: U, Un, Q,
+                            metrics and J are Float32 and every step is Float32 except the
+                            WENO7 weights (FP64, schemes.jl:178-185); the *_f32 entries
+                            below, the FP64-array entries refuse such a context          */
 
 /* explicit filters of U (utils.jl:102-315) */
 #define F3D_FILTER_NONE 0
@@ -262,6 +266,23 @@ int f3d_set_inflow_profile(f3d_ctx* ctx, int face, const double* prof, f3d_strea
  * checking it against the conversion instruction. No context; no counterpart in the
  * reference. */
 int f3d_debug_round_f32(const double* in, float* out, long long n, f3d_stream stream);
+
+/* ---- F3D_PREC_REF32: the reference's Float32 arrays and arithmetic ---------------------
+ * The same calls as f3d_set_metrics, f3d_c2prim, f3d_prim2c, f3d_fill_ghosts, f3d_rhs,
+ * f3d_rk3_stage and f3d_rk3_steps on Float32 arrays of the same shapes: the reference's
+ * CuArray{Float32} U, Un, Q, metrics and J (solver.jl:238-337) pass unchanged. The
+ * computation follows the reference's Float32 operations (c2Prim clamps at eps(Float32),
+ * Float32 splitting, sensor, UP7/WENO5 and viscous fluxes, WENO7 weights in FP64, Float32
+ * RK update); FP64 entries and these refuse each other's contexts (F3D_ERR_ARG). No
+ * inflow-profile faces, local time stepping, filters, LES, adjoint or finite-volume
+ * scheme in this form (F3D_ERR_UNSUPPORTED at f3d_create). */
+int f3d_set_metrics_f32(f3d_ctx* ctx, const float* const metrics[9], const float* jac, f3d_stream stream);
+int f3d_c2prim_f32(f3d_ctx* ctx, const float* U, float* Q, f3d_stream stream);
+int f3d_prim2c_f32(f3d_ctx* ctx, const float* Q, float* U, f3d_stream stream);
+int f3d_fill_ghosts_f32(f3d_ctx* ctx, float* Q, float* U, f3d_stream stream);
+int f3d_rhs_f32(f3d_ctx* ctx, const float* Q, float* dUdt, f3d_stream stream);
+int f3d_rk3_stage_f32(f3d_ctx* ctx, int stage, float dt, float* U, float* Un, float* Q, f3d_stream stream);
+int f3d_rk3_steps_f32(f3d_ctx* ctx, int nsteps, float dt, float* U, float* Un, float* Q, f3d_stream stream);
 
 /* ---- discrete adjoint (FP64, component-wise reconstruction, SW or LF splitting) ---- */
 

@@ -272,6 +272,23 @@ def rhs32(P, Q32, m32, J32):
     return out
 
 
+def c2prim32(P, U32):
+    """c2Prim in the reference's Float32 arithmetic (interior cells; the rest of Q zero)."""
+    Q = zeros(P, 6, np.float32)
+    lib().orc32_c2prim(C.byref(P), _p(U32), _p(Q))
+    return Q
+
+
+def prim2c32(P, Q32):
+    U = zeros(P, 5, np.float32)
+    lib().orc32_prim2c(C.byref(P), _p(Q32), _p(U))
+    return U
+
+
+def fill_ghosts32(P, Q32, U32):
+    lib().orc32_fill_ghosts(C.byref(P), _p(Q32), _p(U32))
+
+
 def rk3_32(P, nsteps, dt, U, Un, Q, m, J):
     lib().orc32_rk3(C.byref(P), C.c_int(nsteps), C.c_float(dt), _p(U), _p(Un), _p(Q), _pp(m), _p(J))
 

@@ -214,6 +214,7 @@ void orc32_rk3(const f3d_params* P, int nsteps, float dt, float* U, float* Un, f
 }
 void orc32_c2prim(const f3d_params* P, const float* U, float* Q) { c2prim<float>(*P, U, Q); }
 void orc32_fill_ghosts(const f3d_params* P, float* Q, float* U) { fill_ghosts<float>(*P, Q, U); }
+void orc32_prim2c(const f3d_params* P, const float* Q, float* U) { prim2c<float>(*P, Q, U); }
 
 // ---- forward-mode derivative (dual numbers) -----------------------------------------
 // JVP of the RHS as a function of the interior conserved state: U -> c2Prim -> ghost fill
