@@ -358,6 +358,22 @@ def run_ours(args):
              "step_hbm_frac": STEP_BYTES_PER_CELL * cells / (ms_mixed / args.steps / 1e3) / 1e9 / load_peaks()["hbm_gbs"]}
     sm.close()
 
+    # the reference's own Float32 arrays and arithmetic (F3D_PREC_REF32), same workload and
+    # step count, from the Float32 copy of the same initial state
+    from flame3d_mhd_gb300.abi import PREC_REF32
+    sr = Flame3D(params_copy(P, precision=PREC_REF32))
+    sr.set_metrics([a.float() for a in ms], J.float())
+    Ur, Unr, Qr = U0.float(), torch.zeros_like(U0, dtype=torch.float32), Q0.float()
+    sr.q_from_u(Ur, Qr)
+    ms_r32, _, _ = timed_steps(sr, Ur, Unr, Qr, args.steps, args.warmup)
+    ref32 = {"value": ws * cells * 3 * args.steps / (ms_r32 / 1e3) / 1e6, "unit": UNIT,
+             "ms_per_step": ms_r32 / args.steps,
+             "form": "the reference's Float32 arrays and arithmetic (WENO7 weights in FP64)",
+             "state_rel_linf_vs_fp64_after_steps":
+                 float((Ur[Iin].double() - U_fp64[Iin]).abs().max() / U_fp64[Iin].abs().max()),
+             "state_finite": bool(torch.isfinite(Ur).all())}
+    sr.close()
+
     # the reference's default scheme (run.jl:64-65: finite volume, eigen reconstruction,
     # HLLC) on the same workload and step count, FP64
     from flame3d_mhd_gb300.abi import SCHEME_FVM_EIGEN
@@ -437,6 +453,7 @@ def run_ours(args):
                           "frac": step_gbs / peaks["hbm_gbs"], "alg_bytes_per_cell_step": STEP_BYTES_PER_CELL},
         "mcell_updates_per_s": value / 3,
         "mixed": mixed,
+        "ref32": ref32,
         "fvm": fvm,
         "adjoint": adjoint,
         "clocks": clocks,
