@@ -138,6 +138,34 @@ class RampAdjoint:
         return val
 
 
+def mixed_forward(R: "RampAdjoint", cells: int, J0: float, area0: torch.Tensor) -> dict:
+    """The same N steps in mixed precision (FP32 fluxes, FP64 state): time per step of the
+    steps before the window and J of the window, against the FP64 J0."""
+    Pm = params_copy(R.case["params"], precision=PREC_MIXED, adjoint_lean=0)
+    sm = Flame3D(Pm)
+    sm.set_metrics(*R.metrics[0])
+    sm.set_inflow_profile(0, R.prof0)
+    U, Un, Q = R.U0.clone(), sm.field(5), sm.field(6)
+    acc = []
+    with side_stream() as stream:
+        sm.q_from_u(U, Q)
+        sm.time_step(U, Un, Q, R.dt, 1)  # capture the step graph
+        R.objective(U, 1, acc, area0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sm.time_step(U, Un, Q, R.dt, R.N - R.W - 1)
+        e1.record(stream)
+        for n in range(R.N - R.W + 1, R.N + 1):
+            sm.time_step(U, Un, Q, R.dt, 1)
+            R.objective(U, n, acc, area0)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(R.N - R.W - 1, 1)
+    Jm = float(torch.stack(acc).sum())
+    sm.close()
+    return {"ms_per_step": ms, "mcell_rhs_per_s": 3 * cells / (ms * 1e3), "J": Jm,
+            "J_rel_diff_vs_fp64": abs(Jm - J0) / abs(J0)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--nx", type=int, default=1024)
@@ -159,6 +187,8 @@ def main(argv=None):
     ap.add_argument("--fd-angle-h", type=str, default="1e-3", help="difference step(s) of theta in degrees")
     ap.add_argument("--mixed", type=int, default=1, help="also time the mixed-precision forward run")
     ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--forward-only", action="store_true",
+                    help="only the FP64 and mixed-precision forward runs and their J (no adjoint)")
     ap.add_argument("--fd-only", action="store_true",
                     help="only J and its central differences in theta (no adjoint, no mixed run): the "
                          "difference's dependence on h separates truncation (h^2) from kinks of the "
@@ -176,6 +206,18 @@ def main(argv=None):
     mp, mm = R._metrics(a.angle + a.eta), R._metrics(a.angle - a.eta)
     dA = (R.area(mp) - R.area(mm)) / (2 * a.eta)
 
+    if a.forward_only:  # J in FP64 and the mixed-precision forward run, no gradient
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J0 = R.J()
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        out["fp64_forward"] = {"s": t_fwd, "mcell_rhs_per_s": 3 * cells * a.steps / t_fwd / 1e6}
+        out["J"] = J0
+        out["mixed_forward"] = mixed_forward(R, cells, J0, R.area(R.metrics[0]))
+        print(json.dumps(out))
+        s.close()
+        return out
     if a.fd_only:
         out["J"] = R.J()
         out["checks"] = []
@@ -296,29 +338,7 @@ def main(argv=None):
     out["checks"] = checks
 
     if a.mixed:
-        Pm = params_copy(R.case["params"], precision=PREC_MIXED)
-        sm = Flame3D(Pm)
-        sm.set_metrics(*R.metrics[0])
-        sm.set_inflow_profile(0, R.prof0)
-        U, Un, Q = R.U0.clone(), sm.field(5), sm.field(6)
-        acc = []
-        with side_stream() as stream:
-            sm.q_from_u(U, Q)
-            sm.time_step(U, Un, Q, R.dt, 1)  # capture the step graph
-            R.objective(U, 1, acc, area0)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            sm.time_step(U, Un, Q, R.dt, R.N - R.W - 1)
-            e1.record(stream)
-            for n in range(R.N - R.W + 1, R.N + 1):
-                sm.time_step(U, Un, Q, R.dt, 1)
-                R.objective(U, n, acc, area0)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / max(R.N - R.W - 1, 1)
-        Jm = float(torch.stack(acc).sum())
-        out["mixed_forward"] = {"ms_per_step": ms, "mcell_rhs_per_s": 3 * cells / (ms * 1e3),
-                                "J": Jm, "J_rel_diff_vs_fp64": abs(Jm - J0) / abs(J0)}
-        sm.close()
+        out["mixed_forward"] = mixed_forward(R, cells, J0, area0)
     out["max_rel_diff"] = max((c["rel_diff"] for c in checks), default=None)
     print(json.dumps(out))
     s.close()
