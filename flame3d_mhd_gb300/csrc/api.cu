@@ -203,6 +203,11 @@ struct f3d_ctx {
     double *Qb = nullptr, *Lt = nullptr, *U1 = nullptr, *U2 = nullptr, *Xb = nullptr, *Yb = nullptr;
     double *Qst[3] = {}, *cst_[3] = {}, *phst[3] = {};  // Q, sound speed and sensor of the stage states
     double *Fvb[3] = {}, *gb = nullptr;
+    // metric and Jacobian cotangents (borrowed; f3d_set_metrics_cotangent) and the forward
+    // RHS of the first two stage states kept for the Jacobian's term (10 arrays, owned)
+    double* mbar[9] = {};
+    double* Jbar = nullptr;
+    double* lsave = nullptr;
     // CUDA graph of one RK3 step, keyed by its arguments
     cudaGraphExec_t step_graph = nullptr;
     const void* g_key[4] = {};
@@ -514,8 +519,12 @@ int rhs_prepared(f3d_ctx* ctx, const double* Q, const double* csnd, const double
 }
 
 // out = beta out + alpha (dL/dU)^T Lb at interior cells, for the state U prepared in Q/csnd/phi
+// With metric cotangents set (ctx->mbar) the metric and Jacobian cotangents are accumulated
+// too, scaled by alpha; Lfwd is the forward RHS of the state (for the Jacobian's L = J D).
 int rhs_vjp_prepared(f3d_ctx* ctx, const double* U, const double* Q, const double* csnd, const double* phi,
-                     const double* Lb, double* out, double alpha, double beta, cudaStream_t st) {
+                     const double* Lb, double* out, double alpha, double beta, cudaStream_t st,
+                     const double* Lfwd = nullptr) {
+    const bool mbar = ctx->mbar[0] != nullptr;
     const DevParams& P = ctx->dp;
     const bool hybrid = P.fixed_branch < 0;
     F3D_CUDA(ctx, cudaMemsetAsync(ctx->Qb, 0, (size_t)P.plane * 6 * sizeof(double), st));
@@ -534,10 +543,19 @@ int rhs_vjp_prepared(f3d_ctx* ctx, const double* U, const double* Q, const doubl
         a.J = ctx->J;
         a.Lb = Lb;
         a.Qb = ctx->Qb;
+        if (mbar) {
+            for (int n = 0; n < 3; n++) a.mb[n] = ctx->mbar[3 * d + n];
+            a.mscale = alpha;
+        }
         F3D_CUDA(ctx, launch_sweep_vjp(d, a, st));
     }
     if (ctx->params.viscous)
-        F3D_CUDA(ctx, launch_viscous_vjp(P, Q, ctx->m, ctx->J, Lb, ctx->Fvb, ctx->gb, ctx->Qb, st));
+        F3D_CUDA(ctx, launch_viscous_vjp(P, Q, ctx->m, ctx->J, Lb, ctx->Fvb, ctx->gb, ctx->Qb, st,
+                                         mbar ? ctx->mbar : nullptr, ctx->Jbar, alpha));
+    if (mbar) {
+        if (!Lfwd) return fail(ctx, F3D_ERR_STATE, "metric cotangents need the forward RHS of the state");
+        F3D_CUDA(ctx, launch_jbar(P, Lb, Lfwd, ctx->J, ctx->Jbar, alpha, st));
+    }
     F3D_CUDA(ctx, launch_fill_vjp(P, Q, ctx->Qb, alpha, st));
     F3D_CUDA(ctx, launch_c2prim_vjp(P, U, ctx->Qb, out, alpha, beta, st));
     return F3D_OK;
@@ -725,6 +743,7 @@ int f3d_destroy(f3d_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
     if (ctx->adj_slab) cudaFree(ctx->adj_slab);
+    if (ctx->lsave) cudaFree(ctx->lsave);
     if (ctx->extra) cudaFree(ctx->extra);
     cudaError_t e = cudaFree(ctx->slab);
     delete ctx;
@@ -989,6 +1008,28 @@ int f3d_set_coordinates(f3d_ctx* ctx, const double* x, const double* y, const do
     return F3D_OK;
 }
 
+int f3d_set_metrics_cotangent(f3d_ctx* ctx, double* const metrics_bar[9], double* jac_bar, f3d_stream stream) {
+    (void)stream;
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!metrics_bar) {
+        for (int n = 0; n < 9; n++) ctx->mbar[n] = nullptr;
+        ctx->Jbar = nullptr;
+        return F3D_OK;
+    }
+    if ((rc = adjoint_supported(ctx))) return rc;
+    if ((rc = check_ptrs(ctx, {metrics_bar[0], metrics_bar[1], metrics_bar[2], metrics_bar[3], metrics_bar[4],
+                              metrics_bar[5], metrics_bar[6], metrics_bar[7], metrics_bar[8], jac_bar})))
+        return rc;
+    if (!ctx->lsave) {
+        cudaError_t e = cudaMalloc(&ctx->lsave, (size_t)ctx->dp.plane * 10 * sizeof(double));
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc (forward RHS of the stage states)");
+    }
+    for (int n = 0; n < 9; n++) ctx->mbar[n] = metrics_bar[n];
+    ctx->Jbar = jac_bar;
+    return F3D_OK;
+}
+
 int f3d_set_inflow_profile_cotangent(f3d_ctx* ctx, int face, double* prof_bar, f3d_stream stream) {
     (void)stream;
     if (!ctx) return F3D_ERR_ARG;
@@ -1023,7 +1064,10 @@ int f3d_rhs_vjp(f3d_ctx* ctx, const double* U, const double* Lbar, double* Ubar,
     cudaStream_t st = (cudaStream_t)stream;
     F3D_CUDA(ctx, cudaMemsetAsync(Ubar, 0, (size_t)ctx->dp.plane * 5 * sizeof(double), st));
     if ((rc = prep_state(ctx, U, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
-    return rhs_vjp_prepared(ctx, U, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], Lbar, Ubar, 1.0, 0.0, st);
+    const bool mbar = ctx->mbar[0] != nullptr;
+    if (mbar && (rc = rhs_prepared(ctx, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], ctx->Lt, st))) return rc;
+    return rhs_vjp_prepared(ctx, U, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], Lbar, Ubar, 1.0, 0.0, st,
+                            mbar ? ctx->Lt : nullptr);
 }
 
 // SSP-RK3 step U1 = U0 + dt L(U0), U2 = 3/4 U0 + 1/4 (U1 + dt L(U1)),
@@ -1048,11 +1092,16 @@ int f3d_rk3_step_vjp_stages(f3d_ctx* ctx, double dt, const double* U0, const dou
     const DevParams& P = ctx->dp;
     // forward recompute of the two intermediate stage states U1, U2
     const double* Us[3] = {U0, ctx->U1, ctx->U2};
+    const bool mbar = ctx->mbar[0] != nullptr;
+    const size_t lbytes = (size_t)P.plane * 5 * sizeof(double);
     if ((rc = prep_state(ctx, U0, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], st))) return rc;
     if ((rc = rhs_prepared(ctx, ctx->Qst[0], ctx->cst_[0], ctx->phst[0], ctx->Lt, st))) return rc;
+    if (mbar) F3D_CUDA(ctx, cudaMemcpyAsync(ctx->lsave, ctx->Lt, lbytes, cudaMemcpyDeviceToDevice, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->U1, U0, 1.0, ctx->Lt, dt, st));
     if ((rc = prep_state(ctx, ctx->U1, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], st))) return rc;
     if ((rc = rhs_prepared(ctx, ctx->Qst[1], ctx->cst_[1], ctx->phst[1], ctx->Lt, st))) return rc;
+    if (mbar)
+        F3D_CUDA(ctx, cudaMemcpyAsync(ctx->lsave + 5 * P.plane, ctx->Lt, lbytes, cudaMemcpyDeviceToDevice, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U1, 0.25, ctx->Lt, 0.25 * dt, st));
     F3D_CUDA(ctx, launch_axpby(P, ctx->U2, ctx->U2, 1.0, U0, 0.75, st));
     // each stage's VJP needs its prepared state (Q, sound speed, sensor): kept from the
@@ -1060,13 +1109,17 @@ int f3d_rk3_step_vjp_stages(f3d_ctx* ctx, double dt, const double* U0, const dou
     // ghost fill, and the sensor) for stages 1 and 0
     const bool lean = ctx->params.adjoint_lean != 0;
     if ((rc = prep_state(ctx, ctx->U2, ctx->Qst[2], ctx->cst_[2], ctx->phst[2], st))) return rc;
+    // the metric cotangents' Jacobian term needs L(U2) too (one more RHS)
+    if (mbar && (rc = rhs_prepared(ctx, ctx->Qst[2], ctx->cst_[2], ctx->phst[2], ctx->Lt, st))) return rc;
+    const double* Lf[3] = {ctx->lsave, ctx->lsave ? ctx->lsave + 5 * P.plane : nullptr, ctx->Lt};
     const long long pl5 = 5 * P.plane;
     if (Ustage)
         for (int k = 0; k < 3; k++) F3D_CUDA(ctx, launch_axpby(P, Ustage + k * pl5, Us[k], 1.0, nullptr, 0.0, st));
     auto vjp = [&](int k, const double* Lb, double* out) {
         if (Lbar_stage) F3D_CUDA(ctx, launch_axpby(P, Lbar_stage + k * pl5, Lb, dt, nullptr, 0.0, st));
         int r = (lean && k < 2) ? prep_state(ctx, Us[k], ctx->Qst[k], ctx->cst_[k], ctx->phst[k], st) : 0;
-        return r ? r : rhs_vjp_prepared(ctx, Us[k], ctx->Qst[k], ctx->cst_[k], ctx->phst[k], Lb, out, dt, 1.0, st);
+        return r ? r : rhs_vjp_prepared(ctx, Us[k], ctx->Qst[k], ctx->cst_[k], ctx->phst[k], Lb, out, dt, 1.0, st,
+                                        mbar ? Lf[k] : nullptr);
     };
     // stage 3: U3 = 1/3 U0 + 2/3 W, W = U2 + dt L(U2)
     F3D_CUDA(ctx, launch_axpby(P, Ubar, Ubar_next, 1.0 / 3.0, nullptr, 0.0, st));

@@ -40,9 +40,11 @@ __device__ __forceinline__ void c2prim_vjp(const DevParams& P, const double U[5]
 // ---- flux splitting (split.jl) -------------------------------------------------------
 // q = (rho,u,v,w,p,T); c = the split's sound speed; fpb/fmb cotangents of Fp/Fm.
 // Accumulates into qb[6] (the sound-speed dependence goes to T for SW, to p and rho for LF).
+// mg (optional): cotangents of the metric inputs, {A1, A2, A3, H1, H2, H3, |A|} += .
 __device__ __forceinline__ void split_sw_vjp(const Cst<double>& K, const double q[6], double c, double A1, double A2,
                                              double A3, double H1, double H2, double H3, double ss,
-                                             const double fpb[5], const double fmb[5], double qb[6]) {
+                                             const double fpb[5], const double fmb[5], double qb[6],
+                                             double* mg = nullptr) {
     const double rho = q[0], u = q[1], v = q[2], w = q[3];
     const double E1 = A1 * u + A2 * v + A3 * w;
     const double E[3] = {E1, E1 - c * ss, E1 + c * ss};
@@ -105,6 +107,15 @@ __device__ __forceinline__ void split_sw_vjp(const Cst<double>& K, const double 
     // E2 = E1 - c ss, E3 = E1 + c ss
     const double E1b = Eb[0] + Eb[1] + Eb[2];
     cb += (Eb[2] - Eb[1]) * ss;
+    if (mg) {  // E1 = A . u; uc = u -+ c H; E2, E3 = E1 -+ c ss
+        mg[0] += E1b * u;
+        mg[1] += E1b * v;
+        mg[2] += E1b * w;
+        mg[3] += (ucb[1] - ucb[0]) * c;
+        mg[4] += (vcb[1] - vcb[0]) * c;
+        mg[5] += (wcb[1] - wcb[0]) * c;
+        mg[6] += (Eb[2] - Eb[1]) * c;
+    }
     ub += A1 * E1b;
     vb += A2 * E1b;
     wb += A3 * E1b;
@@ -118,7 +129,7 @@ __device__ __forceinline__ void split_sw_vjp(const Cst<double>& K, const double 
 
 __device__ __forceinline__ void split_lf_vjp(const Cst<double>& K, const double q[6], double c, double A1, double A2,
                                              double A3, double ss, const double fpb[5], const double fmb[5],
-                                             double qb[6]) {
+                                             double qb[6], double* mg = nullptr) {
     const double rho = q[0], u = q[1], v = q[2], w = q[3], p = q[4];
     const double un = A1 * u + A2 * v + A3 * w;
     const double l0 = fabs(un) + c * ss;
@@ -155,6 +166,12 @@ __device__ __forceinline__ void split_lf_vjp(const Cst<double>& K, const double 
     // l0 = |un| + c ss
     unb += l0b * (un >= 0.0 ? 1.0 : -1.0);
     const double cb = l0b * ss;
+    if (mg) {  // un = A . u; the pressure terms A_k p; l0 = |un| + c ss (no A/|A| here)
+        mg[0] += unb * u + Fb[1] * p;
+        mg[1] += unb * v + Fb[2] * p;
+        mg[2] += unb * w + Fb[3] * p;
+        mg[6] += l0b * c;
+    }
     ub += A1 * unb;
     vb += A2 * unb;
     wb += A3 * unb;
@@ -173,7 +190,9 @@ __device__ __forceinline__ void split_lf_vjp(const Cst<double>& K, const double 
 // (schemes.jl:153-185, 233-252). With fb the cotangent of f (already divided by 12 or 6):
 // qb_k = fb w_k, alphab_k = fb (q_k - f) / sum alpha, tb_k = -2 alpha_k / t_k alphab_k, and
 // IS_k is a quadratic form whose gradient is formed from the coefficient table.
-__device__ __forceinline__ void weno5_vjp(const double V[5], double s0, double fb, double Vb[5]) {
+// s0b (optional): += the cotangent of the scale s0 (t_k = eps + IS_k s0).
+__device__ __forceinline__ void weno5_vjp(const double V[5], double s0, double fb, double Vb[5],
+                                          double* s0b = nullptr) {
     const double V1 = V[0], V2 = V[1], V3 = V[2], V4 = V[3], V5 = V[4];
     const double a1_ = V1 - 2 * V2 + V3, b1_ = V1 - 4 * V2 + 3 * V3;
     const double a2_ = V2 - 2 * V3 + V4, b2_ = V2 - V4;
@@ -198,7 +217,9 @@ __device__ __forceinline__ void weno5_vjp(const double V[5], double s0, double f
         const double wk = al[k] * rs;
         qb[k] = fb * wk;
         // alpha_k-bar = fb (q_k - f) / sum, t_k-bar = -2 alpha_k / t_k alpha_k-bar
-        ISb[k] = -2.0 * s0 * fb * (q[k] - f) * wk * it[k];
+        const double tb = -2.0 * fb * (q[k] - f) * wk * it[k];
+        ISb[k] = s0 * tb;
+        if (s0b) *s0b += IS[k] * tb;
     }
     for (int j = 0; j < 5; j++) Vb[j] = 0.0;
     // q
@@ -223,9 +244,10 @@ __device__ __constant__ const double kW7IS[4][4][4] = {
     {{2107, -9402, 7042, -1854}, {0, 11003, -17246, 4642}, {0, 0, 7043, -3882}, {0, 0, 0, 547}}};
 __device__ __constant__ const double kW7Q[4][4] = {{-3, 13, -23, 25}, {1, -5, 13, 3}, {-1, 7, 7, -1}, {3, 13, -5, 1}};
 
-__device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double fb, double Vb[7]) {
+__device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double fb, double Vb[7],
+                                          double* s0b = nullptr) {
     const double d[4] = {1.0, 12.0, 18.0, 4.0};
-    double q[4], t[4];
+    double q[4], t[4], IS[4];
     for (int k = 0; k < 4; k++) {
         double is = 0, qq = 0;
         for (int i = 0; i < 4; i++) {
@@ -233,6 +255,7 @@ __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double f
             for (int j = i; j < 4; j++) is += kW7IS[k][i][j] * V[k + i] * V[k + j];
         }
         q[k] = qq;
+        IS[k] = is;
         t[k] = 1e-20 + is * s0;
     }
     // two FP64 divisions: 1/t_k from 1/(t1 t2 t3 t4), and 1/sum alpha
@@ -250,7 +273,9 @@ __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double f
     for (int k = 0; k < 4; k++) {
         const double wk = al[k] * rs;
         const double qb = fb * wk;
-        const double ISb = -2.0 * s0 * fb * (q[k] - f) * wk * it[k];
+        const double tb = -2.0 * fb * (q[k] - f) * wk * it[k];
+        const double ISb = s0 * tb;
+        if (s0b) *s0b += IS[k] * tb;
         for (int i = 0; i < 4; i++) {
             Vb[k + i] += kW7Q[k][i] * qb;
             double g = 0;  // dIS/dV_{k+i}

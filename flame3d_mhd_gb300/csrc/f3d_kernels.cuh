@@ -41,6 +41,13 @@ struct SweepArgs {
     float dt32, ca32, cb32;
 };
 
+// Metric and Jacobian cotangents accumulated by the viscous VJP (null m[0]: none)
+struct MetricBar {
+    double* m[9];
+    double* J;
+    double scale;
+};
+
 // Arguments of one sweep VJP (k_adjoint.cu, FP64, component-wise reconstruction)
 struct AdjArgs {
     DevParams P;
@@ -53,12 +60,18 @@ struct AdjArgs {
     const double* J;
     const double* Lb;     // cotangent of the RHS (U layout, interior cells)
     double* Qb;           // accumulated cotangent of Q (6 x Nt^3)
+    double* mb[3];        // optional: accumulated cotangent of this direction's metric row
+    double mscale;        //   (scaled by mscale, the VJP's alpha)
 };
 
 cudaError_t adjoint_configure();
 cudaError_t launch_sweep_vjp(int dir, const AdjArgs& a, cudaStream_t st);
 cudaError_t launch_viscous_vjp(const DevParams& P, const double* Q, const double* const m[9], const double* J,
-                               const double* Lb, double* Fvb[3], double* gb, double* Qb, cudaStream_t st);
+                               const double* Lb, double* Fvb[3], double* gb, double* Qb, cudaStream_t st,
+                               double* const mbar[9] = nullptr, double* Jbar = nullptr, double mscale = 0.0);
+// Jbar += mscale sum_n Lb L / J at interior cells: the RHS's direct dependence on J (L = J D)
+cudaError_t launch_jbar(const DevParams& P, const double* Lb, const double* L, const double* J, double* Jbar,
+                        double mscale, cudaStream_t st);
 cudaError_t launch_fill_vjp(const DevParams& P, const double* Q, double* Qb, double pscale, cudaStream_t st);
 cudaError_t launch_c2prim_vjp(const DevParams& P, const double* U, const double* Qb, double* out, double alpha,
                               double beta, cudaStream_t st);

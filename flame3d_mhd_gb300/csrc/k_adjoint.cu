@@ -115,6 +115,8 @@ __global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(
             for (int n = 0; n < 5; n++) Fb[n] -= j * a.Lb[cl + n * pl];
         }
         const double s0 = (br == 1 || br == 2) ? 2.0 / (a.S[cl] + a.S[cr]) : 0.0;
+        double s0b_ = 0.0;
+        double* s0b = a.mb[0] ? &s0b_ : nullptr;  // metric cotangent wanted
         for (int n = 0; n < 5; n++) {
             const double g = Fb[n];
             if (g == 0.0) continue;
@@ -132,18 +134,18 @@ __global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(
             } else if (br == 1) {  // WENO7, (fp + fm)/12
                 double V[7], Vb[7];
                 for (int k = 0; k < 7; k++) V[k] = P_(t + k);
-                weno7_vjp(V, s0, g * (1.0 / 12.0), Vb);
+                weno7_vjp(V, s0, g * (1.0 / 12.0), Vb, s0b);
                 for (int k = 0; k < 7; k++) atomicAdd(&pb[sidx(l, t + k)], Vb[k]);
                 for (int k = 0; k < 7; k++) V[k] = M_(t + 7 - k);
-                weno7_vjp(V, s0, g * (1.0 / 12.0), Vb);
+                weno7_vjp(V, s0, g * (1.0 / 12.0), Vb, s0b);
                 for (int k = 0; k < 7; k++) atomicAdd(&mb[sidx(l, t + 7 - k)], Vb[k]);
             } else if (br == 2) {  // WENO5, (fp + fm)/6: Fp at t+1..t+5, Fm at t+6..t+2
                 double V[5], Vb[5];
                 for (int k = 0; k < 5; k++) V[k] = P_(t + 1 + k);
-                weno5_vjp(V, s0, g * (1.0 / 6.0), Vb);
+                weno5_vjp(V, s0, g * (1.0 / 6.0), Vb, s0b);
                 for (int k = 0; k < 5; k++) atomicAdd(&pb[sidx(l, t + 1 + k)], Vb[k]);
                 for (int k = 0; k < 5; k++) V[k] = M_(t + 6 - k);
-                weno5_vjp(V, s0, g * (1.0 / 6.0), Vb);
+                weno5_vjp(V, s0, g * (1.0 / 6.0), Vb, s0b);
                 for (int k = 0; k < 5; k++) atomicAdd(&mb[sidx(l, t + 6 - k)], Vb[k]);
             } else {  // NND2 (schemes.jl:277-286): minmod picks one difference or none
                 // fp = Fp[t+3] + 0.5 minmod(Fp[t+4]-Fp[t+3], Fp[t+3]-Fp[t+2])
@@ -170,6 +172,15 @@ __global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(
                         atomicAdd(&mb[sidx(l, t + 4)], 0.5 * g);
                     }
                 }
+            }
+        }
+        if (s0b && s0b_ != 0.0) {
+            // s0 = 2 / (S_l + S_r): both |A| get -s0^2/2 s0-bar, and |A| passes A_j / |A| to A_j
+            const double Sb = -0.5 * s0 * s0 * s0b_ * a.mscale;
+            const long long cc[2] = {cl, cr};
+            for (int e = 0; e < 2; e++) {
+                const double r = Sb / a.S[cc[e]];
+                for (int j = 0; j < 3; j++) atomicAdd(&a.mb[j][cc[e]], r * a.A[j][cc[e]]);
             }
         }
     };
@@ -221,14 +232,27 @@ __global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(
         if (!any) continue;
         const long long c = cell(l, c0 + p);
         double q[6], qb[6] = {0, 0, 0, 0, 0, 0};
+        double mg[7] = {0, 0, 0, 0, 0, 0, 0};
+        double* mgp = a.mb[0] ? mg : nullptr;
         for (int n = 0; n < 6; n++) q[n] = a.Q[c + n * pl];
+        const double A3[3] = {a.A[0][c], a.A[1][c], a.A[2][c]};
+        const double S = a.S[c];
         if (P.split == F3D_SPLIT_SW)
-            split_sw_vjp(P.cd, q, a.csnd[c], a.A[0][c], a.A[1][c], a.A[2][c], a.Ah[0][c], a.Ah[1][c], a.Ah[2][c],
-                         a.S[c], fpb, fmb, qb);
+            split_sw_vjp(P.cd, q, a.csnd[c], A3[0], A3[1], A3[2], a.Ah[0][c], a.Ah[1][c], a.Ah[2][c], S, fpb, fmb, qb,
+                         mgp);
         else
-            split_lf_vjp(P.cd, q, a.csnd[c], a.A[0][c], a.A[1][c], a.A[2][c], a.S[c], fpb, fmb, qb);
+            split_lf_vjp(P.cd, q, a.csnd[c], A3[0], A3[1], A3[2], S, fpb, fmb, qb, mgp);
         for (int n = 0; n < 6; n++)
             if (qb[n] != 0.0) atomicAdd(&a.Qb[c + n * pl], qb[n]);
+        if (mgp) {
+            // A/|A| and |A| derive from A: A_j-bar += H_j-bar/S - (H-bar . A) A_j/S^3 + S-bar A_j/S
+            const double iS = 1.0 / S;
+            const double hA = (mg[3] * A3[0] + mg[4] * A3[1] + mg[5] * A3[2]) * iS * iS * iS;
+            for (int j = 0; j < 3; j++) {
+                const double b = mg[j] + mg[3 + j] * iS - hA * A3[j] + mg[6] * A3[j] * iS;
+                if (b != 0.0) atomicAdd(&a.mb[j][c], a.mscale * b);
+            }
+        }
     }
 }
 
@@ -278,7 +302,7 @@ __global__ void k_visc_fvb(const DevParams P, const double* __restrict__ Lb, con
 __global__ void k_visc_vjp(const DevParams P, const double* __restrict__ Q, const double* m0, const double* m1,
                            const double* m2, const double* m3, const double* m4, const double* m5, const double* m6,
                            const double* m7, const double* m8, const double* __restrict__ J, const double* Fvbx,
-                           const double* Fvby, const double* Fvbz, double* gb, double* Qb) {
+                           const double* Fvby, const double* Fvbz, double* gb, double* Qb, MetricBar mbar) {
     const int vxt = P.nxt - 4, vyt = P.nyt - 4, vzt = P.nzt - 4;
     const long long vpl = (long long)vxt * vyt * vzt;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -365,6 +389,37 @@ __global__ void k_visc_vjp(const DevParams P, const double* __restrict__ Q, cons
     atomicAdd(&Qb[c + 2 * pl], ub[1]);
     atomicAdd(&Qb[c + 3 * pl], ub[2]);
     atomicAdd(&Qb[c + 5 * pl], Tb_mu);
+    if (mbar.m[0]) {
+        // metric cotangents of this cell: the projections Fv_d = sum_x M[d][x] (tau, E)[x] and
+        // the gradients D[a][x] = (sum_d G[a][d] M[d][x]) J
+        double E[3];
+        for (int x = 0; x < 3; x++) E[x] = uvw[0] * tau[0][x] + uvw[1] * tau[1][x] + uvw[2] * tau[2][x] + lam * D[3][x];
+        double Jb = 0.0;
+        for (int a = 0; a < 4; a++)
+            for (int x = 0; x < 3; x++) Jb += Db[a][x] * D[a][x];
+        for (int d = 0; d < 3; d++) {
+            const double fb[4] = {Fvb[d][t], Fvb[d][t + vpl], Fvb[d][t + 2 * vpl], Fvb[d][t + 3 * vpl]};
+            for (int x = 0; x < 3; x++) {
+                double b = fb[0] * tau[x][0] + fb[1] * tau[x][1] + fb[2] * tau[x][2] + fb[3] * E[x];
+                for (int a = 0; a < 4; a++) b += Db[a][x] * G[a][d] * Jac;
+                mbar.m[3 * d + x][c] += mbar.scale * b;  // one thread per cell, after the sweeps
+            }
+        }
+        mbar.J[c] += mbar.scale * Jb / Jac;
+    }
+}
+
+// J-bar += scale sum_n Lb L / J at interior cells (L = J D: the direct dependence on J)
+__global__ void k_jbar(const DevParams P, const double* __restrict__ Lb, const double* __restrict__ L,
+                       const double* __restrict__ J, double* Jbar, double scale) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)P.nx * P.ny * P.nz) return;
+    int i, j, k;
+    split3(t, P.dnx, P.dny, i, j, k);
+    const long long c = lin3(P, i + NG, j + NG, k + NG), pl = P.plane;
+    double s = 0.0;
+    for (int n = 0; n < 5; n++) s += Lb[c + n * pl] * L[c + n * pl];
+    Jbar[c] += scale * s / J[c];
 }
 
 // Transpose of the CD4 gradients: G[c'] = c1 (f[c'-2] - f[c'+2]) + c2 (f[c'-1] - f[c'+1]),
@@ -520,12 +575,23 @@ cudaError_t launch_sweep_vjp(int dir, const AdjArgs& a, cudaStream_t st) {
 static unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 cudaError_t launch_viscous_vjp(const DevParams& P, const double* Q, const double* const m[9], const double* J,
-                               const double* Lb, double* Fvb[3], double* gb, double* Qb, cudaStream_t st) {
+                               const double* Lb, double* Fvb[3], double* gb, double* Qb, cudaStream_t st,
+                               double* const mbar[9], double* Jbar, double mscale) {
     const long long nv = (long long)(P.nxt - 4) * (P.nyt - 4) * (P.nzt - 4);
+    MetricBar mb;
+    for (int n = 0; n < 9; n++) mb.m[n] = mbar ? mbar[n] : nullptr;
+    mb.J = Jbar;
+    mb.scale = mscale;
     k_visc_fvb<<<blocks_for(nv, 256), 256, 0, st>>>(P, Lb, J, Fvb[0], Fvb[1], Fvb[2]);
     k_visc_vjp<<<blocks_for(nv, 128), 128, 0, st>>>(P, Q, m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], J,
-                                                     Fvb[0], Fvb[1], Fvb[2], gb, Qb);
+                                                     Fvb[0], Fvb[1], Fvb[2], gb, Qb, mb);
     k_visc_gather<<<blocks_for(P.plane, 256), 256, 0, st>>>(P, gb, Qb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_jbar(const DevParams& P, const double* Lb, const double* L, const double* J, double* Jbar,
+                        double mscale, cudaStream_t st) {
+    k_jbar<<<blocks_for((long long)P.nx * P.ny * P.nz, 256), 256, 0, st>>>(P, Lb, L, J, Jbar, mscale);
     return cudaGetLastError();
 }
 

@@ -154,6 +154,20 @@ class Flame3D:
         self._profile_bars = getattr(self, "_profile_bars", {})
         self._profile_bars[face] = prof_bar
 
+    def set_metrics_cotangent(self, metrics_bar: list[torch.Tensor] | None, J_bar: torch.Tensor | None = None):
+        """Accumulate dJ/d(metrics) and dJ/dJ into the nine arrays and J_bar during the
+        adjoint calls (None stops)."""
+        if metrics_bar is None:
+            self._check(self.lib.f3d_set_metrics_cotangent(self._h, None, None, self._stream()))
+            self._metric_bars = None
+            return
+        if len(metrics_bar) != 9:
+            raise ValueError("need nine metric cotangent arrays")
+        arr = (C.c_void_p * 9)(*[self._ptr(m, 1) for m in metrics_bar])
+        self._check(self.lib.f3d_set_metrics_cotangent(self._h, C.cast(arr, C.c_void_p), self._ptr(J_bar, 1),
+                                                       self._stream()))
+        self._metric_bars = (list(metrics_bar), J_bar, arr)
+
     def profile_shape(self, face: int) -> tuple[int, int, int]:
         """(5, Tb, Ta) of an inflow-profile face: its transverse extent including ghosts."""
         nxt, nyt, nzt = self.shape3[2], self.shape3[1], self.shape3[0]

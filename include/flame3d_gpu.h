@@ -293,6 +293,15 @@ int f3d_rk3_steps_f32(f3d_ctx* ctx, int nsteps, float dt, float* U, float* Un, f
  * in the reference. */
 int f3d_set_inflow_profile_cotangent(f3d_ctx* ctx, int face, double* prof_bar, f3d_stream stream);
 
+/* Let the adjoint calls also accumulate the cotangents of the nine metrics and of J (the
+ * arrays of f3d_set_metrics, same layout; ghost cells included) into metrics_bar / jac_bar:
+ * after a backward pass they hold dJ/d(metrics) and dJ/dJ, so a grid parameter's gradient
+ * is their dot product with the metrics' derivative in it. The caller zeroes them first;
+ * nullptr stops the accumulation. Costs one RHS more per step VJP (the forward RHS of the
+ * last stage state, for the J-term) and 10 arrays of scratch. No counterpart in the
+ * reference. */
+int f3d_set_metrics_cotangent(f3d_ctx* ctx, double* const metrics_bar[9], double* jac_bar, f3d_stream stream);
+
 /* Ubar = (dL/dU)^T Lbar at interior cells (ghost cells of Ubar are zeroed), where
  * L(U) = RHS(ghost-filled c2Prim(U)) is the right-hand side as a function of the interior
  * conserved state. Branches (hybrid scheme choice, minmod, sign splits, c2Prim clamps)

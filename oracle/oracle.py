@@ -293,6 +293,20 @@ def rk3_32(P, nsteps, dt, U, Un, Q, m, J):
     lib().orc32_rk3(C.byref(P), C.c_int(nsteps), C.c_float(dt), _p(U), _p(Un), _p(Q), _pp(m), _p(J))
 
 
+def rhs_jvp_m(P, Q, m, dm, J, dJ):
+    """(dUdt, d dUdt) of the RHS at fixed Q along the metric tangents (dm, dJ), forward mode."""
+    r, dr = zeros(P, 5), zeros(P, 5)
+    lib().orc_rhs_jvp_m(C.byref(P), _p(Q), _pp(m), _pp(dm), _p(J), _p(dJ), _p(r), _p(dr))
+    return r, dr
+
+
+def rk3_jvp_m(P, nsteps, dt, U0, m, dm, J, dJ):
+    u, du = zeros(P, 5), zeros(P, 5)
+    lib().orc_rk3_jvp_m(C.byref(P), C.c_int(nsteps), C.c_double(dt), _p(U0), _pp(m), _pp(dm), _p(J), _p(dJ),
+                        _p(u), _p(du))
+    return u, du
+
+
 def rhs_jvp_u(P, U, dU, m, J):
     """(dUdt, d dUdt) of U -> c2Prim -> ghost fill -> RHS, forward mode."""
     r, dr = zeros(P, 5), zeros(P, 5)

@@ -272,6 +272,58 @@ void orc_rk3_jvp_u(const f3d_params* P, int nsteps, double dt, const double* U0,
     }
 }
 
+// JVP of the RHS with respect to the metrics and J at a fixed ghost-filled Q (the metric
+// tangents dm[9], dJ seed the dual numbers; |A| and A/|A| follow inside the solver).
+void orc_rhs_jvp_m(const f3d_params* P, const double* Q, const double* const m[9], const double* const dm[9],
+                   const double* J, const double* dJ, double* dUdt, double* d_dUdt) {
+    Grid g(*P);
+    const size_t nc = g.ncell();
+    using D = Dual;
+    std::vector<D> Qd(nc * 6), Rd(nc * 5, D(0.0));
+    for (size_t i = 0; i < nc * 6; i++) Qd[i] = D(Q[i]);
+    std::vector<D> md[9], Jd(nc);
+    const D* mp[9];
+    for (int a = 0; a < 9; a++) {
+        md[a].resize(nc);
+        for (size_t i = 0; i < nc; i++) md[a][i] = D(m[a][i], dm[a][i]);
+        mp[a] = md[a].data();
+    }
+    for (size_t i = 0; i < nc; i++) Jd[i] = D(J[i], dJ[i]);
+    Solver<D, D> s(*P, mp, Jd.data());
+    s.rhs(Qd.data(), Rd.data());
+    for (size_t i = 0; i < nc * 5; i++) {
+        dUdt[i] = Rd[i].v;
+        d_dUdt[i] = Rd[i].d;
+    }
+}
+
+// JVP of nsteps RK3 steps from a fixed U0 with respect to the metrics and J.
+void orc_rk3_jvp_m(const f3d_params* P, int nsteps, double dt, const double* U0, const double* const m[9],
+                   const double* const dm[9], const double* J, const double* dJ, double* U_out, double* dU_out) {
+    Grid g(*P);
+    const size_t nc = g.ncell();
+    using D = Dual;
+    std::vector<D> Ud(nc * 5), Und(nc * 5, D(0.0)), Qd(nc * 6, D(0.0));
+    for (size_t i = 0; i < nc * 5; i++) Ud[i] = D(U0[i]);
+    std::vector<D> md[9], Jd(nc);
+    const D* mp[9];
+    for (int a = 0; a < 9; a++) {
+        md[a].resize(nc);
+        for (size_t i = 0; i < nc; i++) md[a][i] = D(m[a][i], dm[a][i]);
+        mp[a] = md[a].data();
+    }
+    for (size_t i = 0; i < nc; i++) Jd[i] = D(J[i], dJ[i]);
+    c2prim<D>(*P, Ud.data(), Qd.data());
+    fill_ghosts<D>(*P, Qd.data(), Ud.data());
+    Solver<D, D> s(*P, mp, Jd.data());
+    for (int t = 0; t < nsteps; t++)
+        for (int st = 1; st <= 3; st++) s.rk3_stage(st, D(dt), Ud.data(), Und.data(), Qd.data());
+    for (size_t i = 0; i < nc * 5; i++) {
+        U_out[i] = Ud[i].v;
+        dU_out[i] = Ud[i].d;
+    }
+}
+
 // ---- exact operation counts ------------------------------------------------------------
 // Runs the RHS on counting scalars and returns the number of floating-point operations by
 // class: out[0] add/sub, out[1] mul, out[2] div, out[3] sqrt, out[4] compare/abs/max.
