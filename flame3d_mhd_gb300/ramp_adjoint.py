@@ -19,11 +19,14 @@ force on the wall is -p J^-1 grad eta):
 Gradients (FP64 state, component-wise hybrid reconstruction, Steger-Warming):
   - dJ/ds from the adjoint: the step VJPs carry the ghost cotangents of the inflow face into
     the profile (f3d_set_inflow_profile_cotangent), dJ/ds_j = sum_k profile_bar[u, k, j] u_0;
-  - dJ/dtheta = sum over steps and stages <Lbar_s, dL/dtheta at V_s> + the objective's own
-    area term, with the stage states V_s and RHS cotangents Lbar_s of every step VJP
-    (f3d_rk3_step_vjp_stages) and dL/dtheta at fixed V_s by a central difference of the RHS
-    over the metrics of the grids at theta +- eta (the metric computation and the grid
-    generator are differentiated by that difference, not by VJP kernels).
+  - dJ/dtheta (--angle-method adjoint, the default) = <metrics_bar, dm/dtheta> + <J_bar,
+    dJ/dtheta> + the objective's own area term: the step VJPs accumulate the cotangents of
+    the nine metrics and J (f3d_set_metrics_cotangent), and the metrics' derivative in theta
+    is a central difference of the grid generator and the metric kernel over theta +- eta
+    (once, not per step). --angle-method fd instead forms sum over steps and stages
+    <Lbar_s, dL/dtheta at V_s> from the stage states V_s and RHS cotangents Lbar_s of every
+    step VJP (f3d_rk3_step_vjp_stages), with dL/dtheta at fixed V_s a central difference of
+    the RHS over the two metric sets (6 RHS per step): an independent check of the first.
 The reversal holds at most `slots` trajectory states, sized from the memory left under
 `--hbm-gb` after the solver contexts (multi-level checkpointing, adjoint.plan).
 Checks: central differences of J in FP64 along seeded unit directions of s and in theta.
@@ -181,7 +184,12 @@ def main(argv=None):
                          "smooth in the parameters); weno5: one reconstruction everywhere")
     ap.add_argument("--hbm-gb", type=float, default=180.0, help="memory budget of the whole run")
     ap.add_argument("--slots", type=int, default=0, help="trajectory states held (0: from --hbm-gb)")
-    ap.add_argument("--eta", type=float, default=1e-3, help="angle step (degrees) of the RHS difference in theta")
+    ap.add_argument("--angle-method", choices=("adjoint", "fd"), default="adjoint",
+                    help="adjoint: metric and Jacobian cotangents from the VJP kernels, dotted with the metrics' "
+                         "derivative in theta; fd: per stage, a central difference of the RHS over the metric "
+                         "sets at theta +- eta (6 RHS per step)")
+    ap.add_argument("--eta", type=float, default=1e-3,
+                    help="angle step (degrees) of the metrics' (adjoint) or the RHS's (fd) difference in theta")
     ap.add_argument("--fd-dirs", type=int, default=1, help="seeded directions of s checked by central differences")
     ap.add_argument("--fd-h", type=str, default="1e-6", help="difference step(s) of s (comma-separated)")
     ap.add_argument("--fd-angle-h", type=str, default="1e-3", help="difference step(s) of theta in degrees")
@@ -291,22 +299,36 @@ def main(argv=None):
         torch.cuda.synchronize()
         sink_s[0] += time.perf_counter() - t
 
+    mbar = Jbar = None
+    if a.angle_method == "adjoint":  # metric and Jacobian cotangents accumulated by the VJPs
+        mbar, Jbar = [s.field(1) for _ in range(9)], s.field(1)
+        s.set_metrics_cotangent(mbar, Jbar)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     with side_stream():
         UN, U0bar, st = trajectory_gradient(s, R.U0, R.dt, R.N, slots, final_grad=lambda U: source(R.N, U),
-                                            source=source, observe=observe, stage_sink=stage_sink)
+                                            source=source, observe=observe,
+                                            stage_sink=stage_sink if a.angle_method == "fd" else None)
     torch.cuda.synchronize()
     t_grad = time.perf_counter() - t0
     out["reversal"] = st
     del UN, U0bar
     out["memory"]["peak_allocated_gb"] = torch.cuda.max_memory_allocated() / 1e9
     s.set_inflow_profile_cotangent(0, None)
+    if mbar is not None:
+        # dJ/dtheta = <metrics-bar, dm/dtheta> + <J-bar, dJ/dtheta>, the metric derivatives by
+        # a central difference of the grid generator and the metric kernel over +- eta
+        s.set_metrics_cotangent(None)
+        for k in range(9):
+            theta["stages"] += torch.dot(mbar[k].view(-1), ((mp[0][k] - mm[0][k]) / (2 * a.eta)).view(-1))
+        theta["stages"] += torch.dot(Jbar.view(-1), ((mp[1] - mm[1]) / (2 * a.eta)).view(-1))
+        del mbar, Jbar
     u0 = R.prof0[1, :, R.rows]
     dJds = (pbar[1, :, R.rows] * u0).sum(dim=0)
     dJdtheta = float(theta["stages"] + theta["area"])
     out["gradient"] = {"dJds_norm": float(dJds.norm()), "dJds_first_rows": dJds[:4].tolist(),
-                       "dJdtheta_deg": dJdtheta, "dJdtheta_area_term": float(theta["area"])}
+                       "dJdtheta_deg": dJdtheta, "dJdtheta_area_term": float(theta["area"]),
+                       "angle_method": a.angle_method}
     # the angle's stage differences (6 RHS per step) are timed apart: without them the
     # reversal is the profile (and initial-state) gradient alone
     out["cost"] = {"gradient_s": t_grad, "angle_stage_differences_s": sink_s[0],

@@ -11,7 +11,9 @@ Tolerances, written per check:
   atomics ordered differently); the dt-derivative identity to 1e-7 (central difference);
 - reversal schedules: gradients to 1e-12 relative (same step VJPs, atomics order);
 - windowed objective: adjoint against central differences to 1e-5 relative (h = 1e-4 for
-  the scalings, 1e-3 degrees for the angle; FP64 forward runs)."""
+  the scalings, 1e-3 degrees for the angle; FP64 forward runs); the angle gradient from the
+  metric cotangents and from per-stage RHS differences within 1e-6 of each other (both
+  difference the metrics over +- 1e-3 degrees, truncation ~1e-7)."""
 import numpy as np
 import pytest
 import torch
@@ -195,6 +197,12 @@ def test_windowed_wall_force_gradient_vs_central_differences(gpu_lib):
                              "--fd-angle-h", "1e-3", "--eta", "1e-3", "--mixed", "0"])
     (ch,) = out["checks"]
     assert ch["param"] == "theta_deg" and ch["rel_diff"] <= 1e-5, ch
+    # the two ways to the angle gradient: metric cotangents, and per-stage RHS differences
+    fd = ramp_adjoint.main(["--nx", "48", "--ny", "24", "--nz", "8", "--first-cell", "1e-2", "--steps", "8",
+                            "--window", "3", "--slots", "4", "--force", "x", "--fd-dirs", "0", "--fd-angle-h", "",
+                            "--eta", "1e-3", "--mixed", "0", "--angle-method", "fd"])
+    g_adj, g_fd = out["gradient"]["dJdtheta_deg"], fd["gradient"]["dJdtheta_deg"]
+    assert abs(g_adj - g_fd) <= 1e-6 * abs(g_fd), (g_adj, g_fd)
 
 
 def test_lean_stage_cache_gives_the_same_step_vjp(gpu_lib, ramp):
