@@ -11,18 +11,23 @@ import numpy as np
 NG = 4
 
 
-def extend_ghosts(x: np.ndarray, y: np.ndarray, z: np.ndarray,
-                  dtype=np.float64) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-    """Fill the ghost layers of interior coordinates as SCU-benchmark/readfort.jl:34-95 does.
+def extend_ghosts(x: np.ndarray, y: np.ndarray, z: np.ndarray, dtype=np.float64,
+                  rule: str = "readfort") -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Fill the ghost layers of interior coordinates as SCU-benchmark/readfort.jl:34-95 does
+    (rule="readfort", the grid pipeline), or as the solver's `extrapolation` does after
+    reading mesh.h5 (rule="solver", solver.jl:682-826, one rank).
 
     Point reflection about the first / last interior cell (x_g = 2 x_b - x_mirror) on the
-    xi and eta faces for all three coordinates, except that z is copied unreflected across
-    the eta faces (readfort.jl:48-58); parallelogram completion x = x[i, b] + x[b, j] - x[b, b]
-    in the four xi-eta edge regions (readfort.jl:61-83); then point reflection on the zeta
-    faces over the full xi-eta extent (readfort.jl:85-95). Interior values are untouched.
+    xi and eta faces for all three coordinates, except that readfort.jl copies z unreflected
+    across the eta faces (readfort.jl:48-58; solver.jl:731-751 reflects it too);
+    parallelogram completion x = x[i, b] + x[b, j] - x[b, b] in the four xi-eta edge regions
+    (readfort.jl:61-83, solver.jl:753-795); then point reflection on the zeta faces over the
+    full xi-eta extent (readfort.jl:85-95, solver.jl:797-823). Interior values are untouched.
     Returns new arrays of `dtype` (arithmetic in that type: np.float32 repeats the Float32
-    arrays of readfort.jl); inputs are (Nz+8, Ny+8, Nx+8) with the interior filled.
+    arrays of the reference); inputs are (Nz+8, Ny+8, Nx+8) with the interior filled.
     """
+    if rule not in ("readfort", "solver"):
+        raise ValueError(f"rule {rule!r}: 'readfort' or 'solver'")
     X, Y, Z = (np.array(a, dtype=dtype, copy=True) for a in (x, y, z))
     nzt, nyt, nxt = X.shape
     nx, ny = nxt - 2 * NG, nyt - 2 * NG
@@ -37,8 +42,8 @@ def extend_ghosts(x: np.ndarray, y: np.ndarray, z: np.ndarray,
             A[ki, ji, g] = 2 * A[ki, ji, lo_i] - A[ki, ji, 2 * lo_i - g]
             gh = hi_i + 1 + g
             A[ki, ji, gh] = 2 * A[ki, ji, hi_i] - A[ki, ji, 2 * hi_i - gh]
-    for A, reflect in ((X, True), (Y, True), (Z, False)):
-        # eta faces (readfort.jl:48-58); z is copied from the mirror cell
+    for A, reflect in ((X, True), (Y, True), (Z, rule == "solver")):
+        # eta faces (readfort.jl:48-58: z is copied from the mirror cell)
         for g in range(NG):
             gh = hi_j + 1 + g
             if reflect:

@@ -11,12 +11,13 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import sys
 
 import numpy as np
 import torch
 
-from . import cases
+from . import cases, files
 from .abi import PREC_MIXED
 from .solver import Flame3D, side_stream
 
@@ -49,17 +50,23 @@ def skin_friction(Q: np.ndarray, x: np.ndarray, y: np.ndarray, wall: dict) -> np
 
 
 def run(case: dict, precision: int, steps: int, dev: str = "cuda", perturb: float = 0.0,
-        seed: int = 7) -> tuple[np.ndarray, float]:
+        seed: int = 7, out_dir: str | None = None) -> tuple[np.ndarray, float]:
     """Advance `steps` SSP-RK3 steps (graph-captured) and return (Q, ms per step). With
     perturb > 0 the initial interior primitive state is multiplied by 1 + perturb * N(0,1)
     (seeded): an FP64 run perturbed at FP32 rounding level measures how far the flow itself
-    amplifies last-bit differences (the yardstick for the mixed form's deviation)."""
+    amplifies last-bit differences (the yardstick for the mixed form's deviation).
+    With `out_dir` the reference's files are written there: metrics.h5 and mesh.h5 from the
+    device metrics and the grid, and after the last step PLT/plt-<steps>.h5 + .xmf and
+    CHK/chk-<steps>.h5 from the primitives of the final state and their shock sensor."""
     from .cases import params_copy
     P = params_copy(case["params"], precision=precision)
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     s = Flame3D(P)
     ms, J = s.compute_metrics(to(case["x"]), to(case["y"]), to(case["z"]))
     s.set_metrics(ms, J)
+    if out_dir:
+        files.write_metrics(os.path.join(out_dir, "metrics.h5"), ms, J)
+        files.write_mesh(os.path.join(out_dir, "mesh.h5"), case["x"], case["y"], case["z"])
     s.set_inflow_profile(0, to(case["profile"]))
     Q0 = case["Q"]
     if perturb > 0.0:
@@ -79,6 +86,12 @@ def run(case: dict, precision: int, steps: int, dev: str = "cuda", perturb: floa
         e1.synchronize()
     s.check_finite(U)
     out = Q.cpu().numpy()
+    if out_dir:
+        Qf = s.q_from_u(U)
+        phi = s.field(1)
+        s.shockSensor(phi, Qf)
+        files.plotFile_xdmf(out_dir, steps, Qf, phi, case["dt"])
+        files.checkpointFile(out_dir, steps, Qf)
     s.close()
     return out, e0.elapsed_time(e1) / max(steps - 1, 1)
 
@@ -107,9 +120,13 @@ def main(argv=None):
     ap.add_argument("--yardstick", type=float, default=1e-8,
                     help="relative perturbation of an extra FP64 run (0: skip it)")
     ap.add_argument("--save", default="", help="write the wall arrays to this .npz")
+    ap.add_argument("--out", default="", help="write metrics.h5, mesh.h5 and the FP64 run's plot and "
+                                              "checkpoint files (the reference's HDF5 layouts) here")
     a = ap.parse_args(argv)
     case = cases.compression_ramp(a.nx, a.ny, a.nz, first_cell=a.first_cell)
-    Q64, t64 = run(case, 0, a.steps)
+    if a.out:
+        os.makedirs(a.out, exist_ok=True)
+    Q64, t64 = run(case, 0, a.steps, out_dir=a.out or None)
     Q32, t32 = run(case, PREC_MIXED, a.steps)
     Qpt = run(case, 0, a.steps, perturb=a.yardstick)[0] if a.yardstick > 0 else None
     cells = a.nx * a.ny * a.nz

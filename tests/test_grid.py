@@ -10,9 +10,10 @@ from flame3d_mhd_gb300.grid import NG, compression_ramp_grid, extend_ghosts, tan
 from oracle import oracle as orc
 
 
-def _readfort_loops(x, y, z):
+def _readfort_loops(x, y, z, solver=False):
     """readfort.jl:34-95 cell by cell, 1-based indices as in the Julia source, on arrays
-    indexed [i, j, k] (Julia order); returns new arrays."""
+    indexed [i, j, k] (Julia order); returns new arrays. solver=True: solver.jl:682-826 (one
+    rank), which differs only in reflecting z across the eta faces (solver.jl:731-751)."""
     x, y, z = x.copy(), y.copy(), z.copy()
     Nxt, Nyt, Nzt = x.shape
     Nx, Ny, Nz = Nxt - 2 * NG, Nyt - 2 * NG, Nzt - 2 * NG
@@ -33,11 +34,17 @@ def _readfort_loops(x, y, z):
             for j in range(1, NG + 1):
                 S(x, i, j, k, 2 * A(x, i, NG + 1, k) - A(x, i, 2 * NG + 2 - j, k))
                 S(y, i, j, k, 2 * A(y, i, NG + 1, k) - A(y, i, 2 * NG + 2 - j, k))
-                S(z, i, j, k, A(z, i, 2 * NG + 2 - j, k))
+                if solver:
+                    S(z, i, j, k, 2 * A(z, i, NG + 1, k) - A(z, i, 2 * NG + 2 - j, k))
+                else:
+                    S(z, i, j, k, A(z, i, 2 * NG + 2 - j, k))
             for j in range(Ny + NG + 1, Nyt + 1):
                 S(x, i, j, k, 2 * A(x, i, Ny + NG, k) - A(x, i, 2 * NG + 2 * Ny - j, k))
                 S(y, i, j, k, 2 * A(y, i, Ny + NG, k) - A(y, i, 2 * NG + 2 * Ny - j, k))
-                S(z, i, j, k, A(z, i, 2 * NG + 2 * Ny - j, k))
+                if solver:
+                    S(z, i, j, k, 2 * A(z, i, Ny + NG, k) - A(z, i, 2 * NG + 2 * Ny - j, k))
+                else:
+                    S(z, i, j, k, A(z, i, 2 * NG + 2 * Ny - j, k))
         for jr, jb in ((range(Ny + NG + 1, Nyt + 1), Ny + NG), (range(1, NG + 1), NG + 1)):
             for ir, ib in ((range(1, NG + 1), NG + 1), (range(Nx + NG + 1, Nxt + 1), Nx + NG)):
                 for j in jr:
@@ -55,7 +62,8 @@ def _readfort_loops(x, y, z):
     return x, y, z
 
 
-def test_extend_ghosts_matches_readfort_loops():
+@pytest.mark.parametrize("rule", ["readfort", "solver"])
+def test_extend_ghosts_matches_readfort_loops(rule):
     rng = np.random.default_rng(3)
     shape = (6 + 2 * NG, 5 + 2 * NG, 7 + 2 * NG)  # (Nz+8, Ny+8, Nx+8)
     xyz = []
@@ -63,9 +71,9 @@ def test_extend_ghosts_matches_readfort_loops():
         a = np.zeros(shape)
         a[NG:-NG, NG:-NG, NG:-NG] = rng.standard_normal((6, 5, 7))
         xyz.append(a)
-    got = extend_ghosts(*xyz)
+    got = extend_ghosts(*xyz, rule=rule)
     # the loops work on Julia-ordered [i, j, k] views
-    ref = _readfort_loops(*[a.transpose(2, 1, 0) for a in xyz])
+    ref = _readfort_loops(*[a.transpose(2, 1, 0) for a in xyz], solver=rule == "solver")
     for g, r in zip(got, ref):
         assert np.array_equal(g, r.transpose(2, 1, 0))
 
