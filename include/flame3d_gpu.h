@@ -38,7 +38,7 @@ extern "C" {
 #define F3D_ERR_ALIGN 2        /* a pointer is not 16-byte aligned                      */
 #define F3D_ERR_CUDA 3         /* a CUDA runtime call failed                            */
 #define F3D_ERR_NONFINITE 4    /* a NaN/Inf was found in the checked state              */
-#define F3D_ERR_UNSUPPORTED 5  /* valid request that this build does not implement       */
+#define F3D_ERR_UNSUPPORTED 5  /* valid request that the library does not implement      */
 #define F3D_ERR_STATE 6        /* call order violated (e.g. metrics not set)            */
 #define F3D_ERR_TOO_LARGE 7    /* the grid needs more scratch than f3d_rhs_noalloc holds */
 
