@@ -245,3 +245,69 @@ def test_solution_files(tmp_path):
     assert np.array_equal(files.read_checkpoint(p), Q.astype(np.float32))
     p = files.averageFile(out, 800, Q)
     assert np.array_equal(h5.read(p)["avg"], Q[(slice(None),) + I].astype(np.float32))
+
+
+def test_lookup3_published_vectors():
+    # Bob Jenkins' lookup3.c driver values for hashlittle
+    s = b"Four score and seven years ago"
+    assert h5.lookup3(b"", 0) == 0xDEADBEEF
+    assert h5.lookup3(b"", 0xDEADBEEF) == 0xBD5B7DDE
+    assert h5.lookup3(s, 0) == 0x17770551
+    assert h5.lookup3(s, 1) == 0xCD628161
+
+
+@pytest.mark.parametrize("new_format", [False, True])
+@pytest.mark.parametrize("links,n", [(False, 3), (True, 3), (True, 12)])
+def test_link_groups_and_version2_headers(tmp_path, new_format, links, n):
+    """Groups as link messages (compact, and dense in a fractal heap indexed by link-name
+    hashes), version-2 superblock and object headers, the single-chunk and implicit chunk
+    indexes; every checksum is verified on reading."""
+    rng = np.random.default_rng(5)
+    d = {f"dξd{i:02d}": rng.standard_normal((3, 4, 5)).astype(np.float32) for i in range(n)}
+    d.update(NG=np.int64(4), Q=rng.standard_normal((6, 5, 4, 3)), c=rng.standard_normal((9, 10, 11)),
+             e=rng.standard_normal((9, 10, 11)).astype(np.float32))
+    p = h5.write(str(tmp_path / "n.h5"), d, chunks={"Q": (6, 5, 4, 3), "c": (4, 5, 6), "e": (4, 5, 6)},
+                 links=links, new_format=new_format)
+    with h5.H5File(p) as f:
+        assert f.version == (2 if new_format else 0) and f.eof == os.path.getsize(p)
+        msgs = dict(f.messages(f.root[1]))
+        if links:
+            heap = struct.unpack("<Q", msgs[h5.M_LINK_INFO][2:10])[0]
+            assert (heap != h5.UNDEF) == (len(d) > h5.MAX_COMPACT_LINKS)
+        else:
+            assert h5.M_SYMBOL_TABLE in msgs
+        kinds = {k: f.dataset(k).layout[0] for k in ("Q", "c")}
+        assert kinds == ({"Q": "single", "c": "implicit"} if new_format else {"Q": "chunked", "c": "chunked"})
+        r = {k: f[k] for k in f.keys()}
+    assert sorted(r) == sorted(d)
+    for k, v in d.items():
+        assert np.array_equal(r[k], np.asarray(v)), k
+    # filtered: single chunk with its filtered size, several chunks through the v1 B-tree
+    p = h5.write(str(tmp_path / "z.h5"), d, chunks={"Q": (6, 5, 4, 3), "c": (4, 5, 6)}, deflate=3, shuffle=True,
+                 links=links, new_format=new_format)
+    with h5.H5File(p) as f:
+        assert f.dataset("c").layout[0] == "chunked"
+        assert f.dataset("Q").layout[0] == ("single" if new_format else "chunked")
+        assert np.array_equal(f["Q"], d["Q"]) and np.array_equal(f["c"], d["c"])
+
+
+def test_checksums_catch_damage(tmp_path):
+    d = {f"x{i:02d}": np.arange(i + 2, dtype=np.float64) for i in range(12)}
+    p = h5.write(str(tmp_path / "d.h5"), d, links=True, new_format=True)
+    raw = open(p, "rb").read()
+    with h5.H5File(p) as f:
+        assert f.keys() == sorted(d, key=lambda s: h5.lookup3(s.encode()))  # the name index's hash order
+    for sig in (b"OHDR", b"FRHP", b"BTHD", b"BTLF"):
+        bad = bytearray(raw)
+        at = raw.index(sig) + 6
+        bad[at] ^= 0x40
+        q = tmp_path / "bad.h5"
+        q.write_bytes(bytes(bad))
+        with pytest.raises(ValueError):
+            with h5.H5File(str(q)) as f:
+                [f[k] for k in f.keys()]
+    bad = bytearray(raw)
+    bad[20] ^= 1  # inside the version-2 superblock
+    (tmp_path / "sb.h5").write_bytes(bytes(bad))
+    with pytest.raises(ValueError):
+        h5.H5File(str(tmp_path / "sb.h5"))
