@@ -21,6 +21,8 @@ import numpy as np
 import torch
 
 from . import cases
+from .abi import PREC_REF32
+from .cases import params_copy
 from .solver import Flame3D
 
 
@@ -37,6 +39,19 @@ def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: i
     P.precision = precision
     P.scheme = scheme
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    if precision == PREC_REF32:
+        # the reference's Float32 arrays: metrics computed in FP64 by an FP64 context, then
+        # Float32 copies of them and of the state (as the reference reads metrics.h5)
+        g = Flame3D(params_copy(P, precision=0))
+        ms, J = g.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
+        g.close()
+        s = Flame3D(P)
+        s.set_metrics([m.float() for m in ms], J.float())
+        Q = dev(c["Q"]).float()
+        U = s.field(5)
+        s.prim2c(U, Q)
+        s.fillGhost(Q, U)
+        return s, c, U, Q
     s = Flame3D(P)
     ms, J = s.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
     s.set_metrics(ms, J)
@@ -56,7 +71,7 @@ def main(argv=None):
     ap.add_argument("--ny", type=int, default=64)
     ap.add_argument("--nz", type=int, default=64)
     ap.add_argument("--character", type=int, default=1)
-    ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--precision", type=int, default=0, help="0 FP64, 1 mixed, 2 the reference's Float32 form")
     ap.add_argument("--scheme", type=int, default=0, help="0 FDM, 1 FVM eigen, 2 FVM component-wise")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--step", action="store_true", help="profile_step instead of rhs (per-kernel event times)")
