@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <string>
 #include <type_traits>
 
@@ -657,7 +658,8 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
         std::fprintf(stderr, "f3d_create: %s\n", why.c_str());
         return rc;
     }
-    f3d_ctx* ctx = new f3d_ctx();
+    f3d_ctx* ctx = new (std::nothrow) f3d_ctx();  // no exception crosses the C ABI
+    if (!ctx) return F3D_ERR_CUDA;
     ctx->params = *p;
     ctx->dp = make_dev_params(*p);
     if (cudaGetDevice(&ctx->device) != cudaSuccess) { delete ctx; return F3D_ERR_CUDA; }

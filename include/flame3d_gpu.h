@@ -36,7 +36,7 @@ extern "C" {
 #define F3D_OK 0
 #define F3D_ERR_ARG 1          /* invalid argument (null pointer, bad dims, bad enum)   */
 #define F3D_ERR_ALIGN 2        /* a pointer is not 16-byte aligned                      */
-#define F3D_ERR_CUDA 3         /* a CUDA runtime call failed                            */
+#define F3D_ERR_CUDA 3         /* a CUDA runtime call or a host allocation failed       */
 #define F3D_ERR_NONFINITE 4    /* a NaN/Inf was found in the checked state              */
 #define F3D_ERR_UNSUPPORTED 5  /* valid request that the library does not implement      */
 #define F3D_ERR_STATE 6        /* call order violated (e.g. metrics not set)            */
