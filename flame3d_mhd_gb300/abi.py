@@ -22,6 +22,7 @@ NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 SPLIT_SW, SPLIT_LF, SPLIT_VL, SPLIT_AUSM = 0, 1, 2, 3
 SPLIT_NAMES = {"SW": SPLIT_SW, "LF": SPLIT_LF, "VL": SPLIT_VL, "AUSM": SPLIT_AUSM}
 PREC_FP64, PREC_MIXED, PREC_REF32 = 0, 1, 2
+METRICS_READFORT, METRICS_PARSE_MESH = 0, 1  # coefficient sets of f3d_compute_metrics_f32
 SCHEME_FDM, SCHEME_FVM_EIGEN, SCHEME_FVM_CONS = 0, 1, 2
 FILTER_NONE, FILTER_LINEAR, FILTER_NONLINEAR = 0, 1, 2
 LES_NONE, LES_SMAGORINSKY, LES_WALE = 0, 1, 2
@@ -137,6 +138,7 @@ def load() -> C.CDLL:
         "f3d_set_inflow_profile_cotangent": (ip, [vp, ip, vp, vp]),
         "f3d_rk3_step_vjp_stages": (ip, [vp, C.c_double, vp, vp, vp, vp, vp, vp]),
         "f3d_set_metrics_f32": (ip, [vp, vp * 9, vp, vp]),
+        "f3d_compute_metrics_f32": (ip, [vp, vp, vp, vp, vp * 9, vp, ip, vp]),
         "f3d_set_metrics_cotangent": (ip, [vp, C.c_void_p, vp, vp]),
         "f3d_c2prim_f32": (ip, [vp, vp, vp, vp]),
         "f3d_prim2c_f32": (ip, [vp, vp, vp, vp]),
@@ -163,7 +165,7 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_set_coordinates", "f3d_filter", "f3d_local_dt", "f3d_debug_round_f32",
             "f3d_set_inflow_profile_cotangent", "f3d_rk3_step_vjp_stages", "f3d_set_metrics_f32",
             "f3d_c2prim_f32", "f3d_prim2c_f32", "f3d_fill_ghosts_f32", "f3d_rhs_f32", "f3d_rk3_stage_f32",
-            "f3d_rk3_steps_f32", "f3d_set_metrics_cotangent"]
+            "f3d_rk3_steps_f32", "f3d_set_metrics_cotangent", "f3d_compute_metrics_f32"]
 
 
 class F3DError(RuntimeError):

@@ -908,6 +908,21 @@ int f3d_set_metrics_f32(f3d_ctx* ctx, const float* const metrics[9], const float
     return F3D_OK;
 }
 
+int f3d_compute_metrics_f32(f3d_ctx* ctx, const float* x, const float* y, const float* z, float* const metrics[9],
+                            float* jac, int coefficients, f3d_stream stream) {
+    int rc = check_ctx32(ctx, false);
+    if (rc) return rc;
+    if (!metrics) return fail(ctx, F3D_ERR_ARG, "null metrics array");
+    if (coefficients != F3D_METRICS_READFORT && coefficients != F3D_METRICS_PARSE_MESH)
+        return fail(ctx, F3D_ERR_ARG, "coefficients must be F3D_METRICS_READFORT or F3D_METRICS_PARSE_MESH");
+    if ((rc = check_ptrs(ctx, {x, y, z, metrics[0], metrics[1], metrics[2], metrics[3], metrics[4], metrics[5],
+                              metrics[6], metrics[7], metrics[8], jac})))
+        return rc;
+    F3D_CUDA(ctx, launch_metrics32(ctx->dp, x, y, z, metrics, jac, coefficients == F3D_METRICS_PARSE_MESH,
+                                   (cudaStream_t)stream));
+    return F3D_OK;
+}
+
 int f3d_c2prim_f32(f3d_ctx* ctx, const float* U, float* Q, f3d_stream stream) {
     int rc = check_ctx32(ctx, false);
     if (rc || (rc = check_ptrs(ctx, {U, Q}))) return rc;

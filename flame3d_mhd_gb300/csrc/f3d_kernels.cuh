@@ -151,6 +151,13 @@ cudaError_t launch_viscous32(const DevParams& P, const float* Q, const float* co
                              float* Fvx, float* Fvy, float* Fvz, cudaStream_t st);
 
 // metrics from coordinates (k_metrics.cu)
+// nine metric outputs and J of the Float32 set-up metrics (k_metrics32)
+struct MetricOut32 {
+    float* m[9];
+    float* J;
+};
+cudaError_t launch_metrics32(const DevParams& P, const float* x, const float* y, const float* z,
+                             float* const m[9], float* J, bool f64coef, cudaStream_t st);
 cudaError_t launch_metrics(const DevParams& P, const double* x, const double* y, const double* z,
                            double* const m[9], double* J, cudaStream_t st);
 

@@ -184,13 +184,20 @@ class Flame3D:
         self._profiles = getattr(self, "_profiles", {})
         self._profiles[face] = prof  # keep the borrowed array alive
 
-    def compute_metrics(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor):
-        """Metrics and J from coordinates on the device (parse_mesh.jl:139-248)."""
+    def compute_metrics(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor,
+                        coefficients: int = abi.METRICS_READFORT):
+        """Metrics and J from coordinates on the device: in FP64 (parse_mesh.jl:139-248), or
+        in the Float32 form the reference's own Float32 set-up metrics with the coefficients
+        of readfort.jl or parse_mesh.jl (bitwise those of its metrics.h5)."""
         ms = [self.field(1) for _ in range(9)]
         J = self.field(1)
         arr = (C.c_void_p * 9)(*[self._ptr(m, 1) for m in ms])
-        self._check(self.lib.f3d_compute_metrics(self._h, self._ptr(x, 1), self._ptr(y, 1), self._ptr(z, 1), arr,
-                                                 self._ptr(J, 1), self._stream()))
+        xyz = (self._ptr(x, 1), self._ptr(y, 1), self._ptr(z, 1))
+        if self.ref32:
+            self._check(self.lib.f3d_compute_metrics_f32(self._h, *xyz, arr, self._ptr(J, 1), coefficients,
+                                                         self._stream()))
+        else:
+            self._check(self.lib.f3d_compute_metrics(self._h, *xyz, arr, self._ptr(J, 1), self._stream()))
         return ms, J
 
     # ---- utils.jl / boundary.jl ----------------------------------------------------------

@@ -277,6 +277,16 @@ int f3d_debug_round_f32(const double* in, float* out, long long n, f3d_stream st
  * inflow-profile faces, local time stepping, filters, LES, adjoint or finite-volume
  * scheme in this form (F3D_ERR_UNSUPPORTED at f3d_create). */
 int f3d_set_metrics_f32(f3d_ctx* ctx, const float* const metrics[9], const float* jac, f3d_stream stream);
+/* The Float32 metrics and J the reference's set-up writes to metrics.h5, from Float32
+ * coordinates with ghosts (Nxt,Nyt,Nzt): the CD6 / one-sided CD2 differences with Float32
+ * coefficients (F3D_METRICS_READFORT, SCU-benchmark/readfort.jl:103-181) or with Float64
+ * coefficients on Float32 differences, rounded to Float32 (F3D_METRICS_PARSE_MESH,
+ * parse_mesh.jl:138-248); every operation rounded to nearest in the Julia loops' order, so
+ * the results equal the reference's bit for bit. The outputs can go to f3d_set_metrics_f32. */
+#define F3D_METRICS_READFORT 0
+#define F3D_METRICS_PARSE_MESH 1
+int f3d_compute_metrics_f32(f3d_ctx* ctx, const float* x, const float* y, const float* z,
+                            float* const metrics[9], float* jac, int coefficients, f3d_stream stream);
 int f3d_c2prim_f32(f3d_ctx* ctx, const float* U, float* Q, f3d_stream stream);
 int f3d_prim2c_f32(f3d_ctx* ctx, const float* Q, float* U, f3d_stream stream);
 int f3d_fill_ghosts_f32(f3d_ctx* ctx, float* Q, float* U, f3d_stream stream);

@@ -174,3 +174,34 @@ def test_ref32_entry_errors(gpu_lib):
             Flame3D(params_copy(P, **kw))
         assert e.value.code == F3D_ERR_UNSUPPORTED
     s.close()
+
+
+@pytest.mark.parametrize("pipeline", ["readfort", "parse_mesh"])
+def test_set_up_metrics_bitwise(gpu_lib, tmp_path, pipeline):
+    """f3d_compute_metrics_f32 equals the reference's Float32 set-up metrics bit for bit:
+    the swept ramp through readfort.jl's pipeline (OCFD file, Float32, ghosts, metres) and the
+    flat plate of parse_mesh.jl."""
+    from flame3d_mhd_gb300 import meshgen
+    from flame3d_mhd_gb300.abi import METRICS_PARSE_MESH, METRICS_READFORT
+    from flame3d_mhd_gb300.grid import mesh_from_ocfd, write_ocfd_mesh
+    if pipeline == "readfort":
+        q = dict(nx=64, ny=24, nz=6, nprocs=1, nx_inlet=40, nx_corner=20, nx_buff=4, dx_inlet=0.9, lx_inlet=30.0,
+                 lx_corner=8.0, alfax_buff=1.05, sw_angle=20.0, comp_angle=24.0, high=6.0, hy_wall=0.01, lz=3.0)
+        path = str(tmp_path / "OCFD3d-Mesh.dat")
+        write_ocfd_mesh(path, *meshgen.swept_ramp_mesh(q))
+        X, Y, Z = mesh_from_ocfd(path, q["nx"], q["ny"], q["nz"])
+        n, coef = (q["nx"], q["ny"], q["nz"]), METRICS_READFORT
+    else:
+        n = (24, 20, 8)
+        X, Y, Z = meshgen.flat_plate_grid(*n)
+        coef = METRICS_PARSE_MESH
+    s = Flame3D(params_copy(make_params(*n), precision=PREC_REF32))
+    ms, J = s.compute_metrics(dev(X), dev(Y), dev(Z), coef)
+    mr, Jr = meshgen.metrics_f32(X, Y, Z, pipeline)
+    assert np.array_equal(host(J), Jr)
+    for a, b in zip(ms, mr):
+        assert np.array_equal(host(a), b)
+    s.set_metrics(ms, J)  # usable as the context's metrics
+    with pytest.raises(F3DError):
+        s.compute_metrics(dev(X), dev(Y), dev(Z), 7)
+    s.close()
