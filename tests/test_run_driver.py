@@ -47,12 +47,15 @@ def test_run_from_the_reference_files(gpu_lib, tmp_path):
     avg = h5.read(str(a / "AVG/avg-10.h5"))["avg"]
     assert avg.shape == (6, 8, 20, 24) and np.isfinite(avg).all()
     # restart from the checkpoint of step 20 for 5 steps: as steps 21-25 of the first run,
-    # but from the Float32 primitives of the file
+    # but from the Float32 primitives of the file. Time 0.0055: in Float32, 5 dt lies just
+    # above 0.005, where the reference's loop would stop after 4 steps
+    assert run.n_steps(1e-3, 0.0055, 200000) == 5 and run.n_steps(1e-3, 0.005, 200000) == 4
     b = tmp_path / "b"
-    assert run.main(common + ["--out", str(b), "--time", "0.005", "--restart", str(a / "CHK/chk-20.h5")]) == 0
+    assert run.main(common + ["--out", str(b), "--time", "0.0055", "--restart", str(a / "CHK/chk-20.h5")]) == 0
     Qa = files.read_checkpoint(str(a / "CHK/chk-25.h5")).astype(np.float64)
     pb = h5.read(str(b / "PLT/plt-5.h5"))
     I = (slice(4, -4),) * 3
+    vel = np.abs(Qa[1:4][(slice(None),) + I]).max()  # one scale for u, v, w
     for n, name in enumerate(files.PRIM_NAMES):
-        scale = np.abs(Qa[n][I]).max() or 1.0
+        scale = vel if name in ("u", "v", "w") else np.abs(Qa[n][I]).max()
         assert np.abs(pb[name] - Qa[n][I]).max() <= 1e-5 * scale, name
