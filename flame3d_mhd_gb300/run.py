@@ -24,7 +24,6 @@ import argparse
 import datetime
 import json
 import math
-import os
 import sys
 import time
 

@@ -15,7 +15,6 @@ RHS disagree by 2% there, and so do the dual numbers); with UP7 faces there, or 
 faces, all three agree to 1e-9."""
 import numpy as np
 import pytest
-import torch
 
 from flame3d_mhd_gb300.abi import BC_DIRICHLET, BC_PERIODIC, BC_WALL_ADIABATIC, BC_WALL_ISOTHERMAL, make_params
 from flame3d_mhd_gb300.solver import Flame3D
