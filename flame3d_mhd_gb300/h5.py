@@ -28,6 +28,7 @@ Arrays are C order. HDF5.jl stores a Julia array of size (n1, ..., nk) with file
 from __future__ import annotations
 
 import mmap
+import os
 import struct
 import zlib
 
@@ -53,6 +54,15 @@ def _u(b, off, n):
 
 def _pad8(n):
     return (n + 7) & ~7
+
+
+def _parallel_map(fn, items: list) -> list:
+    """fn over items on a thread pool (zlib and numpy copies release the GIL), in order."""
+    if len(items) < 2:
+        return [fn(x) for x in items]
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(len(items), os.cpu_count() or 1)) as ex:
+        return list(ex.map(fn, items))
 
 
 def _rot(x, k):
@@ -145,7 +155,8 @@ class Dataset:
             origins = np.stack(np.meshgrid(*grid, indexing="ij"), -1).reshape(-1, rank)
             chunks = [(cbytes, 0, tuple(int(v) for v in o), self.layout[1] + i * cbytes)
                       for i, o in enumerate(origins)]
-        for size, mask, offs, addr in chunks:
+        def place(entry):
+            size, mask, offs, addr = entry
             raw = bytes(self.f.buf[self.f.abs(addr):self.f.abs(addr) + size])
             for i in reversed(range(len(self.filters))):
                 fid, cd = self.filters[i]
@@ -154,7 +165,9 @@ class Dataset:
                 raw = _unfilter(fid, cd, raw, esize)
             c = np.frombuffer(raw, self.dtype, int(np.prod(cshape))).reshape(cshape)
             sl = tuple(slice(o, min(o + s, d)) for o, s, d in zip(offs, cshape, self.shape))
-            out[sl] = c[tuple(slice(0, s.stop - s.start) for s in sl)]
+            out[sl] = c[tuple(slice(0, s.stop - s.start) for s in sl)]  # disjoint regions
+
+        _parallel_map(place, list(chunks))
         return out
 
 
@@ -780,8 +793,7 @@ def write(path: str, datasets: dict, chunks: dict | None = None, deflate: int | 
                     fm += struct.pack("<HHHH", fid, 0, 1, len(cd))  # both filters optional
                     fm += b"".join(struct.pack("<I", c) for c in cd) + (b"\0" * 4 if len(cd) % 2 else b"")
                 msgs.append((M_FILTERS, fm, 0))
-            data = []
-            for o in origins:
+            def encode(o, a=a, cshape=cshape, pipe=pipe):
                 sl = tuple(slice(int(s), int(s) + c) for s, c in zip(o, cshape))
                 c = np.zeros(cshape, a.dtype)
                 part = a[sl]
@@ -789,7 +801,9 @@ def write(path: str, datasets: dict, chunks: dict | None = None, deflate: int | 
                 d = c.tobytes()
                 for fid, cd in pipe:
                     d = _shuffle(d, cd[0]) if fid == F_SHUFFLE else zlib.compress(d, cd[0])
-                data.append(d)
+                return d
+
+            data = _parallel_map(encode, list(origins))
             dims4 = b"".join(struct.pack("<I", c) for c in cshape + (a.itemsize,))
             v4 = bytes([4, 2])
             if new_format and len(origins) == 1:  # layout v4, single-chunk index
