@@ -1,6 +1,7 @@
 """The reference's grid generators and its CPU metrics, restated (host-side set-up code).
 
-  swept_ramp_mesh   SCU-benchmark/swept-compression-ramp.c:180-449: the swept compression
+  swept_ramp_mesh   SCU-benchmark/swept-compression-ramp.c:180-449 (and its output files,
+                    write_swept_outputs, :446-560): the swept compression
                     ramp written to OCFD3d-Mesh.dat (Hermite-stretched inlet, the corner arc
                     of the upper boundary, exponential wall-normal stretching whose exponent
                     Newton's method finds, wall orthogonalisation, spanwise sweep), for the
@@ -78,14 +79,14 @@ def _inlet_x(n: int, length: float, dx1: float, dx2: float) -> list:
     return out
 
 
-def swept_ramp_mesh(p: dict | None = None, **kw) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+def swept_ramp_mesh(p: dict | None = None, with_2d: bool = False, **kw) -> tuple:
     """Coordinates (Nz, Ny, Nx) float64 of swept-compression-ramp.c for the parameters `p`
     (SWEPT_DEFAULTS, updated by keyword arguments): the lower wall xa, ya and the upper
     boundary xb, yb along xi (gridx, :199-236), points between them on an exponential
     distribution whose first spacing is hy_wall (gridxy, :238-275), the first 19 grid lines
     off the wall made orthogonal to it (Wall_Orthonormalization, :385-426), then the spanwise
     extrusion with the inlet stretched by the sweep (gridxyz, :277-383), for the z slab of
-    each of `nprocs` processes."""
+    each of `nprocs` processes. with_2d: also the (Ny, Nx) plane x, y it extrudes."""
     q = dict(SWEPT_DEFAULTS)
     q.update(p or {})
     q.update(kw)
@@ -194,7 +195,44 @@ def swept_ramp_mesh(p: dict | None = None, **kw) -> tuple[np.ndarray, np.ndarray
             x3[kk, :, ni:] = x3[kk, :, ni - 1:ni] + x2[:, ni:] - x2[:, ni - 1:ni]
             y3[kk] = y2
             z3[kk] = z
-    return x3, y3, z3
+    return (x3, y3, z3, x2, y2) if with_2d else (x3, y3, z3)
+
+
+def write_swept_outputs(out_dir: str, p: dict, x3, y3, z3, x2, y2) -> list:
+    """The files of swept-compression-ramp.c's output() (:446-560): OCFD3d-Mesh.dat; y1d.dat
+    (the first column's y, "%15.6f"); with Tec1 gridxy.dat and with Tec2 grid.dat (Tecplot
+    text of the plane and of the grid); with Mesh2D OCFD2d-Mesh.dat (x and y of the plane,
+    each one record). Returns the paths written."""
+    os.makedirs(out_dir, exist_ok=True)
+    nz, ny, nx = x3.shape
+    out = [os.path.join(out_dir, "OCFD3d-Mesh.dat")]
+    write_ocfd_mesh(out[0], x3, y3, z3)
+    path = os.path.join(out_dir, "y1d.dat")
+    with open(path, "w") as f:
+        f.writelines(f"{v:15.6f}\n" for v in y2[:, 0].tolist())
+    out.append(path)
+    if p.get("tec1", 1) == 1:
+        path = os.path.join(out_dir, "gridxy.dat")
+        with open(path, "w") as f:
+            f.write(f"variables=x,y\nzone i={nx} ,j={ny}\n")
+            f.writelines(f"{a:15.6f}{b:15.6f}\n" for a, b in zip(x2.ravel().tolist(), y2.ravel().tolist()))
+        out.append(path)
+    if p.get("mesh2d", 1) == 1:
+        path = os.path.join(out_dir, "OCFD2d-Mesh.dat")
+        mark = np.array([nx * ny * 8], dtype="<i4").tobytes()
+        with open(path, "wb") as f:
+            for a in (x2, y2):
+                f.write(mark + np.ascontiguousarray(a, dtype="<f8").tobytes() + mark)
+        out.append(path)
+    if p.get("tec2", 0) == 1:
+        path = os.path.join(out_dir, "grid.dat")
+        with open(path, "w") as f:
+            f.write(f"variables=x,y,z\nzone i={nx} ,j={ny} ,k={nz}\n")
+            for k in range(nz):
+                f.writelines(f"{a:15.6f}{b:15.6f}{c:15.6f}\n" for a, b, c in
+                             zip(x3[k].ravel().tolist(), y3[k].ravel().tolist(), z3[k].ravel().tolist()))
+        out.append(path)
+    return out
 
 
 def flat_plate_grid(nx: int = 256, ny: int = 128, nz: int = 32, lx: float = 2.0, ly: float = 0.1,
@@ -287,11 +325,10 @@ def main(argv=None):
     a = ap.parse_args(argv)
     os.makedirs(a.out, exist_ok=True)
     if a.cmd == "swept":
-        q = read_swept_params(a.params) if a.params else dict(SWEPT_DEFAULTS)
-        x, y, z = swept_ramp_mesh(q)
-        path = os.path.join(a.out, "OCFD3d-Mesh.dat")
-        write_ocfd_mesh(path, x, y, z)
-        print(path)
+        q = read_swept_params(a.params) if a.params else dict(SWEPT_DEFAULTS, tec1=1, mesh2d=1, tec2=0)
+        paths = write_swept_outputs(a.out, q, *swept_ramp_mesh(q, with_2d=True))
+        print(*paths)
+        path = paths[0]
         if a.metrics:
             X, Y, Z = mesh_from_ocfd(path, q["nx"], q["ny"], q["nz"])
             print(*reference_files(a.out, X, Y, Z, "readfort"))

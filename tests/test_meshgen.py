@@ -149,6 +149,22 @@ def test_swept_ramp_geometry(tmp_path):
     assert X.dtype == np.float32 and np.array_equal(X[NG:-NG, NG:-NG, NG:-NG], (x.astype(np.float32) / np.float32(1000)))
     m, J = meshgen.metrics_f32(X, Y, Z)
     assert np.isfinite(J).all() and (J[NG:-NG, NG:-NG, NG:-NG] > 0).all()
+    # the generator's other files: y1d.dat, Tecplot text, the 2-D record file
+    x3, y3, z3, x2, y2 = meshgen.swept_ramp_mesh(q, with_2d=True)
+    assert np.array_equal(x3, x) and np.array_equal(y2, y[0])
+    paths = meshgen.write_swept_outputs(str(tmp_path / "out"), dict(q, tec1=1, mesh2d=1, tec2=1), x3, y3, z3, x2, y2)
+    assert [os.path.basename(p) for p in paths] == ["OCFD3d-Mesh.dat", "y1d.dat", "gridxy.dat", "OCFD2d-Mesh.dat",
+                                                    "grid.dat"]
+    y1d = open(paths[1]).read().splitlines()
+    assert len(y1d) == q["ny"] and y1d[1] == "%15.6f" % y2[1, 0]
+    txt = open(paths[2]).read().splitlines()
+    assert txt[:2] == ["variables=x,y", f"zone i={q['nx']} ,j={q['ny']}"] and len(txt) == 2 + q["nx"] * q["ny"]
+    assert txt[2 + q["nx"] + 3] == "%15.6f%15.6f" % (x2[1, 3], y2[1, 3])
+    raw = np.fromfile(paths[3], dtype=np.uint8)
+    rec = q["nx"] * q["ny"] * 8
+    assert raw.size == 2 * (rec + 8) and np.array_equal(raw[4:4 + rec].view("<f8").reshape(x2.shape), x2)
+    g = open(paths[4]).read().splitlines()
+    assert g[1] == f"zone i={q['nx']} ,j={q['ny']} ,k={q['nz']}" and len(g) == 2 + x3.size
     params = tmp_path / "swept-compression-grid.in"
     params.write_text("nx ny nz Nprocs\n64 24 6 1\nnx_inlet nx_conner nx_buff\n40 20 4\n"
                       "dx_inlet Lx_inlet Lx_conner alfax_buff\n0.9 30. 8. 1.05\nsw_angle comp_angle\n0. 24.\n"
