@@ -1,0 +1,23 @@
+"""Write tests/golden/fdm_coeffs.json from the reference's own coefficient script,
+Utils/FDMcoeffs.py: the flux-form face coefficients of the 8-point first-derivative stencil
+from -4 (UP7 of run.jl:75) and of the 7-point one from -3 (CD6 of run.jl:76, with its leading
+zero), and the half-and-half blend the script prints. Runs where the reference is present:
+
+  python tests/golden/make_fdm_coeffs.py [path/to/reference]
+"""
+import json
+import runpy
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+ns = runpy.run_path(str(ref / "Utils" / "FDMcoeffs.py"))  # the script prints its blend
+up7 = ns["fluxCoeff"](8, -4)
+cd6 = np.concatenate(([0.0], ns["fluxCoeff"](7, -3)))
+out = {"source": "Utils/FDMcoeffs.py fluxCoeff(8, -4), fluxCoeff(7, -3)",
+       "up7": up7.tolist(), "cd6": cd6.tolist(), "blend_half": (0.5 * up7 + 0.5 * cd6).tolist()}
+path = Path(__file__).resolve().parent / "fdm_coeffs.json"
+path.write_text(json.dumps(out, indent=1) + "\n")
+print(path)

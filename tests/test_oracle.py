@@ -286,3 +286,27 @@ def test_golden_fixtures():
         r = orc.rhs(P, np.ascontiguousarray(g["Q"]), m, np.ascontiguousarray(g["J"]))
         I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
         assert rel_linf(r[I], g["rhs"][I]) <= meta["tol"], f.name
+
+
+def test_linear_scheme_coefficients_from_the_reference_script():
+    """UP7 and CD6 (run.jl:75-77) in the NumPy oracle, the C++ oracle and the CUDA library
+    equal the face coefficients the reference's Utils/FDMcoeffs.py derives (fixture made by
+    tests/golden/make_fdm_coeffs.py; the script's linear solve rounds at 1e-15)."""
+    import json
+    import re
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    g = json.loads((root / "tests" / "golden" / "fdm_coeffs.json").read_text())
+    up7, cd6 = np.array(g["up7"]), np.array(g["cd6"])
+    assert np.abs(npo.UP7 - up7).max() < 2e-15 and np.abs(npo.CD6 - cd6).max() < 2e-15
+    P = make_params(8, 8, 8, linear_phi=0.5)
+    assert np.abs(npo.consts(P)[2] - np.array(g["blend_half"])).max() < 2e-15
+    for src in ("flame3d_mhd_gb300/csrc/api.cu", "oracle/f3d_oracle.hpp"):
+        text = (root / src).read_text()
+        for name, want in (("up7", up7), ("cd6", cd6)):
+            body = re.search(r"const double %s\[7\] = \{([^}]*)\}" % name, text).group(1)
+            vals = []
+            for t in body.split(","):
+                m = re.fullmatch(r"\s*([-+]?[\d.]+)\s*/\s*([\d.]+)\s*", t)
+                vals.append(float(m.group(1)) / float(m.group(2)) if m else float(t))
+            assert np.abs(np.array(vals) - want).max() < 2e-15, (src, name)
