@@ -39,18 +39,20 @@ def _interior(a: np.ndarray) -> np.ndarray:
     return a[..., NG:-NG, NG:-NG, NG:-NG]
 
 
-def _slabs(shape, axis=0) -> tuple:
-    """A chunk shape that splits `shape` into at most MAX_CHUNKS slabs along `axis`."""
-    n = shape[axis]
+def _slabs(shape) -> tuple:
+    """A chunk shape that splits `shape` into at most MAX_CHUNKS slabs along its slowest
+    axis longer than 1 (the chunks are compressed in parallel; readers see no difference
+    from the reference's one chunk a rank)."""
+    axis = next((d for d, n in enumerate(shape) if n > 1), 0)
     c = list(shape)
-    c[axis] = max(1, -(-n // MAX_CHUNKS))
+    c[axis] = max(1, -(-shape[axis] // MAX_CHUNKS))
     return tuple(c)
 
 
-def _write(path, datasets, compress, shuffle, chunks=None):
+def _write(path, datasets, compress, shuffle):
     if compress is None:
         return h5.write(path, datasets)
-    chunks = chunks or {k: _slabs(np.shape(v)) for k, v in datasets.items() if np.ndim(v) > 0}
+    chunks = {k: _slabs(np.shape(v)) for k, v in datasets.items() if np.ndim(v) > 0}
     return h5.write(path, datasets, chunks=chunks, deflate=compress, shuffle=shuffle)
 
 
@@ -149,9 +151,8 @@ def write_XDMF(plt_dir: str, tt: int, dt: float, nx: int, ny: int, nz: int, mesh
 def plotFile_xdmf(out_dir: str, tt: int, Q, phi, dt: float, shuffle: bool = True,
                   compress: int | None = 1) -> str:
     """PLT/plt-tt.h5 with the interior rho, u, v, w, p, T and the shock sensor phi as
-    separate (Nz, Ny, Nx) Float32 datasets, and its XDMF file (IO.jl:1-112; one rank, so one
-    chunk a dataset as chunk=(Nxp, Nyp, Nzp) gives there). Q is (6, Nz+8, Ny+8, Nx+8), phi
-    (Nz+8, Ny+8, Nx+8)."""
+    separate (Nz, Ny, Nx) Float32 datasets, and its XDMF file (IO.jl:1-112). Q is (6, Nz+8,
+    Ny+8, Nx+8), phi (Nz+8, Ny+8, Nx+8)."""
     Qh, ph = _interior(_host(Q)), _interior(_host(phi))
     if Qh.shape[0] != 6 or ph.shape != Qh.shape[1:]:
         raise ValueError("Q must be (6, Nz+8, Ny+8, Nx+8) and phi (Nz+8, Ny+8, Nx+8)")
@@ -160,8 +161,7 @@ def plotFile_xdmf(out_dir: str, tt: int, Q, phi, dt: float, shuffle: bool = True
     write_XDMF(plt_dir, tt, dt, Qh.shape[3], Qh.shape[2], Qh.shape[1])
     data = {name: Qh[n] for n, name in enumerate(PRIM_NAMES)}
     data["phi"] = ph
-    return _write(os.path.join(plt_dir, f"plt-{tt}.h5"), data, compress, shuffle,
-                  {k: v.shape for k, v in data.items()})
+    return _write(os.path.join(plt_dir, f"plt-{tt}.h5"), data, compress, shuffle)
 
 
 def plotFile_h5(out_dir: str, tt: int, Q, shuffle: bool = True, compress: int | None = 1) -> str:
@@ -172,19 +172,19 @@ def plotFile_h5(out_dir: str, tt: int, Q, shuffle: bool = True, compress: int | 
         raise ValueError("Q must be (6, Nz+8, Ny+8, Nx+8)")
     plt_dir = os.path.join(out_dir, "PLT")
     os.makedirs(plt_dir, exist_ok=True)
-    return _write(os.path.join(plt_dir, f"plt-{tt}.h5"), {"Q": Qh}, compress, shuffle, {"Q": Qh.shape})
+    return _write(os.path.join(plt_dir, f"plt-{tt}.h5"), {"Q": Qh}, compress, shuffle)
 
 
 def checkpointFile(out_dir: str, tt: int, Q, shuffle: bool = True, compress: int | None = 1) -> str:
     """CHK/chk-tt.h5 with Q_h: the primitives with ghosts, (ranks=1, 6, Nz+8, Ny+8, Nx+8)
-    Float32, one chunk a rank (IO.jl:153-183)."""
+    Float32 (IO.jl:153-183)."""
     Qh = _host(Q)
     if Qh.ndim != 4 or Qh.shape[0] != 6:
         raise ValueError("Q must be (6, Nz+8, Ny+8, Nx+8)")
     chk_dir = os.path.join(out_dir, "CHK")
     os.makedirs(chk_dir, exist_ok=True)
     Qr = Qh[None]
-    return _write(os.path.join(chk_dir, f"chk-{tt}.h5"), {"Q_h": Qr}, compress, shuffle, {"Q_h": Qr.shape})
+    return _write(os.path.join(chk_dir, f"chk-{tt}.h5"), {"Q_h": Qr}, compress, shuffle)
 
 
 def read_checkpoint(path: str, rank: int = 0, dtype=np.float32) -> np.ndarray:
@@ -205,4 +205,4 @@ def averageFile(out_dir: str, tt: int, Q_avg, shuffle: bool = True, compress: in
         raise ValueError("Q_avg must be (6, Nz+8, Ny+8, Nx+8)")
     avg_dir = os.path.join(out_dir, "AVG")
     os.makedirs(avg_dir, exist_ok=True)
-    return _write(os.path.join(avg_dir, f"avg-{tt}.h5"), {"avg": A}, compress, shuffle, {"avg": A.shape})
+    return _write(os.path.join(avg_dir, f"avg-{tt}.h5"), {"avg": A}, compress, shuffle)

@@ -240,7 +240,7 @@ def test_solution_files(tmp_path):
     _structure_checks(p)
     with h5.H5File(p) as f:
         d = f.dataset("Q_h")
-        assert d.shape == (1,) + Q.shape and d.layout[2][:5] == [1] + list(Q.shape)
+        assert d.shape == (1,) + Q.shape and d.layout[2][:5] == [1, 1] + list(Q.shape[1:])  # a chunk a variable
         assert [fid for fid, _ in d.filters] == [h5.F_SHUFFLE, h5.F_DEFLATE]
     assert np.array_equal(files.read_checkpoint(p), Q.astype(np.float32))
     p = files.averageFile(out, 800, Q)
