@@ -116,6 +116,7 @@ def load() -> C.CDLL:
         "f3d_rhs": (ip, [vp, vp, vp, vp]),
         "f3d_rk3_stage": (ip, [vp, ip, C.c_double, vp, vp, vp, vp]),
         "f3d_rk3_steps": (ip, [vp, ip, C.c_double, vp, vp, vp, vp]),
+        "f3d_rk3_step": (ip, [vp, C.c_double, vp, vp, vp, vp]),
         "f3d_cfl_dt": (ip, [vp, vp, C.c_double, dp, vp]),
         "f3d_check_finite": (ip, [vp, vp, vp]),
         "f3d_debug_sensor": (ip, [vp, vp, vp, vp]),
@@ -165,7 +166,7 @@ EXPORTED = ["f3d_version", "f3d_default_params", "f3d_create", "f3d_destroy", "f
             "f3d_set_coordinates", "f3d_filter", "f3d_local_dt", "f3d_debug_round_f32",
             "f3d_set_inflow_profile_cotangent", "f3d_rk3_step_vjp_stages", "f3d_set_metrics_f32",
             "f3d_c2prim_f32", "f3d_prim2c_f32", "f3d_fill_ghosts_f32", "f3d_rhs_f32", "f3d_rk3_stage_f32",
-            "f3d_rk3_steps_f32", "f3d_set_metrics_cotangent", "f3d_compute_metrics_f32"]
+            "f3d_rk3_steps_f32", "f3d_set_metrics_cotangent", "f3d_compute_metrics_f32", "f3d_rk3_step"]
 
 
 class F3DError(RuntimeError):

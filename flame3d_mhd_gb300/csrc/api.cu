@@ -892,6 +892,10 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
     return F3D_OK;
 }
 
+int f3d_rk3_step(f3d_ctx* ctx, double dt, double* U, double* Un, double* Q, f3d_stream stream) {
+    return f3d_rk3_steps(ctx, 1, dt, U, Un, Q, stream);
+}
+
 // ---- F3D_PREC_REF32 entries (Float32 arrays) ---------------------------------------------
 int f3d_set_metrics_f32(f3d_ctx* ctx, const float* const metrics[9], const float* jac, f3d_stream stream) {
     int rc = check_ctx32(ctx, false);

@@ -206,6 +206,9 @@ int f3d_rk3_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, dou
  * first call with the same pointers. */
 int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, double* Q,
                   f3d_stream stream);
+/* One SSP-RK3 step: f3d_rk3_steps with nsteps = 1 (one pass of the loop body of
+ * solver.jl:409-470). */
+int f3d_rk3_step(f3d_ctx* ctx, double dt, double* U, double* Un, double* Q, f3d_stream stream);
 
 /* Largest stable dt for the given CFL number over interior cells:
  * min over cells and directions of cfl / (J (|U_d| + c |grad xi_d|)), U_d = grad xi_d . u.

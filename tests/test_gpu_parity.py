@@ -303,6 +303,27 @@ def test_rk3_steps_parity(gpu_lib, name):
     c.close()
 
 
+def test_rk3_step_is_one_of_rk3_steps(gpu_lib):
+    """f3d_rk3_step (the one-step export) gives the state of f3d_rk3_steps with nsteps = 1."""
+    c = RHS_CASES["sod32_hybrid_char"]()
+    dt = 2e-4
+    outs = []
+    for one in (True, False):
+        U, Un, Q = dev(c.U), torch.zeros_like(dev(c.U)), dev(c.Q)
+        with side_stream() as stream:
+            for _ in range(3):
+                if one:
+                    rc = c.s.lib.f3d_rk3_step(c.s._h, dt, U.data_ptr(), Un.data_ptr(), Q.data_ptr(),
+                                              stream.cuda_stream)
+                    assert rc == 0
+                else:
+                    c.s.time_step(U, Un, Q, dt, 1)
+        stream.synchronize()
+        outs.append((host(U), host(Q)))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    c.close()
+
+
 def test_metrics_parity(gpu_lib):
     P = make_params(20, 12, 16)
     x, y, z = curvilinear_coords(P, amp=0.05)
