@@ -16,7 +16,9 @@
 // with fastmath=true; the <float,double> instantiation uses IEEE operations instead.
 //
 // Parity is unpinned by the reference's own tests: the reference has no tests, fixtures
-// or golden vectors, and Julia is not available to run it.
+// or golden vectors, and Julia is not available to run it. The one piece of the reference
+// that runs here, its Python coefficient script (Utils/FDMcoeffs.py), pins the UP7 and CD6
+// face coefficients (tests/golden/fdm_coeffs.json).
 #pragma once
 #include <cmath>
 #include <cstddef>

@@ -4,6 +4,9 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.
 baseline, never by the flame3d_mhd_gb300 package. All arrays are numpy float64 in the
 reference layout, C-ordered (nvar, Nz+8, Ny+8, Nx+8). The library is built from
 oracle/f3d_oracle.hpp by oracle/Makefile on first use.
+
+Parity unpinned: the reference has no tests or golden vectors and cannot be run here (no
+Julia); only its UP7 / CD6 coefficients are pinned, on its own Utils/FDMcoeffs.py.
 """
 from __future__ import annotations
 
