@@ -197,6 +197,34 @@ def read_checkpoint(path: str, rank: int = 0, dtype=np.float32) -> np.ndarray:
     return Qh[rank].astype(dtype)
 
 
+def assemble_checkpoint(path: str, nprocs=(1, 1, 1), dtype=np.float32) -> np.ndarray:
+    """The global Q (6, Nz+8, Ny+8, Nx+8) from the checkpoint of a run on px x py x pz ranks,
+    to restart it on one GPU. Each rank wrote its local block with its ghost frame
+    (IO.jl:153-183, Q_h[..., rank+1]); ranks are numbered as MPI_Cart_create numbers them
+    (run.jl:117: row-major, z fastest). Every block lands at its rank's offset, then every
+    block's interior over the halos, so the global ghost frame comes from the blocks on the
+    domain faces. (The reference's own restart, solver.jl:211-216, reads one rank.)"""
+    with h5.H5File(path) as f:
+        Qh = f["Q_h"]
+    px, py, pz = nprocs
+    if Qh.ndim != 5 or Qh.shape[0] != px * py * pz or Qh.shape[1] != 6:
+        raise ValueError(f"{path}: Q_h of shape {Qh.shape} for {px}x{py}x{pz} ranks")
+    nzp, nyp, nxp = (n - 2 * NG for n in Qh.shape[2:])
+    G = np.zeros((6, pz * nzp + 2 * NG, py * nyp + 2 * NG, px * nxp + 2 * NG), dtype)
+
+    def at(r, inner):
+        cx, cy, cz = r // (py * pz), (r // pz) % py, r % pz
+        o = 0 if not inner else NG
+        return (slice(None), slice(cz * nzp + o, (cz + 1) * nzp + 2 * NG - o),
+                slice(cy * nyp + o, (cy + 1) * nyp + 2 * NG - o), slice(cx * nxp + o, (cx + 1) * nxp + 2 * NG - o))
+
+    for r in range(Qh.shape[0]):
+        G[at(r, False)] = Qh[r]
+    for r in range(Qh.shape[0]):
+        G[at(r, True)] = _interior(Qh[r])
+    return G
+
+
 def averageFile(out_dir: str, tt: int, Q_avg, shuffle: bool = True, compress: int | None = 1) -> str:
     """AVG/avg-tt.h5 with avg: the interior of the averaged primitives (6, Nz, Ny, Nx)
     Float32 (IO.jl:185-210)."""

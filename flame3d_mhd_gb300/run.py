@@ -77,6 +77,8 @@ def parser() -> argparse.ArgumentParser:
     ap.add_argument("--metrics", default="metrics.h5")
     ap.add_argument("--out", default=".", help="where PLT/, CHK/ and AVG/ go")
     ap.add_argument("--restart", default="none", help="a checkpoint file CHK/chk-N.h5, or none")
+    ap.add_argument("--restart-nprocs", type=int, nargs=3, default=[1, 1, 1], metavar=("PX", "PY", "PZ"),
+                    help="the rank layout of the run that wrote the checkpoint (run.jl's Nprocs)")
     ap.add_argument("--precision", choices=["fp64", "mixed", "ref32"], default="fp64")
     ap.add_argument("--scheme", choices=["fvm-eigen", "fvm", "fdm"], default="fvm-eigen",
                     help="finite volume with eigen / component-wise reconstruction, or finite difference")
@@ -129,7 +131,7 @@ def setup(a):
     if scheme != SCHEME_FDM:
         s.set_coordinates(*(dev(c) for c in files.read_mesh(a.mesh)))
     if a.restart != "none":
-        Q = dev(files.read_checkpoint(a.restart))
+        Q = dev(files.assemble_checkpoint(a.restart, tuple(a.restart_nprocs)))
     else:  # boundary.jl:163-193: the free stream at interior cells, ghosts from fillGhost
         rho, u, p = dtype(1.0), dtype(0.5), dtype(1.0) / dtype(1.4)
         q = np.zeros((6,) + s.shape3, dtype)

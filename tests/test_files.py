@@ -311,3 +311,22 @@ def test_checksums_catch_damage(tmp_path):
     (tmp_path / "sb.h5").write_bytes(bytes(bad))
     with pytest.raises(ValueError):
         h5.H5File(str(tmp_path / "sb.h5"))
+
+
+@pytest.mark.parametrize("nprocs", [(1, 1, 1), (2, 1, 1), (2, 3, 2)])
+def test_assemble_multi_rank_checkpoint(tmp_path, nprocs):
+    """Blocks cut from a global field with their ghost frames, as each rank of a multi-GPU
+    run holds them, reassemble to that field."""
+    px, py, pz = nprocs
+    nxp, nyp, nzp = 5, 4, 3
+    rng = np.random.default_rng(8)
+    G0 = rng.standard_normal((6, pz * nzp + 2 * NG, py * nyp + 2 * NG, px * nxp + 2 * NG)).astype(np.float32)
+    blocks = []
+    for r in range(px * py * pz):
+        cx, cy, cz = r // (py * pz), (r // pz) % py, r % pz  # MPI_Cart_create: row-major, z fastest
+        blocks.append(G0[:, cz * nzp:(cz + 1) * nzp + 2 * NG, cy * nyp:(cy + 1) * nyp + 2 * NG,
+                         cx * nxp:(cx + 1) * nxp + 2 * NG])
+    p = h5.write(str(tmp_path / "chk.h5"), {"Q_h": np.stack(blocks)})
+    assert np.array_equal(files.assemble_checkpoint(p, nprocs), G0)
+    with pytest.raises(ValueError):
+        files.assemble_checkpoint(p, (px * py * pz + 1, 1, 1))
