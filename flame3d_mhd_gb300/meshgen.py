@@ -31,7 +31,7 @@ import sys
 
 import numpy as np
 
-from . import files
+from . import files, vtk
 from .grid import NG, extend_ghosts, mesh_from_ocfd, write_ocfd_mesh
 
 PI = 3.1415926535897932  # swept-compression-ramp.c:8
@@ -299,15 +299,19 @@ def metrics_f32(x, y, z, coefficients: str = "readfort") -> tuple[list, np.ndarr
     return m, J
 
 
-def reference_files(out_dir: str, x, y, z, coefficients: str = "readfort") -> tuple[str, str]:
+def reference_files(out_dir: str, x, y, z, coefficients: str = "readfort", vis: bool = False) -> tuple:
     """metrics.h5 and mesh.h5 as the reference's set-up writes them from ghost-filled Float32
     coordinates: readfort.jl (deflate level 0, stored uncompressed here) or parse_mesh.jl
-    (deflate level 3)."""
+    (deflate level 3); with `vis` also its mesh.vts (J, and the metrics for parse_mesh.jl)."""
     m, J = metrics_f32(x, y, z, coefficients)
     level = None if coefficients == "readfort" else 3
     os.makedirs(out_dir, exist_ok=True)
-    return (files.write_metrics(os.path.join(out_dir, "metrics.h5"), m, J, compress=level),
-            files.write_mesh(os.path.join(out_dir, "mesh.h5"), x, y, z, compress=level))
+    out = (files.write_metrics(os.path.join(out_dir, "metrics.h5"), m, J, compress=level),
+           files.write_mesh(os.path.join(out_dir, "mesh.h5"), x, y, z, compress=level))
+    if vis:
+        out += (vtk.write_mesh_vts(os.path.join(out_dir, "mesh.vts"), x, y, z, J,
+                                   m if coefficients == "parse_mesh" else None),)
+    return out
 
 
 def main(argv=None):
@@ -317,11 +321,13 @@ def main(argv=None):
     s.add_argument("--params", default="", help="swept-compression-grid.in (default: the reference's values)")
     s.add_argument("--out", default=".")
     s.add_argument("--metrics", action="store_true", help="also metrics.h5 and mesh.h5 as readfort.jl makes them")
+    s.add_argument("--vis", action="store_true", help="and mesh.vts (readfort.jl's vis)")
     p = sub.add_parser("plate", help="parse_mesh.jl: the flat plate's metrics.h5 and mesh.h5")
     p.add_argument("--nx", type=int, default=256)
     p.add_argument("--ny", type=int, default=128)
     p.add_argument("--nz", type=int, default=32)
     p.add_argument("--out", default=".")
+    p.add_argument("--vis", action="store_true", help="also mesh.vts (parse_mesh.jl's vis)")
     a = ap.parse_args(argv)
     os.makedirs(a.out, exist_ok=True)
     if a.cmd == "swept":
@@ -331,10 +337,10 @@ def main(argv=None):
         path = paths[0]
         if a.metrics:
             X, Y, Z = mesh_from_ocfd(path, q["nx"], q["ny"], q["nz"])
-            print(*reference_files(a.out, X, Y, Z, "readfort"))
+            print(*reference_files(a.out, X, Y, Z, "readfort", vis=a.vis))
     else:
         X, Y, Z = flat_plate_grid(a.nx, a.ny, a.nz)
-        print(*reference_files(a.out, X, Y, Z, "parse_mesh"))
+        print(*reference_files(a.out, X, Y, Z, "parse_mesh", vis=a.vis))
     return 0
 
 

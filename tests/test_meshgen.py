@@ -277,6 +277,12 @@ def test_flat_plate_and_reference_files(tmp_path):
     assert np.array_equal(J, J2) and all(np.array_equal(a, b) for a, b in zip(m, m2))
     Xr, Yr, Zr = files.read_mesh(pg)
     assert np.array_equal(Xr, X) and np.array_equal(Yr, Y) and np.array_equal(Zr, Z)
-    # the command line
-    assert meshgen.main(["plate", "--nx", "16", "--ny", "12", "--nz", "6", "--out", str(tmp_path / "p")]) == 0
-    assert sorted(os.listdir(tmp_path / "p")) == ["mesh.h5", "metrics.h5"]
+    # the command line, with parse_mesh.jl's mesh.vts
+    assert meshgen.main(["plate", "--nx", "16", "--ny", "12", "--nz", "6", "--out", str(tmp_path / "p"),
+                         "--vis"]) == 0
+    assert sorted(os.listdir(tmp_path / "p")) == ["mesh.h5", "mesh.vts", "metrics.h5"]
+    from flame3d_mhd_gb300 import vtk
+    v = vtk.read_vts(str(tmp_path / "p" / "mesh.vts"))
+    assert v["extent"] == (16 + 2 * NG, 12 + 2 * NG, 6 + 2 * NG)
+    assert np.array_equal(v["J"], J.ravel()) and np.array_equal(v["dedy"], m[4].ravel())
+    assert np.array_equal(v["points"][:, 1], Y.ravel())
