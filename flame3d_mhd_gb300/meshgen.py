@@ -60,9 +60,13 @@ def read_swept_params(path: str) -> dict:
     return out
 
 
-def _pow2(v: np.ndarray) -> np.ndarray:
-    """pow(v, 2) of libm per element, as the C program squares (libm's pow need not equal v*v
-    in the last bit)."""
+def _pow2(v: np.ndarray, square: str = "libm") -> np.ndarray:
+    """pow(v, 2) as the C program squares: libm's pow per element (square="libm", the program
+    built without optimisation or with -fno-builtin), or v*v (square="mul": gcc -O1 and above
+    replace pow(v, 2.0) by a multiplication). glibc's pow is within 0.52 ulp, not correctly
+    rounded, so the two can differ in the last bit."""
+    if square == "mul":
+        return v * v
     return np.array([math.pow(t, 2.0) for t in v.tolist()])
 
 
@@ -79,14 +83,18 @@ def _inlet_x(n: int, length: float, dx1: float, dx2: float) -> list:
     return out
 
 
-def swept_ramp_mesh(p: dict | None = None, with_2d: bool = False, **kw) -> tuple:
+def swept_ramp_mesh(p: dict | None = None, with_2d: bool = False, square: str = "libm", **kw) -> tuple:
     """Coordinates (Nz, Ny, Nx) float64 of swept-compression-ramp.c for the parameters `p`
     (SWEPT_DEFAULTS, updated by keyword arguments): the lower wall xa, ya and the upper
     boundary xb, yb along xi (gridx, :199-236), points between them on an exponential
     distribution whose first spacing is hy_wall (gridxy, :238-275), the first 19 grid lines
     off the wall made orthogonal to it (Wall_Orthonormalization, :385-426), then the spanwise
     extrusion with the inlet stretched by the sweep (gridxyz, :277-383), for the z slab of
-    each of `nprocs` processes. with_2d: also the (Ny, Nx) plane x, y it extrudes."""
+    each of `nprocs` processes. with_2d: also the (Ny, Nx) plane x, y it extrudes. square: how
+    the orthogonalisation squares (_pow2): "libm" reproduces the program built at gcc's default
+    optimisation level, "mul" the program built with -O2."""
+    if square not in ("libm", "mul"):
+        raise ValueError("square must be 'libm' or 'mul'")
     q = dict(SWEPT_DEFAULTS)
     q.update(p or {})
     q.update(kw)
@@ -164,7 +172,7 @@ def swept_ramp_mesh(p: dict | None = None, with_2d: bool = False, **kw) -> tuple
     for _ in range(10):
         for j in range(1, 20):
             ex, ey = x2[j, 2:] - x2[j, :-2], y2[j, 2:] - y2[j, :-2]
-            qn = np.sqrt(_pow2(ex) + _pow2(ey))
+            qn = np.sqrt(_pow2(ex, square) + _pow2(ey, square))
             qnx, qny = -ey / qn, ex / qn
             rx, ry = x2[j, 1:-1] - x2[j - 1, 1:-1], y2[j, 1:-1] - y2[j - 1, 1:-1]
             s = rx * qnx + ry * qny

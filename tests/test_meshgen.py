@@ -286,3 +286,47 @@ def test_flat_plate_and_reference_files(tmp_path):
     assert v["extent"] == (16 + 2 * NG, 12 + 2 * NG, 6 + 2 * NG)
     assert np.array_equal(v["J"], J.ravel()) and np.array_equal(v["dedy"], m[4].ravel())
     assert np.array_equal(v["points"][:, 1], Y.ravel())
+
+
+# ---- pinned on the reference program itself ------------------------------------------------
+# tests/golden/swept_ramp_ref.npz holds OCFD3d-Mesh.dat coordinates written by the unmodified
+# swept-compression-ramp.c (compiled against the MPI stand-in oracle/ref_ramp/mpi.h; made by
+# tests/golden/make_ramp_fixture.py) and digests of its 1000 x 240 x 100 benchmark grid from
+# the program built at gcc's default optimisation level and at -O2.
+def _ramp_fixture():
+    import json
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "swept_ramp_ref.npz"))
+    return d, json.loads(str(d["meta"]))
+
+
+@pytest.mark.parametrize("name", ["one_process", "two_processes_swept", "three_processes"])
+def test_swept_ramp_equals_reference_program(name):
+    d, meta = _ramp_fixture()
+    q = dict(meta["small"], **meta["variants"][name])
+    got = meshgen.swept_ramp_mesh(q)
+    for a, key in zip(got, "xyz"):
+        assert np.array_equal(a, d[f"{name}_{key}"]), key
+
+
+@pytest.mark.parametrize("square,build", [("libm", "O0"), ("mul", "O2")])
+def test_swept_ramp_benchmark_grid_digest(square, build):
+    import hashlib
+    _, meta = _ramp_fixture()
+    h = hashlib.sha256()
+    for a in meshgen.swept_ramp_mesh(meta["benchmark"], square=square):
+        h.update(np.ascontiguousarray(a, dtype="<f8").tobytes())
+    assert h.hexdigest() == meta[f"benchmark_sha256_{build}"]
+
+
+def test_swept_ramp_live_against_reference_program():
+    """Runs the compiled reference program where its source tree is present (oracle/_ref)."""
+    from oracle.ref_ramp import run_ref
+    if not run_ref.available():
+        pytest.skip("the reference program is not built here")
+    q = dict(SMALL, nx=48, nx_inlet=30, nx_corner=14, nx_buff=4, ny=22, nz=8, nprocs=2, sw_angle=15.0,
+             comp_angle=20.0, hy_wall=0.02)
+    for o2, square in ((False, "libm"), (True, "mul")):
+        ref = run_ref.run(q, o2=o2)
+        got = meshgen.swept_ramp_mesh(q, square=square)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
