@@ -3,16 +3,18 @@ Utils/FDMcoeffs.py: the flux-form face coefficients of the 8-point first-derivat
 from -4 (UP7 of run.jl:75) and of the 7-point one from -3 (CD6 of run.jl:76, with its leading
 zero), and the half-and-half blend the script prints. Runs where the reference is present:
 
-  python tests/golden/make_fdm_coeffs.py [path/to/reference]
+  python tests/golden/make_fdm_coeffs.py <root of the reference source tree>
 """
+import argparse
 import json
 import runpy
-import sys
 from pathlib import Path
 
 import numpy as np
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+ap = argparse.ArgumentParser()
+ap.add_argument("ref", help="root of the reference source tree")
+ref = Path(ap.parse_args().ref)
 ns = runpy.run_path(str(ref / "Utils" / "FDMcoeffs.py"))  # the script prints its blend
 up7 = ns["fluxCoeff"](8, -4)
 cd6 = np.concatenate(([0.0], ns["fluxCoeff"](7, -3)))

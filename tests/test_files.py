@@ -313,6 +313,18 @@ def test_checksums_catch_damage(tmp_path):
         h5.H5File(str(tmp_path / "sb.h5"))
 
 
+# Cartesian coordinates of each rank of MPI_Cart_create (run.jl:117 with reorder off), written
+# out from the MPI standard's rule (ranks in row-major order of the coordinates, the last
+# dimension varying fastest) rather than computed, so a wrong ordering in assemble_checkpoint
+# cannot cancel against the same mistake here.
+CART_COORDS = {
+    (1, 1, 1): [(0, 0, 0)],
+    (2, 1, 1): [(0, 0, 0), (1, 0, 0)],
+    (2, 3, 2): [(0, 0, 0), (0, 0, 1), (0, 1, 0), (0, 1, 1), (0, 2, 0), (0, 2, 1),
+                (1, 0, 0), (1, 0, 1), (1, 1, 0), (1, 1, 1), (1, 2, 0), (1, 2, 1)],
+}
+
+
 @pytest.mark.parametrize("nprocs", [(1, 1, 1), (2, 1, 1), (2, 3, 2)])
 def test_assemble_multi_rank_checkpoint(tmp_path, nprocs):
     """Blocks cut from a global field with their ghost frames, as each rank of a multi-GPU
@@ -323,7 +335,7 @@ def test_assemble_multi_rank_checkpoint(tmp_path, nprocs):
     G0 = rng.standard_normal((6, pz * nzp + 2 * NG, py * nyp + 2 * NG, px * nxp + 2 * NG)).astype(np.float32)
     blocks = []
     for r in range(px * py * pz):
-        cx, cy, cz = r // (py * pz), (r // pz) % py, r % pz  # MPI_Cart_create: row-major, z fastest
+        cx, cy, cz = CART_COORDS[nprocs][r]
         blocks.append(G0[:, cz * nzp:(cz + 1) * nzp + 2 * NG, cy * nyp:(cy + 1) * nyp + 2 * NG,
                          cx * nxp:(cx + 1) * nxp + 2 * NG])
     p = h5.write(str(tmp_path / "chk.h5"), {"Q_h": np.stack(blocks)})

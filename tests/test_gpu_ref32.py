@@ -67,8 +67,9 @@ def _case(bcs="periodic", seed=41, spikes=20, n=(24, 16, 12), **kw):
     P64 = make_params(*n, bc=BCS[bcs], **kw)
     x, y, z = curvilinear_coords(P64)
     Q0 = random_state(P64, seed, spikes)
-    if kw.get("viscous"):
-        Q0[5] = Q0[4] / (Q0[0] * P64.rg)
+    if kw.get("viscous"):  # T at the interior (the ghosts are filled by the oracle below)
+        I = (slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+        Q0[5][I] = Q0[4][I] / (Q0[0][I] * P64.rg)
     m, J, Q, U = orc.prepare(P64, Q0, x, y, z)
     P = params_copy(P64, precision=PREC_REF32)
     m32, J32, U32 = [a.astype(f32) for a in m], J.astype(f32), U.astype(f32)
