@@ -178,6 +178,31 @@ def workload_flops_per_cell() -> float:
     return float(oc["add"] + oc["mul"] + oc["div"] + oc["sqrt"]) / cells
 
 
+def rhs_parity(rhs_gpu) -> dict:
+    """The FP64 RHS of the workload's initial state against the oracle (the checker, outside
+    the timed region): relative L-inf per variable, and the difference relative to the flux
+    scale (per variable, max of J times the summed face fluxes the RHS differences), beside
+    the oracle's own distance from an extended-precision evaluation."""
+    import numpy as np
+
+    from flame3d_mhd_gb300 import cases
+    from oracle import oracle as orc
+    c = cases.sod(**WORKLOAD)
+    P = c["params"]
+    m, J, Q, _ = orc.prepare(P, c["Q"], c["x"], c["y"], c["z"])
+    ro = orc.rhs(P, Q, m, J)
+    rl, scale = orc.rhs_ld(P, Q, m, J)
+    I = (slice(NG, -NG),) * 3
+    r = np.asarray(rhs_gpu)
+
+    def rel(a, b):
+        return max(float(np.abs(a[n][I] - b[n][I]).max() / np.abs(b[n][I]).max()) for n in range(5))
+    scaled = max(float(np.abs(r[n][I] - ro[n][I]).max() / scale[n]) for n in range(5))
+    return {"rhs_rel_linf": rel(r, ro), "rhs_flux_scaled": scaled, "rhs_rel_linf_vs_extended": rel(r, rl),
+            "oracle_rel_linf_vs_extended": rel(ro, rl), "tolerance": 1e-12,
+            "note": "FP64 RHS of the initial state vs the oracle; flux-scaled = |GPU - oracle| / max J sum|F|"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -500,6 +525,7 @@ def run_ours(args):
                                   "note": "flops from the oracle's exact op count (CPU leg); GPU divides "
                                           "and square roots cost ~10 FMA slots each but count as 1"}
     if rank == 0 and ws == 1 and not args.no_cpu:
+        line["parity"] = rhs_parity(r64.cpu().numpy())
         line["cpu_baseline"] = cpu_sample()
         f = workload_flops_per_cell()
         ach = f * value * 1e6 / ws / 1e12

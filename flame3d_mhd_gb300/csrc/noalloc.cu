@@ -1,10 +1,10 @@
 // noalloc.cu — f3d_rhs_noalloc: the right-hand side without any device allocation.
 //
 // f3d_rhs needs a context, and f3d_create obtains the context's scratch with cudaMalloc.
-// Some callers cannot allocate device memory: code that runs while a stream is being
-// captured into a CUDA graph, and hosts whose memory pool owns all device memory and
-// forbids foreign cudaMalloc/cudaFree (cudaFree also synchronises the whole device, which
-// a time-critical loop cannot afford). f3d_rhs_noalloc serves them: it takes the parameters,
+// Some callers cannot allocate device memory: hosts whose memory pool has reserved the
+// device's memory and forbids foreign cudaMalloc/cudaFree (a framework allocator, or a job
+// held to a fixed device-memory quota), and time-critical loops that cannot afford
+// cudaFree's implicit synchronisation of the whole device. f3d_rhs_noalloc serves them: it takes the parameters,
 // metrics and arrays directly, and keeps its scratch in one file-scope __device__ array of
 // F3D_NOALLOC_SCRATCH_BYTES that the module holds on every GPU that loads the library,
 // until the process exits.

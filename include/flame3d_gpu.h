@@ -227,16 +227,19 @@ int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream);
 #define F3D_NOALLOC_SCRATCH_BYTES (32 * 1024 * 1024)
 
 /* The same dUdt as f3d_create + f3d_set_metrics + f3d_rhs, for callers that cannot
- * allocate device memory: code running while its stream is captured into a CUDA graph, or
- * hosts whose memory pool owns the device and forbids cudaMalloc/cudaFree (cudaFree would
- * also synchronise the device). No context is needed: p, the nine metrics, J, the
+ * allocate device memory: a host whose memory pool has reserved the device's memory and
+ * forbids foreign cudaMalloc/cudaFree (a framework allocator, or a job held to a fixed
+ * device-memory quota), or a time-critical loop that cannot afford cudaFree's implicit
+ * synchronisation of the whole device. No context is needed: p, the nine metrics, J, the
  * ghost-filled Q and dUdt are the caller's; nothing is allocated and no allocating library
  * routine is called. Scratch (|A|, A/|A|, sound speed, sensor and, when viscous, the
  * viscous fluxes: 14 (Nx+8)(Ny+8)(Nz+8) doubles + 12 (Nx+4)(Ny+4)(Nz+4) doubles) lives in
  * one shared device array of F3D_NOALLOC_SCRATCH_BYTES; larger grids return
  * F3D_ERR_TOO_LARGE (about 58^3 interior cells inviscid, 48^3 viscous). The first call on
- * a device looks up that array's device address and sets kernel attributes for that
- * device: make it before any stream capture. Every call uses the same array and leaves its
+ * a device looks up that array's device address (cudaGetSymbolAddress, with that device
+ * current) and sets kernel attributes for that device; the address is kept for the rest of
+ * the process, so a cudaDeviceReset of that device leaves the entry point unusable. Make the
+ * first call before any stream capture. Every call uses the same array and leaves its
  * contents behind, so calls whose kernels overlap on the GPU (on different streams or host
  * threads) race: serialise them. Returns F3D_* codes; messages go to stderr.
  * This entry point has no counterpart in the reference, whose kernels take preallocated

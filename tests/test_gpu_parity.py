@@ -241,6 +241,9 @@ RHS_CASES = {
 # so any two FP64 evaluations differ by that much. For every case the test asserts that the
 # GPU is as accurate as the FP64 oracle (distance to the extended-precision result within 2x
 # the oracle's) and that GPU and oracle differ by at most 3x the oracle's own rounding error.
+# On every case the difference from the FP64 oracle relative to the flux scale (per
+# variable, the largest J x summed face flux the RHS differences: the size of the terms that
+# cancel) is asserted <= 1e-12.
 STRICT = {"random_all4_char", "random_default_bcs_viscous", "random_LF", "random_VL_comp", "random_AUSM"}
 
 
@@ -261,6 +264,7 @@ def test_rhs_parity(gpu_lib, name):
     r = host(c.s.rhs(dev(c.Q)))
     plain, scaled, gpu_ld, orc_ld = rhs_errors(c, r)
     msg = f"plain {plain:.2e} flux-scaled {scaled:.2e} gpu-vs-ld {gpu_ld:.2e} oracle-vs-ld {orc_ld:.2e}"
+    assert scaled <= RHS_TOL, msg
     assert gpu_ld <= max(RHS_TOL, 2.0 * orc_ld), msg
     assert plain <= max(RHS_TOL, 3.0 * orc_ld), msg
     if name in STRICT:

@@ -1,12 +1,15 @@
 """f3d_rhs_noalloc: the RHS for callers that cannot allocate device memory.
 
-Such callers (code running inside a CUDA-graph stream capture, or hosts whose memory pool
-owns the device and forbids cudaMalloc/cudaFree) get the RHS without a context: the
-entry point keeps its scratch in a fixed device array of the library. This test calls it
-through the C ABI twice in a row, on two different grids and states, and checks each result
-against the context-based f3d_rhs at the parity tolerance. The array keeps the previous
-call's contents, so the second call also shows that nothing stale leaks into a result.
-The file is collected last so that a run stopping at the first failure has run the rest.
+Such callers (a host whose memory pool has reserved the device's memory and forbids
+foreign cudaMalloc/cudaFree, or a loop that cannot afford cudaFree's device-wide
+synchronisation) get the RHS without a context: the entry point keeps its scratch in a fixed
+device array of the library. This test calls it through the C ABI three times in a row:
+two viscous grids of different sizes and states, then an inviscid shock tube. Each result is
+checked against the CPU oracle at the RHS parity tolerance (relative to the flux scale, as
+tests/test_gpu_parity.py states it) and against the context-based f3d_rhs. The array keeps
+the previous call's contents, and the second viscous call reads viscous-flux scratch the
+first one left behind at other offsets, so a stale value would show in its result. The file
+is collected last so that a run stopping at the first failure has run the rest.
 """
 import ctypes as C
 
@@ -29,17 +32,17 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def _viscous_hybrid_inputs():
-    """24x16x12 curvilinear grid, reference boundary conditions, viscous, hybrid scheme."""
-    P = make_params(24, 16, 12, rg=1.0, c_s=1e-2, t_s=1.0, phi1=0.02, phi2=0.1, phi3=0.4)
+def _viscous_hybrid_inputs(n=(24, 16, 12), seed=21, amp=0.03):
+    """Curvilinear grid, reference boundary conditions, viscous, hybrid scheme."""
+    P = make_params(*n, viscous=1, rg=1.0, c_s=1e-2, t_s=1.0, phi1=0.02, phi2=0.1, phi3=0.4)
     s = (P.nz + 8, P.ny + 8, P.nx + 8)
-    ax = [(np.arange(n) - NG + 0.5) / (n - 8) for n in s]
+    ax = [(np.arange(k) - NG + 0.5) / (k - 8) for k in s]
     Z, E, X = np.meshgrid(*ax, indexing="ij")
     tp = 2 * np.pi
-    x = X + 0.03 * np.sin(tp * E) * np.sin(tp * Z)
-    y = E + 0.03 * np.sin(tp * Z) * np.sin(tp * X)
-    z = Z + 0.03 * np.sin(tp * X) * np.sin(tp * E)
-    rng = np.random.default_rng(21)
+    x = X + amp * np.sin(tp * E) * np.sin(tp * Z)
+    y = E + amp * np.sin(tp * Z) * np.sin(tp * X)
+    z = Z + amp * np.sin(tp * X) * np.sin(tp * E)
+    rng = np.random.default_rng(seed)
     Q = np.zeros((6, *s))
     Q[0] = 1.0 + 0.1 * rng.uniform(-1, 1, s)
     Q[1:4] = 0.2 * rng.uniform(-1, 1, (3, *s))
@@ -54,29 +57,50 @@ def _sod_inputs():
     return c["params"], c["Q"], c["x"], c["y"], c["z"]
 
 
-def _rhs_both(lib, P, Q0, x, y, z):
+def _noalloc_call(lib, P, Q0, x, y, z):
+    """f3d_rhs_noalloc through the C ABI; returns its interior result, f3d_rhs's, and the
+    oracle-prepared inputs."""
     m, J, Q, _ = orc.prepare(P, Q0, x, y, z)
     md, Jd, Qd = [_dev(a) for a in m], _dev(J), _dev(Q)
-    out = torch.zeros((5, *Q.shape[1:]), dtype=torch.float64, device="cuda")
+    out = torch.full((5, *Q.shape[1:]), float("nan"), dtype=torch.float64, device="cuda")
     arr = (C.c_void_p * 9)(*[C.c_void_p(a.data_ptr()) for a in md])
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     rc = lib.f3d_rhs_noalloc(C.byref(P), arr, C.c_void_p(Jd.data_ptr()), C.c_void_p(Qd.data_ptr()),
                              C.c_void_p(out.data_ptr()), stream)
     assert rc == abi.F3D_OK
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
     ref_solver = Flame3D(P)
     ref_solver.set_metrics(md, Jd)
     ref = ref_solver.rhs(Qd)
     torch.cuda.synchronize()
     ref_solver.close()
     I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
-    return out.cpu().numpy()[I], ref.cpu().numpy()[I]
+    return got[I], ref.cpu().numpy()[I], (P, Q, m, J)
 
 
-def test_rhs_noalloc_matches_rhs_twice(gpu_lib):
+def _check_against_oracle(got, inputs):
+    """The parity bar of tests/test_gpu_parity.py: error relative to the flux scale <= 1e-12,
+    and no less accurate than the FP64 oracle against an extended-precision evaluation."""
+    P, Q, m, J = inputs
+    I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+    ro = orc.rhs(P, Q, m, J)[I]
+    rl, scale = orc.rhs_ld(P, Q, m, J)
+    rl = rl[I]
+    scaled = max(float(np.abs(got[n] - ro[n]).max() / scale[n]) for n in range(5))
+    assert scaled <= TOL, scaled
+    assert rel_linf(got, rl) <= max(TOL, 2.0 * rel_linf(ro, rl))
+
+
+def test_rhs_noalloc_three_calls_in_a_row(gpu_lib):
     lib = gpu_lib
-    for make in (_viscous_hybrid_inputs, _sod_inputs):
-        got, ref = _rhs_both(lib, *make())
+    runs = [lambda: _viscous_hybrid_inputs((24, 16, 12), 21, 0.03),
+            lambda: _viscous_hybrid_inputs((20, 12, 16), 22, 0.05),  # other grid: other offsets
+            _sod_inputs]
+    for make in runs:
+        got, ref, inputs = _noalloc_call(lib, *make())
         assert np.isfinite(got).all()
+        _check_against_oracle(got, inputs)
         assert rel_linf(got, ref) <= TOL
 
 
