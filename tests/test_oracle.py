@@ -276,7 +276,7 @@ def test_golden_fixtures():
     import json
     from pathlib import Path
     gdir = Path(__file__).resolve().parent / "golden"
-    files = sorted(gdir.glob("*.npz"))
+    files = [f for f in sorted(gdir.glob("*.npz")) if "rhs" in np.load(f).files]  # RHS fixtures only
     assert files, "no golden fixtures"
     for f in files:
         g = np.load(f)
