@@ -196,8 +196,13 @@ struct f3d_ctx {
     MetricPtrs32 m32 = {};
     float* phi32 = nullptr;
     float* acc32 = nullptr;
+    float* acc32b = nullptr;  // mixed form: the eta sweep's differences (summed in FP64 by the last)
     float* Fv32[3] = {};
     double* dscalar = nullptr;  // 8 bytes for reductions
+    unsigned* kstat = nullptr;  // kernel status word (bit 0: a TMA tile wait gave up)
+    // mixed form: the TMA-staged sweeps and their tensor maps (three directions)
+    bool use_tma = false;
+    void* tma_maps = nullptr;
     Prof* prof = nullptr;
     // adjoint scratch, allocated by the first VJP call
     void* adj_slab = nullptr;
@@ -290,6 +295,7 @@ SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const 
     std::memset(&a, 0, sizeof(a));
     a.P = ctx->dp;
     a.J = ctx->J;
+    a.kstat = ctx->kstat;
     if (mixed(ctx) || ctx->dp.ref32) {
         a.fp32 = 1;
         a.Q = ctx->dp.ref32 ? Q32 : ctx->Q32;
@@ -391,8 +397,12 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
         SweepArgs a = sweep_args(ctx, d, Q, hybrid);
         a.acc = mx ? (void*)ctx->acc32 : (void*)acc;
         if (d == 0) a.out_mode = OUT_SET;
-        else if (d == 1) a.out_mode = OUT_ADD;
-        else {
+        else if (d == 1) {
+            // mixed: the eta differences go to their own array; the last sweep sums in FP64
+            a.out_mode = mx ? OUT_SET : OUT_ADD;
+            if (mx) a.acc = ctx->acc32b;
+        } else {
+            if (mx) a.acc2 = ctx->acc32b;
             a.out_mode = last.out_mode;
             a.out = last.out;
             a.U = last.U;
@@ -404,7 +414,8 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
             a.stage1_copy = last.stage1_copy;
             a.dtl = last.dtl;
         }
-        F3D_CUDA(ctx, launch_sweep(d, a, st));
+        if (ctx->use_tma) F3D_CUDA(ctx, launch_sweep_tma(d, a, ctx->tma_maps, st));
+        else F3D_CUDA(ctx, launch_sweep(d, a, st));
         mark(ctx, K_SWEEP_X + d, st);
     }
     return F3D_OK;
@@ -684,8 +695,8 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     const bool fvm = p->scheme != F3D_SCHEME_FDM;
     if (!mx) {  // S(3) + A/|A|(9) + sound speed + phi + acc(5) [+ viscous 12] [+ FVM 12 + 5]
         total += up(nc * 8) * (3 + 9 + 1 + 1 + 5 + (fvm ? 17 : 0)) + (p->viscous ? 3 * up(nv * 4 * 8) : 0);
-    } else {    // [Q32(6) + A32(9) + J32, mixed only] + H32(9) + S32(3) + phi32 + acc32(5) [+ viscous 12]
-        total += up(nc * 4) * ((r32 ? 0 : 16) + 9 + 3 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 4) : 0);
+    } else {    // [Q32(6) + A32(9) + J32 + acc32b(5), mixed only] + H32(9) + S32(3) + phi32 + acc32(5) [+ viscous 12]
+        total += up(nc * 4) * ((r32 ? 0 : 21) + 9 + 3 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 4) : 0);
     }
     cudaError_t e = cudaMalloc(&ctx->slab, total);
     if (e != cudaSuccess) {
@@ -715,11 +726,19 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
         const size_t b1 = up(nc * 4);
         if (!r32) {  // the reference form reads the caller's Float32 Q, metrics and J
             ctx->Q32 = (float*)q; q += 6 * b1;
-            for (int n = 0; n < 9; n++) { ctx->m32.A[n] = (float*)q; q += b1; }
+            // one pack of seven planes per direction, b1 bytes apart: A_d (3), A_d/|A_d| (3),
+            // |A_d| — the tensor the TMA sweeps copy a tile of at once
+            for (int d = 0; d < 3; d++) {
+                for (int n = 0; n < 3; n++) { ctx->m32.A[3 * d + n] = (float*)q; q += b1; }
+                for (int n = 0; n < 3; n++) { ctx->m32.H[3 * d + n] = (float*)q; q += b1; }
+                ctx->m32.S[d] = (float*)q; q += b1;
+            }
             ctx->m32.J = (float*)q; q += b1;
+            ctx->acc32b = (float*)q; q += 5 * b1;
+        } else {
+            for (int n = 0; n < 9; n++) { ctx->m32.H[n] = (float*)q; q += b1; }
+            for (int d = 0; d < 3; d++) { ctx->m32.S[d] = (float*)q; q += b1; }
         }
-        for (int n = 0; n < 9; n++) { ctx->m32.H[n] = (float*)q; q += b1; }
-        for (int d = 0; d < 3; d++) { ctx->m32.S[d] = (float*)q; q += b1; }
         ctx->phi32 = (float*)q; q += b1;
         ctx->acc32 = (float*)q; q += 5 * b1;
         if (p->viscous)
@@ -727,14 +746,32 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
         phi_bytes = b1;
     }
     ctx->dscalar = (double*)q;
+    ctx->kstat = (unsigned*)(q + 8);
+    // the TMA-staged FP32 sweeps for the mixed form (F3D_NO_TMA=1 selects the direct-load
+    // sweeps, for comparison)
+    const char* no_tma = std::getenv("F3D_NO_TMA");
+    const bool want_tma = p->precision == F3D_PREC_MIXED && !fvm && sweep_tma_usable(ctx->dp) &&
+                          !(no_tma && no_tma[0] == '1');
     // phi outside cells 1..Nt-2 is never written; keep it defined (CUDA.zeros in solver.jl:296)
     if ((e = cudaMemset(mx ? (void*)ctx->phi32 : (void*)ctx->phi, 0, phi_bytes)) != cudaSuccess ||
-        (e = sweep_configure()) != cudaSuccess || (fvm && (e = fvm_configure()) != cudaSuccess)) {
+        (e = cudaMemset(q, 0, 16)) != cudaSuccess || (e = sweep_configure()) != cudaSuccess ||
+        (fvm && (e = fvm_configure()) != cudaSuccess) || (want_tma && (e = sweep_tma_configure()) != cudaSuccess)) {
         cudaFree(ctx->slab);
         if (ctx->extra) cudaFree(ctx->extra);
         delete ctx;
         std::fprintf(stderr, "f3d_create: %s\n", cudaGetErrorString(e));
         return F3D_ERR_CUDA;
+    }
+    if (want_tma) {
+        ctx->tma_maps = std::aligned_alloc(64, (sweep_maps_bytes() + 63) & ~(size_t)63);
+        const float* pack[3] = {ctx->m32.A[0], ctx->m32.A[3], ctx->m32.A[6]};
+        if (ctx->tma_maps &&
+            make_sweep_maps(ctx->dp, ctx->Q32, pack, up(nc * 4), ctx->phi32, ctx->tma_maps) == cudaSuccess) {
+            ctx->use_tma = true;
+        } else {  // no tensor maps on this driver: the direct-load sweeps
+            std::free(ctx->tma_maps);
+            ctx->tma_maps = nullptr;
+        }
     }
     *out = ctx;
     return F3D_OK;
@@ -747,6 +784,7 @@ int f3d_destroy(f3d_ctx* ctx) {
     if (ctx->adj_slab) cudaFree(ctx->adj_slab);
     if (ctx->lsave) cudaFree(ctx->lsave);
     if (ctx->extra) cudaFree(ctx->extra);
+    std::free(ctx->tma_maps);
     cudaError_t e = cudaFree(ctx->slab);
     delete ctx;
     return e == cudaSuccess ? F3D_OK : F3D_ERR_CUDA;
@@ -1210,12 +1248,14 @@ int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream) {
     int rc = check_ctx(ctx, false);
     if (rc || (rc = check_ptrs(ctx, {U}))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    int flag = 0;
+    int flag[2] = {0, 0};  // the non-finite flag, then the kernel status word
     F3D_CUDA(ctx, cudaMemsetAsync(ctx->dscalar, 0, 8, st));
     F3D_CUDA(ctx, launch_check_finite(ctx->dp, U, (int*)ctx->dscalar, st));
-    F3D_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->dscalar, 4, cudaMemcpyDeviceToHost, st));
+    F3D_CUDA(ctx, cudaMemcpyAsync(&flag[0], ctx->dscalar, 4, cudaMemcpyDeviceToHost, st));
+    F3D_CUDA(ctx, cudaMemcpyAsync(&flag[1], ctx->kstat, 4, cudaMemcpyDeviceToHost, st));
     F3D_CUDA(ctx, cudaStreamSynchronize(st));
-    return flag ? fail(ctx, F3D_ERR_NONFINITE, "non-finite value in U") : F3D_OK;
+    if (flag[1]) return fail(ctx, F3D_ERR_CUDA, "a sweep's tile copy did not complete (kernel status word set)");
+    return flag[0] ? fail(ctx, F3D_ERR_NONFINITE, "non-finite value in U") : F3D_OK;
 }
 
 int f3d_debug_sensor(f3d_ctx* ctx, const double* Q, double* phi, f3d_stream stream) {

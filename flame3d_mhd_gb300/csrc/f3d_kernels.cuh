@@ -23,6 +23,8 @@ struct SweepArgs {
     const void* Fv;       // viscous flux of this direction ((Nt-4)^3 x 4) or null
     const double* J;      // Jacobian
     void* acc;            // RHS accumulator (U layout)
+    const float* acc2;    // mixed form, last sweep: the eta sweep's own differences (FP32);
+                          // the three directions are then summed in FP64 (null otherwise)
     double* out;          // OUT_RHS destination (may alias acc in the FP64 form)
     double* U;            // OUT_STAGE state, updated in place
     double* Un;           // OUT_STAGE stage-start copy
@@ -39,6 +41,7 @@ struct SweepArgs {
     float* U32;           // OUT_STAGE state
     float* Un32;          // OUT_STAGE stage-start copy
     float dt32, ca32, cb32;
+    unsigned* kstat;      // kernel status word of the context (bit 0: a TMA tile wait gave up)
 };
 
 // Metric and Jacobian cotangents accumulated by the viscous VJP (null m[0]: none)
@@ -84,6 +87,14 @@ DevParams make_dev_params(const f3d_params& p);
 
 cudaError_t sweep_configure();
 cudaError_t launch_sweep(int dir, const SweepArgs& a, cudaStream_t st);
+// TMA-staged FP32 sweeps of the mixed form (k_sweep_tma.cu): usable when the x extent with
+// ghosts is a multiple of 4; maps3 holds the three directions' tensor maps
+bool sweep_tma_usable(const DevParams& P);
+cudaError_t sweep_tma_configure();
+size_t sweep_maps_bytes();
+cudaError_t make_sweep_maps(const DevParams& P, const float* q32, const float* const pack[3], size_t pack_stride,
+                            const float* phi, void* maps3);
+cudaError_t launch_sweep_tma(int dir, const SweepArgs& a, const void* maps3, cudaStream_t st);
 
 // finite-volume scheme (k_fvm.cu): geo = (nx, ny, nz, area) of the faces of x, y, z at
 // their left cells; U the conserved state the faces reconstruct from

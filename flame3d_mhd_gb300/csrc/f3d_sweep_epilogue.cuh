@@ -86,6 +86,12 @@ __device__ __forceinline__ void sweep_epilogue(const SweepArgs& a, const R* sF, 
                 continue;
             }
         }
+        // sum of the three directions: in the arithmetic type, or (mixed form, acc2 set) the
+        // xi and eta sweeps' FP32 differences and this sweep's, converted exactly and added in FP64
+        auto total = [&](int n) -> double {
+            if (a.acc2) return (to_f64(acc[c + n * pl]) + to_f64(a.acc2[c + n * pl])) + to_f64(d[n]);
+            return to_f64(acc[c + n * pl] + d[n]);
+        };
         if (a.out_mode == OUT_SET) {
 #pragma unroll
             for (int n = 0; n < 5; n++) acc[c + n * pl] = d[n];
@@ -95,14 +101,14 @@ __device__ __forceinline__ void sweep_epilogue(const SweepArgs& a, const R* sF, 
         } else if (a.out_mode == OUT_RHS) {
             const double Jc = a.J[c];
 #pragma unroll
-            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * to_f64(acc[c + n * pl] + d[n]);
+            for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * total(n);
         } else {  // OUT_STAGE: RK state accumulation in FP64
             const double Jact = a.J[c] * (a.dtl ? a.dtl[c] : a.dt);  // div_LTS: per-cell dt
 #pragma unroll
             for (int n = 0; n < 5; n++) {
                 const double u = a.U[c + n * pl];
                 if (a.stage1_copy) a.Un[c + n * pl] = u;
-                double un = u + to_f64(acc[c + n * pl] + d[n]) * Jact;
+                double un = u + total(n) * Jact;
                 if (a.combine) un = un * a.ca + a.Un[c + n * pl] * a.cb;
                 a.U[c + n * pl] = un;
             }

@@ -138,18 +138,9 @@ __device__ __forceinline__ double fvm_weno7(const double V[7], double ss) {
     const double q2 = V2 - 5.0 * V3 + 13.0 * V4 + 3.0 * V5;
     const double q3 = -V3 + 7.0 * V4 + 7.0 * V5 - V6;
     const double q4 = 3.0 * V4 + 13.0 * V5 - 5.0 * V6 + V7;
-    const double I1 = V1 * (547.0 * V1 - 3882.0 * V2 + 4642.0 * V3 - 1854.0 * V4) +
-                      V2 * (7043.0 * V2 - 17246.0 * V3 + 7042.0 * V4) + V3 * (11003.0 * V3 - 9402.0 * V4) +
-                      V4 * (2107.0 * V4);
-    const double I2 = V2 * (267.0 * V2 - 1642.0 * V3 + 1602.0 * V4 - 494.0 * V5) +
-                      V3 * (2843.0 * V3 - 5966.0 * V4 + 1922.0 * V5) + V4 * (3443.0 * V4 - 2522.0 * V5) +
-                      V5 * (547.0 * V5);
-    const double I3 = V3 * (547.0 * V3 - 2522.0 * V4 + 1922.0 * V5 - 494.0 * V6) +
-                      V4 * (3443.0 * V4 - 5966.0 * V5 + 1602.0 * V6) + V5 * (2843.0 * V5 - 1642.0 * V6) +
-                      V6 * (267.0 * V6);
-    const double I4 = V4 * (2107.0 * V4 - 9402.0 * V5 + 7042.0 * V6 - 1854.0 * V7) +
-                      V5 * (11003.0 * V5 - 17246.0 * V6 + 4642.0 * V7) + V6 * (7043.0 * V6 - 3882.0 * V7) +
-                      V7 * (547.0 * V7);
+    double Is[4];  // the smoothness indicators in difference form (weno7_is, f3d_flux.cuh)
+    weno7_is<double>(V, Is);
+    const double I1 = Is[0], I2 = Is[1], I3 = Is[2], I4 = Is[3];
     // alpha_k = d_k / t_k^2 with t_k = 1e-10 + IS_k ss, normalised: one divide
     const double t1 = 1e-10 + I1 * ss, t2 = 1e-10 + I2 * ss, t3 = 1e-10 + I3 * ss, t4 = 1e-10 + I4 * ss;
     return weno7_combine(t1, t2, t3, t4, q1, q2, q3, q4) * (1.0 / 12.0);

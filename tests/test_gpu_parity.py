@@ -232,39 +232,41 @@ RHS_CASES = {
 }
 
 
-# Plain relative L-inf <= 1e-12 is asserted where the RHS is not much smaller than the
-# fluxes it differences and WENO weights are not degenerate: the random curvilinear states
-# (measured 2e-15 .. 2.5e-13). On the Taylor-Green vortex (RHS ~1e3 below the flux
-# magnitude) and the noisy shock tube (WENO7 faces across the jump, where smoothness
-# indicators of the smooth sub-stencils cancel to ~1e-8 relative), the FP64 restatement
-# itself is 9e-12 / 2.9e-11 away from an extended-precision evaluation of the same formulas,
-# so any two FP64 evaluations differ by that much. For every case the test asserts that the
-# GPU is as accurate as the FP64 oracle (distance to the extended-precision result within 2x
-# the oracle's) and that GPU and oracle differ by at most 3x the oracle's own rounding error.
-# On every case the difference from the FP64 oracle relative to the flux scale (per
-# variable, the largest J x summed face flux the RHS differences: the size of the terms that
-# cancel) is asserted <= 1e-12.
+# The 1e-12 bar is asserted against the exact value of the reference's formulas: the oracle's
+# extended-precision evaluation (long double). The difference |GPU - extended| relative to the
+# flux scale (per variable, the largest J x summed face flux the RHS differences: the size of
+# the terms that cancel) must be <= 1e-12 on every case. Beside it: plain relative L-inf
+# against the FP64 oracle <= 1e-12 on the random curvilinear states (STRICT, measured 2e-15 ..
+# 2.5e-13), and elsewhere <= 3x the FP64 oracle's own distance from the extended evaluation.
+# On the Taylor-Green vortex (RHS ~1e3 below the fluxes it differences) and the noisy shock
+# tube the FP64 oracle itself is 9e-12 / 3e-11 (6e-11 at 256x64x64) from the extended result:
+# it evaluates the WENO7 smoothness indicators in the reference's expanded quadratic form,
+# whose cancellation costs up to 1e-9 of their value, while the GPU evaluates the same
+# indicators as a weighted sum of squares of stencil differences (f3d_flux.cuh, weno7_is).
 STRICT = {"random_all4_char", "random_default_bcs_viscous", "random_LF", "random_VL_comp", "random_AUSM"}
 
 
 def rhs_errors(c, r):
-    """(plain rel L-inf vs the FP64 oracle, error relative to the flux scale, GPU error vs
-    extended precision, FP64-oracle error vs extended precision)."""
+    """(plain rel L-inf vs the FP64 oracle, |GPU - FP64 oracle| over the flux scale,
+    |GPU - extended| over the flux scale, GPU error vs extended precision, FP64-oracle error vs
+    extended precision)."""
     I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
     ro = orc.rhs(c.P, c.Q, c.m, c.J)
     rl, scale = orc.rhs_ld(c.P, c.Q, c.m, c.J)
     plain = rel_linf(r[I], ro[I])
     scaled = max(float(np.abs(r[n][I[1:]] - ro[n][I[1:]]).max() / scale[n]) for n in range(5))
-    return plain, scaled, rel_linf(r[I], rl[I]), rel_linf(ro[I], rl[I])
+    scaled_ld = max(float(np.abs(r[n][I[1:]] - rl[n][I[1:]]).max() / scale[n]) for n in range(5))
+    return plain, scaled, scaled_ld, rel_linf(r[I], rl[I]), rel_linf(ro[I], rl[I])
 
 
 @pytest.mark.parametrize("name", sorted(RHS_CASES))
 def test_rhs_parity(gpu_lib, name):
     c = RHS_CASES[name]()
     r = host(c.s.rhs(dev(c.Q)))
-    plain, scaled, gpu_ld, orc_ld = rhs_errors(c, r)
-    msg = f"plain {plain:.2e} flux-scaled {scaled:.2e} gpu-vs-ld {gpu_ld:.2e} oracle-vs-ld {orc_ld:.2e}"
-    assert scaled <= RHS_TOL, msg
+    plain, scaled, scaled_ld, gpu_ld, orc_ld = rhs_errors(c, r)
+    msg = (f"plain {plain:.2e} flux-scaled {scaled:.2e} flux-scaled vs extended {scaled_ld:.2e} "
+           f"gpu-vs-ld {gpu_ld:.2e} oracle-vs-ld {orc_ld:.2e}")
+    assert scaled_ld <= RHS_TOL, msg
     assert gpu_ld <= max(RHS_TOL, 2.0 * orc_ld), msg
     assert plain <= max(RHS_TOL, 3.0 * orc_ld), msg
     if name in STRICT:

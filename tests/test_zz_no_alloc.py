@@ -5,8 +5,8 @@ foreign cudaMalloc/cudaFree, or a loop that cannot afford cudaFree's device-wide
 synchronisation) get the RHS without a context: the entry point keeps its scratch in a fixed
 device array of the library. This test calls it through the C ABI three times in a row:
 two viscous grids of different sizes and states, then an inviscid shock tube. Each result is
-checked against the CPU oracle at the RHS parity tolerance (relative to the flux scale, as
-tests/test_gpu_parity.py states it) and against the context-based f3d_rhs. The array keeps
+checked against the CPU oracle at the RHS parity tolerance (as tests/test_gpu_parity.py
+states it) and against the context-based f3d_rhs. The array keeps
 the previous call's contents, and the second viscous call reads viscous-flux scratch the
 first one left behind at other offsets, so a stale value would show in its result. The file
 is collected last so that a run stopping at the first failure has run the rest.
@@ -80,16 +80,17 @@ def _noalloc_call(lib, P, Q0, x, y, z):
 
 
 def _check_against_oracle(got, inputs):
-    """The parity bar of tests/test_gpu_parity.py: error relative to the flux scale <= 1e-12,
-    and no less accurate than the FP64 oracle against an extended-precision evaluation."""
+    """The parity bar of tests/test_gpu_parity.py: the difference from the oracle's
+    extended-precision evaluation relative to the flux scale <= 1e-12, and against the FP64
+    oracle within 3x the oracle's own rounding."""
     P, Q, m, J = inputs
     I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
     ro = orc.rhs(P, Q, m, J)[I]
     rl, scale = orc.rhs_ld(P, Q, m, J)
     rl = rl[I]
-    scaled = max(float(np.abs(got[n] - ro[n]).max() / scale[n]) for n in range(5))
+    scaled = max(float(np.abs(got[n] - rl[n]).max() / scale[n]) for n in range(5))
     assert scaled <= TOL, scaled
-    assert rel_linf(got, rl) <= max(TOL, 2.0 * rel_linf(ro, rl))
+    assert rel_linf(got, ro) <= max(TOL, 3.0 * rel_linf(ro, rl))
 
 
 def test_rhs_noalloc_three_calls_in_a_row(gpu_lib):
