@@ -200,6 +200,7 @@ struct f3d_ctx {
     float* Fv32[3] = {};
     double* dscalar = nullptr;  // 8 bytes for reductions
     unsigned* kstat = nullptr;  // kernel status word (bit 0: a TMA tile wait gave up)
+    unsigned* tile_ctr = nullptr;  // next-tile counters of the TMA sweeps
     // mixed form: the TMA-staged sweeps and their tensor maps (three directions)
     bool use_tma = false;
     void* tma_maps = nullptr;
@@ -296,6 +297,7 @@ SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const 
     a.P = ctx->dp;
     a.J = ctx->J;
     a.kstat = ctx->kstat;
+    a.tile_ctr = ctx->tile_ctr;
     if (mixed(ctx) || ctx->dp.ref32) {
         a.fp32 = 1;
         a.Q = ctx->dp.ref32 ? Q32 : ctx->Q32;
@@ -393,6 +395,7 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
             mark(ctx, K_VISCOUS, st);
         }
     }
+    if (ctx->use_tma) F3D_CUDA(ctx, cudaMemsetAsync(ctx->tile_ctr, 0, 3 * sizeof(unsigned), st));
     for (int d = 0; d < 3; d++) {
         SweepArgs a = sweep_args(ctx, d, Q, hybrid);
         a.acc = mx ? (void*)ctx->acc32 : (void*)acc;
@@ -463,9 +466,6 @@ int adjoint_supported(f3d_ctx* ctx) {
         return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint has no local time stepping, filters or LES");
     if (ctx->params.scheme != F3D_SCHEME_FDM)
         return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for the finite-difference scheme");
-    if (ctx->params.character) return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for component-wise reconstruction");
-    if (ctx->params.split_method != F3D_SPLIT_SW && ctx->params.split_method != F3D_SPLIT_LF)
-        return fail(ctx, F3D_ERR_UNSUPPORTED, "the adjoint is built for SW and LF splitting");
     return F3D_OK;
 }
 
@@ -747,6 +747,7 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     }
     ctx->dscalar = (double*)q;
     ctx->kstat = (unsigned*)(q + 8);
+    ctx->tile_ctr = (unsigned*)(q + 16);  // three counters
     // the TMA-staged FP32 sweeps for the mixed form (F3D_NO_TMA=1 selects the direct-load
     // sweeps, for comparison)
     const char* no_tma = std::getenv("F3D_NO_TMA");
@@ -754,7 +755,7 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
                           !(no_tma && no_tma[0] == '1');
     // phi outside cells 1..Nt-2 is never written; keep it defined (CUDA.zeros in solver.jl:296)
     if ((e = cudaMemset(mx ? (void*)ctx->phi32 : (void*)ctx->phi, 0, phi_bytes)) != cudaSuccess ||
-        (e = cudaMemset(q, 0, 16)) != cudaSuccess || (e = sweep_configure()) != cudaSuccess ||
+        (e = cudaMemset(q, 0, 32)) != cudaSuccess || (e = sweep_configure()) != cudaSuccess ||
         (fvm && (e = fvm_configure()) != cudaSuccess) || (want_tma && (e = sweep_tma_configure()) != cudaSuccess)) {
         cudaFree(ctx->slab);
         if (ctx->extra) cudaFree(ctx->extra);

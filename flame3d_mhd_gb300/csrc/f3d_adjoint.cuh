@@ -185,6 +185,155 @@ __device__ __forceinline__ void split_lf_vjp(const Cst<double>& K, const double 
     qb[4] += pb;
 }
 
+// van Leer (split.jl:110-183) and AUSM (split.jl:185-255): Mach-number splits with
+// c = sqrt(gamma p / rho) (the precomputed sound speed of those splits). The branch |M| >= 1
+// (all flux to one side) is frozen at the forward value, as every other switch.
+// mg (optional): cotangents {A1, A2, A3, -, -, -, |A|} +=.
+__device__ __forceinline__ void split_mach_vjp(int method, const Cst<double>& K, const double q[6], double c, double A1,
+                                               double A2, double A3, double ss, const double fpb[5],
+                                               const double fmb[5], double qb[6], double* mg = nullptr) {
+    const double rho = q[0], u = q[1], v = q[2], w = q[3], p = q[4];
+    const double g = K.gamma;
+    const bool vl = method == F3D_SPLIT_VL;
+    const double un = A1 * u + A2 * v + A3 * w;
+    const double M = un / (c * ss);  // the forward's expression, so the branch below is its branch
+    const double kin = u * u + v * v + w * w;
+    double rhob = 0, ub = 0, vb = 0, wb = 0, pb = 0, cb = 0, unb = 0, Mb = 0, kinb = 0, ssb = 0;
+    double Ab[3] = {0, 0, 0};
+    if (M <= -1.0 || M >= 1.0) {
+        const double* gb = M <= -1.0 ? fmb : fpb;  // the side that carries the whole flux
+        // full = (rho un, rho u un + A1 p, rho v un + A2 p, rho w un + A3 p, f4)
+        rhob += gb[0] * un + (gb[1] * u + gb[2] * v + gb[3] * w) * un;
+        unb += rho * (gb[0] + gb[1] * u + gb[2] * v + gb[3] * w);
+        ub += gb[1] * rho * un;
+        vb += gb[2] * rho * un;
+        wb += gb[3] * rho * un;
+        pb += A1 * gb[1] + A2 * gb[2] + A3 * gb[3];
+        Ab[0] += gb[1] * p;
+        Ab[1] += gb[2] * p;
+        Ab[2] += gb[3] * p;
+        if (vl) {  // f4 = (E0 + p) un, E0 = p/(g-1) + rho kin/2
+            const double E0 = p * K.inv_gm1 + 0.5 * rho * kin;
+            const double E0b = gb[4] * un;
+            pb += gb[4] * un + E0b * K.inv_gm1;
+            unb += gb[4] * (E0 + p);
+            rhob += E0b * 0.5 * kin;
+            kinb += E0b * 0.5 * rho;
+        } else {  // f4 = rho h un, h = g p / (rho (g-1)) + kin/2
+            const double h = g * p / (rho * K.gm1) + 0.5 * kin;
+            const double hb = gb[4] * rho * un;
+            rhob += gb[4] * h * un - hb * g * p / (rho * rho * K.gm1);
+            unb += gb[4] * rho * h;
+            pb += hb * g / (rho * K.gm1);
+            kinb += 0.5 * hb;
+        }
+    } else if (vl) {
+        const double unn = un / ss;
+        const double Mp = M + 1.0, Mm = M - 1.0;
+        const double f1p = rho * c * 0.25 * (Mp * Mp) * ss;
+        const double f1m = -rho * c * 0.25 * (Mm * Mm) * ss;
+        const double gs = g * ss;
+        const double t1 = (-unn + 2.0 * c) / gs, t2 = (-unn - 2.0 * c) / gs;
+        const double t3 = 1.0 / (2.0 * (g * g - 1.0));
+        const double ep = K.gm1 * unn + 2.0 * c, em = K.gm1 * unn - 2.0 * c;
+        const double t4 = 0.5 * (kin - unn * unn);
+        const double Bp[5] = {1.0, A1 * t1 + u, A2 * t1 + v, A3 * t1 + w, ep * ep * t3 + t4};
+        const double Bm[5] = {1.0, A1 * t2 + u, A2 * t2 + v, A3 * t2 + w, em * em * t3 + t4};
+        double f1pb = 0, f1mb = 0;
+        for (int n = 0; n < 5; n++) {
+            f1pb += fpb[n] * Bp[n];
+            f1mb += fmb[n] * Bm[n];
+        }
+        double t1b = 0, t2b = 0, t4b = 0, unnb = 0;
+        const double Ap[3] = {A1, A2, A3};
+        for (int j = 0; j < 3; j++) {
+            const double bp = f1p * fpb[1 + j], bm = f1m * fmb[1 + j];
+            t1b += Ap[j] * bp;
+            t2b += Ap[j] * bm;
+            Ab[j] += t1 * bp + t2 * bm;
+        }
+        ub += f1p * fpb[1] + f1m * fmb[1];
+        vb += f1p * fpb[2] + f1m * fmb[2];
+        wb += f1p * fpb[3] + f1m * fmb[3];
+        const double E4p = f1p * fpb[4], E4m = f1m * fmb[4];
+        const double epb = 2.0 * ep * t3 * E4p, emb = 2.0 * em * t3 * E4m;
+        t4b += E4p + E4m;
+        unnb += K.gm1 * (epb + emb);
+        cb += 2.0 * (epb - emb);
+        unnb -= (t1b + t2b) / gs;
+        cb += 2.0 * (t1b - t2b) / gs;
+        ssb -= (t1b * t1 + t2b * t2) / ss;
+        kinb += 0.5 * t4b;
+        unnb -= unn * t4b;
+        // f1p = rho c (M+1)^2 ss / 4, f1m = -rho c (M-1)^2 ss / 4
+        rhob += 0.25 * c * ss * (f1pb * Mp * Mp - f1mb * Mm * Mm);
+        cb += 0.25 * rho * ss * (f1pb * Mp * Mp - f1mb * Mm * Mm);
+        ssb += 0.25 * rho * c * (f1pb * Mp * Mp - f1mb * Mm * Mm);
+        Mb += 0.5 * rho * c * ss * (f1pb * Mp - f1mb * Mm);
+        unb += unnb / ss;
+        ssb -= unnb * unn / ss;
+    } else {  // AUSM, subsonic
+        const double Mp = M + 1.0, Mm = M - 1.0;
+        const double rcs = rho * c * ss;
+        const double f_p = 0.25 * (Mp * Mp) * rcs, f_m = -0.25 * (Mm * Mm) * rcs;
+        const double Pp = p * (0.25 * (Mp * Mp) * (2.0 - M)), Pm = p * (0.25 * (Mm * Mm) * (2.0 + M));
+        const double h = g * p / (rho * K.gm1) + 0.5 * kin;
+        const double f_pb = fpb[0] + fpb[1] * u + fpb[2] * v + fpb[3] * w + fpb[4] * h;
+        const double f_mb = fmb[0] + fmb[1] * u + fmb[2] * v + fmb[3] * w + fmb[4] * h;
+        const double Ppb = A1 * fpb[1] + A2 * fpb[2] + A3 * fpb[3];
+        const double Pmb = A1 * fmb[1] + A2 * fmb[2] + A3 * fmb[3];
+        Ab[0] += Pp * fpb[1] + Pm * fmb[1];
+        Ab[1] += Pp * fpb[2] + Pm * fmb[2];
+        Ab[2] += Pp * fpb[3] + Pm * fmb[3];
+        ub += f_p * fpb[1] + f_m * fmb[1];
+        vb += f_p * fpb[2] + f_m * fmb[2];
+        wb += f_p * fpb[3] + f_m * fmb[3];
+        const double hb = f_p * fpb[4] + f_m * fmb[4];
+        // f_p, f_m
+        const double rcsb = 0.25 * (f_pb * Mp * Mp - f_mb * Mm * Mm);
+        Mb += 0.5 * rcs * (f_pb * Mp - f_mb * Mm);
+        rhob += rcsb * c * ss;
+        cb += rcsb * rho * ss;
+        ssb += rcsb * rho * c;
+        // Pp = p (M+1)^2 (2-M) / 4, Pm = p (M-1)^2 (2+M) / 4
+        pb += Ppb * 0.25 * (Mp * Mp) * (2.0 - M) + Pmb * 0.25 * (Mm * Mm) * (2.0 + M);
+        Mb += Ppb * p * 0.25 * (2.0 * Mp * (2.0 - M) - Mp * Mp) + Pmb * p * 0.25 * (2.0 * Mm * (2.0 + M) + Mm * Mm);
+        // h = g p / (rho (g-1)) + kin / 2
+        pb += hb * g / (rho * K.gm1);
+        rhob -= hb * g * p / (rho * rho * K.gm1);
+        kinb += 0.5 * hb;
+    }
+    // M = un / (c ss)
+    const double cs = c * ss;
+    unb += Mb / cs;
+    cb -= Mb * M / c;
+    ssb -= Mb * M / ss;
+    ub += 2.0 * u * kinb;
+    vb += 2.0 * v * kinb;
+    wb += 2.0 * w * kinb;
+    // un = A . (u, v, w)
+    ub += A1 * unb;
+    vb += A2 * unb;
+    wb += A3 * unb;
+    Ab[0] += u * unb;
+    Ab[1] += v * unb;
+    Ab[2] += w * unb;
+    // c = sqrt(gamma p / rho)
+    pb += cb * c / (2.0 * p);
+    rhob -= cb * c / (2.0 * rho);
+    if (mg) {
+        mg[0] += Ab[0];
+        mg[1] += Ab[1];
+        mg[2] += Ab[2];
+        mg[6] += ssb;
+    }
+    qb[0] += rhob;
+    qb[1] += ub;
+    qb[2] += vb;
+    qb[3] += wb;
+    qb[4] += pb;
+}
+
 // ---- WENO reconstructions: cotangents of the stencil values ---------------------------
 // The reference normalises alpha_k = d_k / t_k^2, t_k = eps + IS_k s0, f = sum alpha q / sum alpha
 // (schemes.jl:153-185, 233-252). With fb the cotangent of f (already divided by 12 or 6):
@@ -286,6 +435,190 @@ __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double f
             Vb[k + i] += g * ISb;
         }
     }
+}
+
+// ---- characteristic-wise WENO7 / WENO5 face (schemes.jl:756-999) ---------------------
+// Forward: face state (u, v, w, T) and metric row A = the arithmetic means at the two cells
+// beside the face; n = A s0; tangent basis l (from n, switching on |nz| <= |ny|) and m = n x l;
+// left eigenvectors L (rows) from (u, v, w, T, n, l, m); per characteristic field k the
+// projected split fluxes L_k . Fp / L_k . Fm on the stencil, WENO of each side, their sum x
+// 1/12 (WENO7) or 1/6 (WENO5); the face flux is R flux with the right eigenvectors R.
+// Reverse for the face cotangent Fb: the split-flux cotangents are added through addP(n, pos,
+// value) / addM(n, pos, value); stb[7] += cotangents of (u, v, w, T, A1, A2, A3) of the face
+// state; *s0b += the cotangent of s0 (weights' scale and n = A s0) when s0b is set.
+// br: 1 = WENO7, 2 = WENO5; t: the face's stencil origin (positions t..t+7).
+template <class FPA, class FMA, class ADDP, class ADDM>
+__device__ __forceinline__ void char_face_vjp(const DevParams& P, int br, int t, double s0, const double st[7],
+                                              const double Fb[5], FPA FP, FMA FM, ADDP addP, ADDM addM,
+                                              double stb[7], double* s0b) {
+    const Cst<double>& K = P.cd;
+    const double u = st[0], v = st[1], w = st[2], T = st[3];
+    const double nx = st[4] * s0, ny = st[5] * s0, nz = st[6] * s0;
+    const bool zy = fabs(nz) <= fabs(ny);
+    const double ssq = zy ? nx * nx + ny * ny : nx * nx + nz * nz;
+    const double ss = 1.0 / sqrt(ssq);
+    const double lx = zy ? -ny * ss : -nz * ss, ly = zy ? nx * ss : 0.0, lz = zy ? 0.0 : nx * ss;
+    const double mx = ny * lz - nz * ly, my = nz * lx - nx * lz, mz = nx * ly - ny * lx;
+    const double qn = u * nx + v * ny + w * nz, ql = u * lx + v * ly + w * lz, qm = u * mx + v * my + w * mz;
+    const double q2 = 0.5 * (u * u + v * v + w * w);
+    const double gT = K.grg * T;
+    const double rc = 1.0 / sqrt(gT), c = gT * rc, c2 = 0.5 * rc, Kc = K.gm1 * (rc * rc), K2 = 0.5 * Kc;
+    const double H = gT * K.inv_gm1 + q2;
+    const bool w7 = br == 1;
+    const double tmp = w7 ? 1.0 / 12.0 : 1.0 / 6.0;
+    const int np = w7 ? 7 : 5;
+    auto Lrow = [&](int k, double l[5]) {
+        if (k == 0) { l[0] = K2 * q2 + qn * c2; l[1] = -(K2 * u + nx * c2); l[2] = -(K2 * v + ny * c2); l[3] = -(K2 * w + nz * c2); l[4] = K2; }
+        else if (k == 1) { l[0] = 1.0 - Kc * q2; l[1] = Kc * u; l[2] = Kc * v; l[3] = Kc * w; l[4] = -Kc; }
+        else if (k == 2) { l[0] = K2 * q2 - qn * c2; l[1] = -(K2 * u - nx * c2); l[2] = -(K2 * v - ny * c2); l[3] = -(K2 * w - nz * c2); l[4] = K2; }
+        else if (k == 3) { l[0] = -ql; l[1] = lx; l[2] = ly; l[3] = lz; l[4] = 0.0; }
+        else { l[0] = -qm; l[1] = mx; l[2] = my; l[3] = mz; l[4] = 0.0; }
+    };
+    // stencil positions of the two sides, in upwind order
+    auto posP = [&](int k) { return w7 ? t + k : t + 1 + k; };
+    auto posM = [&](int k) { return w7 ? t + 7 - k : t + 6 - k; };
+    // forward characteristic fluxes
+    double f[5];
+#pragma unroll 1
+    for (int k = 0; k < 5; k++) {
+        double l[5];
+        Lrow(k, l);
+        double VP[7], VM[7];
+        for (int j = 0; j < np; j++) {
+            const int a = posP(j), b = posM(j);
+            VP[j] = FP(0, a) * l[0] + FP(1, a) * l[1] + FP(2, a) * l[2] + FP(3, a) * l[3] + FP(4, a) * l[4];
+            VM[j] = FM(0, b) * l[0] + FM(1, b) * l[1] + FM(2, b) * l[2] + FM(3, b) * l[3] + FM(4, b) * l[4];
+        }
+        f[k] = w7 ? (weno7(VP[0], VP[1], VP[2], VP[3], VP[4], VP[5], VP[6], s0) +
+                     weno7(VM[0], VM[1], VM[2], VM[3], VM[4], VM[5], VM[6], s0)) * tmp
+                  : (weno5(VP[0], VP[1], VP[2], VP[3], VP[4], s0) + weno5(VM[0], VM[1], VM[2], VM[3], VM[4], s0)) * tmp;
+    }
+    // ---- reverse of out = R f (the right eigenvectors, schemes.jl:983-999)
+    const double fb[5] = {
+        Fb[0] + Fb[1] * (u - c * nx) + Fb[2] * (v - c * ny) + Fb[3] * (w - c * nz) + Fb[4] * (H - qn * c),
+        Fb[0] + Fb[1] * u + Fb[2] * v + Fb[3] * w + Fb[4] * q2,
+        Fb[0] + Fb[1] * (u + c * nx) + Fb[2] * (v + c * ny) + Fb[3] * (w + c * nz) + Fb[4] * (H + qn * c),
+        Fb[1] * lx + Fb[2] * ly + Fb[3] * lz + Fb[4] * ql,
+        Fb[1] * mx + Fb[2] * my + Fb[3] * mz + Fb[4] * qm};
+    const double s012 = f[0] + f[1] + f[2], d20 = f[2] - f[0];
+    double ub = s012 * Fb[1], vb = s012 * Fb[2], wb = s012 * Fb[3];
+    double cb = d20 * (nx * Fb[1] + ny * Fb[2] + nz * Fb[3] + qn * Fb[4]);
+    double nxb = c * d20 * Fb[1], nyb = c * d20 * Fb[2], nzb = c * d20 * Fb[3];
+    double qnb = c * d20 * Fb[4];
+    double Hb = (f[0] + f[2]) * Fb[4];
+    double q2b = f[1] * Fb[4];
+    double lxb = f[3] * Fb[1], lyb = f[3] * Fb[2], lzb = f[3] * Fb[3], qlb = f[3] * Fb[4];
+    double mxb = f[4] * Fb[1], myb = f[4] * Fb[2], mzb = f[4] * Fb[3], qmb = f[4] * Fb[4];
+    double K2b = 0.0, Kcb = 0.0, c2b = 0.0;
+    // ---- reverse of the WENO of each field and of the projections L_k . F
+#pragma unroll 1
+    for (int k = 0; k < 5; k++) {
+        const double g = fb[k] * tmp;
+        if (g == 0.0) continue;
+        double l[5];
+        Lrow(k, l);
+        double VP[7], VM[7], VPb[7], VMb[7];
+        for (int j = 0; j < np; j++) {
+            const int a = posP(j), b = posM(j);
+            VP[j] = FP(0, a) * l[0] + FP(1, a) * l[1] + FP(2, a) * l[2] + FP(3, a) * l[3] + FP(4, a) * l[4];
+            VM[j] = FM(0, b) * l[0] + FM(1, b) * l[1] + FM(2, b) * l[2] + FM(3, b) * l[3] + FM(4, b) * l[4];
+        }
+        if (w7) {
+            weno7_vjp(VP, s0, g, VPb, s0b);
+            weno7_vjp(VM, s0, g, VMb, s0b);
+        } else {
+            weno5_vjp(VP, s0, g, VPb, s0b);
+            weno5_vjp(VM, s0, g, VMb, s0b);
+        }
+        double lb[5] = {0, 0, 0, 0, 0};
+        for (int j = 0; j < np; j++) {
+            const int a = posP(j), b = posM(j);
+            for (int e = 0; e < 5; e++) {
+                lb[e] += FP(e, a) * VPb[j] + FM(e, b) * VMb[j];
+                if (l[e] != 0.0) {
+                    addP(e, a, l[e] * VPb[j]);
+                    addM(e, b, l[e] * VMb[j]);
+                }
+            }
+        }
+        // row k of L in terms of the face quantities
+        if (k == 0 || k == 2) {
+            const double sg = k == 0 ? 1.0 : -1.0;
+            K2b += lb[0] * q2 - lb[1] * u - lb[2] * v - lb[3] * w + lb[4];
+            q2b += K2 * lb[0];
+            qnb += sg * c2 * lb[0];
+            c2b += sg * (qn * lb[0] - nx * lb[1] - ny * lb[2] - nz * lb[3]);
+            ub -= K2 * lb[1];
+            vb -= K2 * lb[2];
+            wb -= K2 * lb[3];
+            nxb -= sg * c2 * lb[1];
+            nyb -= sg * c2 * lb[2];
+            nzb -= sg * c2 * lb[3];
+        } else if (k == 1) {
+            Kcb += -q2 * lb[0] + u * lb[1] + v * lb[2] + w * lb[3] - lb[4];
+            q2b -= Kc * lb[0];
+            ub += Kc * lb[1];
+            vb += Kc * lb[2];
+            wb += Kc * lb[3];
+        } else if (k == 3) {
+            qlb -= lb[0];
+            lxb += lb[1];
+            lyb += lb[2];
+            lzb += lb[3];
+        } else {
+            qmb -= lb[0];
+            mxb += lb[1];
+            myb += lb[2];
+            mzb += lb[3];
+        }
+    }
+    // ---- the face quantities in terms of (u, v, w, T, n)
+    Kcb += 0.5 * K2b;                                  // K2 = Kc / 2
+    double rcb = Kcb * K.gm1 * 2.0 * rc + 0.5 * c2b;   // Kc = (g-1) rc^2, c2 = rc / 2
+    double gTb = cb * rc + Hb * K.inv_gm1;             // c = gT rc, H = gT/(g-1) + q2
+    rcb += cb * gT;
+    q2b += Hb;
+    gTb += rcb * (-0.5 * rc * rc * rc);                // rc = gT^(-1/2)
+    stb[3] += gTb * K.grg;                             // gT = g Rg T
+    ub += q2b * u + qnb * nx + qlb * lx + qmb * mx;
+    vb += q2b * v + qnb * ny + qlb * ly + qmb * my;
+    wb += q2b * w + qnb * nz + qlb * lz + qmb * mz;
+    nxb += qnb * u;
+    nyb += qnb * v;
+    nzb += qnb * w;
+    lxb += qlb * u;
+    lyb += qlb * v;
+    lzb += qlb * w;
+    mxb += qmb * u;
+    myb += qmb * v;
+    mzb += qmb * w;
+    // m = n x l
+    nyb += mxb * lz; lzb += mxb * ny; nzb -= mxb * ly; lyb -= mxb * nz;
+    nzb += myb * lx; lxb += myb * nz; nxb -= myb * lz; lzb -= myb * nx;
+    nxb += mzb * ly; lyb += mzb * nx; nyb -= mzb * lx; lxb -= mzb * ny;
+    // l from n (the basis branch frozen); ss = ssq^(-1/2)
+    const double ss3 = ss * ss * ss;
+    if (zy) {  // lx = -ny ss, ly = nx ss
+        const double ssb = -ny * lxb + nx * lyb;
+        nyb -= lxb * ss;
+        nxb += lyb * ss;
+        nxb -= ssb * nx * ss3;
+        nyb -= ssb * ny * ss3;
+    } else {  // lx = -nz ss, lz = nx ss
+        const double ssb = -nz * lxb + nx * lzb;
+        nzb -= lxb * ss;
+        nxb += lzb * ss;
+        nxb -= ssb * nx * ss3;
+        nzb -= ssb * nz * ss3;
+    }
+    stb[0] += ub;
+    stb[1] += vb;
+    stb[2] += wb;
+    // n = A s0
+    stb[4] += nxb * s0;
+    stb[5] += nyb * s0;
+    stb[6] += nzb * s0;
+    if (s0b) *s0b += nxb * st[4] + nyb * st[5] + nzb * st[6];
 }
 
 }  // namespace f3d

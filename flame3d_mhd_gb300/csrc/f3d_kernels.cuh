@@ -42,6 +42,7 @@ struct SweepArgs {
     float* Un32;          // OUT_STAGE stage-start copy
     float dt32, ca32, cb32;
     unsigned* kstat;      // kernel status word of the context (bit 0: a TMA tile wait gave up)
+    unsigned* tile_ctr;   // TMA sweeps: next-tile counters of the three directions (zeroed per RHS)
 };
 
 // Metric and Jacobian cotangents accumulated by the viscous VJP (null m[0]: none)

@@ -29,6 +29,21 @@ __device__ __forceinline__ int branch_of(const DevParams& P, const float* ph) {
     return m != m ? 3 : br;
 }
 
+// a + b + c with error-free transformations (Knuth's TwoSum): s + e is the exact sum of the
+// three, returned rounded once. For FP32 operands; the FP64 form never calls it.
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+__device__ __forceinline__ float sum3_compensated(float a, float b, float c) {
+    float e1, e2;
+    const float s1 = two_sum(a, b, e1);
+    const float s2 = two_sum(s1, c, e2);
+    return __fadd_rn(s2, __fadd_rn(e1, e2));
+}
+
 template <int DIR, int TL, int TC, int NTHREADS, class R, class CellFn, class FidxFn>
 __device__ __forceinline__ void sweep_epilogue(const SweepArgs& a, const R* sF, int c0, int l0, int other, int nc,
                                                int nl, const CellFn& cell, const FidxFn& fidx) {
@@ -86,10 +101,14 @@ __device__ __forceinline__ void sweep_epilogue(const SweepArgs& a, const R* sF, 
                 continue;
             }
         }
-        // sum of the three directions: in the arithmetic type, or (mixed form, acc2 set) the
-        // xi and eta sweeps' FP32 differences and this sweep's, converted exactly and added in FP64
+        // sum of the three directions: in the arithmetic type, or (mixed form, acc2 set) the xi
+        // and eta sweeps' FP32 differences and this sweep's summed with compensation, so the
+        // result is the exact sum rounded once to FP32 (relative to the sum, not to the terms
+        // that cancel in it)
         auto total = [&](int n) -> double {
-            if (a.acc2) return (to_f64(acc[c + n * pl]) + to_f64(a.acc2[c + n * pl])) + to_f64(d[n]);
+            if constexpr (sizeof(R) == 4) {
+                if (a.acc2) return to_f64(sum3_compensated(acc[c + n * pl], a.acc2[c + n * pl], d[n]));
+            }
             return to_f64(acc[c + n * pl] + d[n]);
         };
         if (a.out_mode == OUT_SET) {

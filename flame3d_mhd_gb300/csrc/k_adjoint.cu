@@ -4,8 +4,9 @@
 //   --split--> Fp, Fm --reconstruction--> face fluxes --difference x J--> L,
 //   plus Q --gradients--> Fv --CD4 x J--> L (viscous).
 // The kernels below run it backwards for a cotangent Lb of L (interior cells):
-//   k_sweep_vjp<d>      face cotangents from J Lb, reverse of UP7/WENO7/WENO5/NND2 on the
-//                       forward branch (component-wise), reverse of the split, into Qb;
+//   k_sweep_vjp<d,char> face cotangents from J Lb, reverse of UP7/WENO7/WENO5/NND2 on the
+//                       forward branch (component- or characteristic-wise: char_face_vjp),
+//                       reverse of the split (SW, LF, VL, AUSM), into Qb;
 //   k_visc_fvb          Fv cotangents: transpose of the CD4 divergence (div.jl:14-48);
 //   k_visc_vjp          reverse of viscousFlux per cell into gradient/centre cotangents;
 //   k_visc_gather       transpose of the CD4 gradients (viscous.jl:29-42) into Qb;
@@ -41,7 +42,7 @@ template <int DIR> constexpr size_t vjp_smem_bytes() {
            sizeof(int) * (2 * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 1) + 4);
 }
 
-template <int DIR>
+template <int DIR, bool CHAR>
 __global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(const AdjArgs a) {
     constexpr int TL = VTile<DIR>::TL, TC = VTile<DIR>::TC, NP = TC + 8, NT = VTile<DIR>::NT;
     const DevParams& P = a.P;
@@ -117,7 +118,34 @@ __global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(
         const double s0 = (br == 1 || br == 2) ? 2.0 / (a.S[cl] + a.S[cr]) : 0.0;
         double s0b_ = 0.0;
         double* s0b = a.mb[0] ? &s0b_ : nullptr;  // metric cotangent wanted
-        for (int n = 0; n < 5; n++) {
+        if (CHAR && (br == 1 || br == 2)) {
+            // characteristic-wise WENO: the face state is the mean of the two cells beside it
+            const double st[7] = {0.5 * (a.Q[cr + pl] + a.Q[cl + pl]), 0.5 * (a.Q[cr + 2 * pl] + a.Q[cl + 2 * pl]),
+                                  0.5 * (a.Q[cr + 3 * pl] + a.Q[cl + 3 * pl]), 0.5 * (a.Q[cr + 5 * pl] + a.Q[cl + 5 * pl]),
+                                  (a.A[0][cr] + a.A[0][cl]) * 0.5, (a.A[1][cr] + a.A[1][cl]) * 0.5,
+                                  (a.A[2][cr] + a.A[2][cl]) * 0.5};
+            double stb[7] = {0, 0, 0, 0, 0, 0, 0};
+            auto FPv = [&](int n, int pos) { return sFp[n * TL * NP + sidx(l, pos)]; };
+            auto FMv = [&](int n, int pos) { return sFm[n * TL * NP + sidx(l, pos)]; };
+            auto addP = [&](int n, int pos, double v) { atomicAdd(&sFpb[n * TL * NP + sidx(l, pos)], v); };
+            auto addM = [&](int n, int pos, double v) { atomicAdd(&sFmb[n * TL * NP + sidx(l, pos)], v); };
+            char_face_vjp(P, br, t, s0, st, Fb, FPv, FMv, addP, addM, stb, s0b);
+            const int qv[4] = {1, 2, 3, 5};  // u, v, w, T
+            for (int k = 0; k < 4; k++) {
+                const double h = 0.5 * stb[k];
+                if (h != 0.0) {
+                    atomicAdd(&a.Qb[cl + qv[k] * pl], h);
+                    atomicAdd(&a.Qb[cr + qv[k] * pl], h);
+                }
+            }
+            if (a.mb[0])
+                for (int j = 0; j < 3; j++) {
+                    const double h = 0.5 * a.mscale * stb[4 + j];
+                    atomicAdd(&a.mb[j][cl], h);
+                    atomicAdd(&a.mb[j][cr], h);
+                }
+        }
+        for (int n = 0; n < 5 && !(CHAR && (br == 1 || br == 2)); n++) {
             const double g = Fb[n];
             if (g == 0.0) continue;
             double* pb = sFpb + n * TL * NP;
@@ -240,8 +268,10 @@ __global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(
         if (P.split == F3D_SPLIT_SW)
             split_sw_vjp(P.cd, q, a.csnd[c], A3[0], A3[1], A3[2], a.Ah[0][c], a.Ah[1][c], a.Ah[2][c], S, fpb, fmb, qb,
                          mgp);
-        else
+        else if (P.split == F3D_SPLIT_LF)
             split_lf_vjp(P.cd, q, a.csnd[c], A3[0], A3[1], A3[2], S, fpb, fmb, qb, mgp);
+        else  // van Leer, AUSM
+            split_mach_vjp(P.split, P.cd, q, a.csnd[c], A3[0], A3[1], A3[2], S, fpb, fmb, qb, mgp);
         for (int n = 0; n < 6; n++)
             if (qb[n] != 0.0) atomicAdd(&a.Qb[c + n * pl], qb[n]);
         if (mgp) {
@@ -543,33 +573,36 @@ __global__ void k_axpby(const DevParams P, double* out, const double* x, double 
 }
 
 // ---- launchers --------------------------------------------------------------------------
-template <int DIR> static cudaError_t launch_vjp_dir(const AdjArgs& a, cudaStream_t st) {
+template <int DIR, bool CHAR> static cudaError_t launch_vjp_dir(const AdjArgs& a, cudaStream_t st) {
     constexpr int TL = VTile<DIR>::TL, TC = VTile<DIR>::TC;
     const DevParams& P = a.P;
     dim3 grid;
     if (DIR == 0) grid = dim3(cdiv(P.nx, TC), cdiv(P.ny, TL), P.nz);
     else if (DIR == 1) grid = dim3(cdiv(P.nx, TL), cdiv(P.ny, TC), P.nz);
     else grid = dim3(cdiv(P.nx, TL), cdiv(P.nz, TC), P.ny);
-    k_sweep_vjp<DIR><<<grid, VTile<DIR>::NT, vjp_smem_bytes<DIR>(), st>>>(a);
+    k_sweep_vjp<DIR, CHAR><<<grid, VTile<DIR>::NT, vjp_smem_bytes<DIR>(), st>>>(a);
     return cudaGetLastError();
+}
+
+template <int DIR, bool CHAR> static cudaError_t configure_vjp() {
+    return cudaFuncSetAttribute(k_sweep_vjp<DIR, CHAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)vjp_smem_bytes<DIR>());
 }
 
 cudaError_t adjoint_configure() {
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_sweep_vjp<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)vjp_smem_bytes<0>())) != cudaSuccess)
+    if ((e = configure_vjp<0, false>()) != cudaSuccess || (e = configure_vjp<1, false>()) != cudaSuccess ||
+        (e = configure_vjp<2, false>()) != cudaSuccess || (e = configure_vjp<0, true>()) != cudaSuccess ||
+        (e = configure_vjp<1, true>()) != cudaSuccess)
         return e;
-    if ((e = cudaFuncSetAttribute(k_sweep_vjp<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)vjp_smem_bytes<1>())) != cudaSuccess)
-        return e;
-    return cudaFuncSetAttribute(k_sweep_vjp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)vjp_smem_bytes<2>());
+    return configure_vjp<2, true>();
 }
 
 cudaError_t launch_sweep_vjp(int dir, const AdjArgs& a, cudaStream_t st) {
-    if (dir == 0) return launch_vjp_dir<0>(a, st);
-    if (dir == 1) return launch_vjp_dir<1>(a, st);
-    return launch_vjp_dir<2>(a, st);
+    const bool ch = a.P.character != 0;
+    if (dir == 0) return ch ? launch_vjp_dir<0, true>(a, st) : launch_vjp_dir<0, false>(a, st);
+    if (dir == 1) return ch ? launch_vjp_dir<1, true>(a, st) : launch_vjp_dir<1, false>(a, st);
+    return ch ? launch_vjp_dir<2, true>(a, st) : launch_vjp_dir<2, false>(a, st);
 }
 
 static unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }

@@ -8,9 +8,10 @@
 //    lines x (TC + 8) positions with their 4-cell halos, copied by cp.async.bulk.tensor into
 //    shared memory and completed on an mbarrier; the boxes land in the [var][line][pos] /
 //    [var][pos][line] layouts the phases index, so no thread issues a global load for them;
-//  - blocks are persistent: each walks tiles blockIdx.x, blockIdx.x + gridDim.x, ..., and
-//    issues the copies of its next tile as soon as Phase A has consumed the current one, so
-//    those loads overlap Phases B and C.
+//  - blocks are persistent: each takes its next tile from a counter of the launch (atomicAdd;
+//    the shock-capturing faces cluster in a few tile columns, so a static assignment would
+//    leave some blocks with all of them) and issues that tile's copies as soon as Phase A has
+//    consumed the current one, so the loads overlap Phases B and C.
 // Every mbarrier wait is bounded (time and iterations); a wait that gives up sets bit 0 of
 // the context's kernel-status word, waits (bounded) for the copy in flight and ends the
 // block, and the host reports F3D_ERR_CUDA at its next status check.
@@ -49,7 +50,7 @@ template <int DIR> struct TmaLayout {
     static constexpr size_t phi = ff + sizeof(float) * 5 * TL * NF;       // sensor, BOX
     static constexpr size_t sabs = phi + sizeof(float) * BOX;             // |A|, BOX
     static constexpr size_t lists = sabs + sizeof(float) * BOX;           // 2 x TL x NF ints + 4
-    static constexpr size_t bar = (lists + sizeof(int) * (2 * TL * NF + 4) + 7) & ~(size_t)7;
+    static constexpr size_t bar = (lists + sizeof(int) * (2 * TL * NF + 6) + 7) & ~(size_t)7;
     static constexpr size_t total = bar + 8;
     // bytes one tile's copies deliver (complete_tx counts whole boxes, filled or not)
     static constexpr unsigned tx_bytes = (unsigned)(sizeof(float) * (kQVars + kMetVars + 1) * BOX);
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
     float* sS = reinterpret_cast<float*>(smem_raw + L::sabs);
     int* list7 = reinterpret_cast<int*>(smem_raw + L::lists);
     int* list5 = list7 + TL * NF;
-    int* counts = list5 + TL * NF;
+    int* counts = list5 + TL * NF;  // counts[0..1]: WENO7 / WENO5 queue lengths; counts[4]: next tile
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem_raw + L::bar);
 
     const int Nd = DIR == 0 ? P.nx : (DIR == 1 ? P.ny : P.nz);
@@ -169,15 +170,18 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
         tma_load_3d(rphi, &maps.phi, bar, x, y, z);
     };
 
+    unsigned* ctr = a.tile_ctr + DIR;  // zeroed before the three sweeps of an RHS
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
+        const int first = (int)atomicAdd(ctr, 1u);
+        counts[4] = first;
+        if (first < ntiles) issue(first);
     }
     __syncthreads();
-    int tile = blockIdx.x;
-    if (threadIdx.x == 0 && tile < ntiles) issue(tile);
+    int tile = counts[4];
     unsigned parity = 0;
-    for (; tile < ntiles; tile += gridDim.x, parity ^= 1u) {
+    for (; tile < ntiles; parity ^= 1u) {
         int c0, l0, other;
         decode(tile, c0, l0, other);
         const int nc = min(TC, Nd - c0), nl = min(TL, Nl - l0);
@@ -221,7 +225,11 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
         }
         __syncthreads();
         // the staging buffer is free: start the next tile's copies under Phases B and C
-        if (threadIdx.x == 0 && tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x);
+        if (threadIdx.x == 0) {
+            const int next = (int)atomicAdd(ctr, 1u);
+            counts[4] = next;
+            if (next < ntiles) issue(next);
+        }
 
         // ---- Phase B: faces t = 0..nc (between positions t+3 and t+4); WENO faces queued
         auto do_face = [&](int l, int t, int br) {
@@ -268,6 +276,7 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
         // ---- Phase C: differences, viscous terms and the accumulation of out_mode
         sweep_epilogue<DIR, TL, TC, NT, float>(a, sF, c0, l0, other, nc, nl, cell, fidx);
         __syncthreads();  // sF, sPhi and the lists are rewritten by the next tile
+        tile = counts[4];
     }
 }
 

@@ -25,9 +25,20 @@ I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
 def _random(seed, spikes=0, bc="periodic", n=(20, 14, 12), **kw):
     if bc == "periodic":
         kw["bc"] = [dict(kind=BC_PERIODIC)] * 6
-    P = make_params(*n, character=0, **kw)
+    kw.setdefault("character", 0)
+    P = make_params(*n, **kw)
     x, y, z = curvilinear_coords(P)
     return P, random_state(P, seed, spikes), x, y, z
+
+
+def _random_transonic(seed, **kw):
+    """A random curvilinear state streaming along x at Mach 0.6 .. 1.6, so the Mach-number
+    splits take both their subsonic and their supersonic branches."""
+    P, Q0, x, y, z = _random(seed, **kw)
+    rng = np.random.default_rng(seed + 100)
+    c = np.sqrt(1.4 * np.maximum(Q0[4], 1e-12) / np.maximum(Q0[0], 1e-12))
+    Q0[1] += c * rng.uniform(0.6, 1.6, Q0[1].shape) * (Q0[0] > 0)
+    return P, Q0, x, y, z
 
 
 CASES = {
@@ -39,6 +50,18 @@ CASES = {
         34, viscous=1, rg=1.0, c_s=1e-2, t_s=1.0,
         bc=[dict(kind=2), dict(kind=2), dict(kind=4, t_wall=0.8), dict(kind=1, rho=1.0, u=0.2, v=0.0, w=0.0, p=0.7),
             dict(kind=0), dict(kind=0)]),
+    # characteristic-wise reconstruction (the reference's default, run.jl:68) with all four
+    # branches, and the van Leer and AUSM splits in both reconstruction modes
+    "curvi_char_hybrid_sw": lambda: _random(37, spikes=20, phi1=0.02, phi2=0.1, phi3=0.4, character=1),
+    "curvi_char_hybrid_lf": lambda: _random(38, spikes=20, phi1=0.02, phi2=0.1, phi3=0.4, character=1, split="LF"),
+    "curvi_char_vl": lambda: _random(39, spikes=10, phi1=0.02, phi2=0.1, phi3=0.4, character=1, split="VL"),
+    "curvi_char_ausm": lambda: _random(40, spikes=10, phi1=0.02, phi2=0.1, phi3=0.4, character=1, split="AUSM"),
+    "curvi_comp_vl": lambda: _random(41, spikes=10, phi1=0.02, phi2=0.1, phi3=0.4, split="VL"),
+    "curvi_comp_ausm": lambda: _random(42, spikes=10, phi1=0.02, phi2=0.1, phi3=0.4, split="AUSM"),
+    "curvi_char_vl_transonic": lambda: _random_transonic(44, phi1=0.02, phi2=0.1, phi3=0.4, character=1, split="VL"),
+    "curvi_comp_ausm_transonic": lambda: _random_transonic(45, phi1=0.02, phi2=0.1, phi3=0.4, split="AUSM"),
+    "curvi_char_refbc_viscous": lambda: _random(43, bc="reference", viscous=1, rg=1.0, c_s=1e-2, t_s=1.0,
+                                                character=1, phi1=0.0, phi2=0.05, phi3=np.inf),
 }
 
 
@@ -71,7 +94,8 @@ def test_rhs_vjp_dot_product_vs_dual_jvp(gpu_lib, name):
     s.close()
 
 
-@pytest.mark.parametrize("name", ["tgv16_weno5", "curvi_hybrid_sw", "curvi_refbc_viscous"])
+@pytest.mark.parametrize("name", ["tgv16_weno5", "curvi_hybrid_sw", "curvi_refbc_viscous", "curvi_char_hybrid_sw",
+                                  "curvi_char_vl"])
 def test_rk3_step_vjp_dot_product(gpu_lib, name):
     P, m, J, Q, U, s, keep = _setup(name)
     dt = 1e-3 if name.startswith("tgv") else 2e-4

@@ -41,7 +41,8 @@ def _walls(seed, wall):
     return P, Q0, x, y, z
 
 
-CASES = {k: STATE_CASES[k] for k in ("tgv16_weno5", "curvi_hybrid_sw", "curvi_hybrid_lf")}
+CASES = {k: STATE_CASES[k] for k in ("tgv16_weno5", "curvi_hybrid_sw", "curvi_hybrid_lf", "curvi_char_hybrid_sw",
+                                     "curvi_char_vl", "curvi_comp_ausm")}
 CASES["curvi_dirichlet_adiabatic_viscous"] = lambda: _walls(35, dict(kind=BC_WALL_ADIABATIC))
 CASES["curvi_dirichlet_isothermal_viscous"] = lambda: _walls(36, dict(kind=BC_WALL_ISOTHERMAL, t_wall=1.0))
 

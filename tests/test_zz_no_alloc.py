@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import rel_linf
+from conftest import assert_rhs_parity, rel_linf, rhs_parity
 from flame3d_mhd_gb300 import abi, cases
 from flame3d_mhd_gb300.abi import BC_PERIODIC, make_params
 from flame3d_mhd_gb300.solver import Flame3D
@@ -80,17 +80,11 @@ def _noalloc_call(lib, P, Q0, x, y, z):
 
 
 def _check_against_oracle(got, inputs):
-    """The parity bar of tests/test_gpu_parity.py: the difference from the oracle's
-    extended-precision evaluation relative to the flux scale <= 1e-12, and against the FP64
-    oracle within 3x the oracle's own rounding."""
+    """The RHS parity bar of tests/test_gpu_parity.py (conftest.assert_rhs_parity)."""
     P, Q, m, J = inputs
-    I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
-    ro = orc.rhs(P, Q, m, J)[I]
-    rl, scale = orc.rhs_ld(P, Q, m, J)
-    rl = rl[I]
-    scaled = max(float(np.abs(got[n] - rl[n]).max() / scale[n]) for n in range(5))
-    assert scaled <= TOL, scaled
-    assert rel_linf(got, ro) <= max(TOL, 3.0 * rel_linf(ro, rl))
+    full = np.zeros((5, *Q.shape[1:]))
+    full[:, NG:-NG, NG:-NG, NG:-NG] = got
+    assert_rhs_parity(rhs_parity(P, Q, m, J, full))
 
 
 def test_rhs_noalloc_three_calls_in_a_row(gpu_lib):
