@@ -242,17 +242,39 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def adjoint_cost(args, n: int = 128, steps: int = 4) -> dict:
+def ramp_leg(nx: int, ny: int, nz: int, steps: int) -> dict:
+    """The viscous Mach 2.9 compression ramp (24 degrees, body-fitted grid, isothermal wall,
+    1/7-power inflow, Re 1e5, Sutherland, Pr 0.72) in FP64 and in mixed precision from the
+    same initial state: Mcell-RHS/s of each (CUDA events over steps - 1 graph-replayed RK3
+    steps after one) and the mixed form's deviation from FP64 in wall pressure and skin
+    friction after `steps` steps (max and mean, relative to the FP64 values' maximum / mean)."""
+    from flame3d_mhd_gb300 import cases, ramp
+    from flame3d_mhd_gb300.abi import PREC_MIXED
+    case = cases.compression_ramp(nx, ny, nz)
+    Q64, t64 = ramp.run(case, 0, steps, wall_only=True)
+    Q32, t32 = ramp.run(case, PREC_MIXED, steps, wall_only=True)
+    cells = nx * ny * nz
+    return {"workload": f"{case['name']}: viscous Mach 2.9 compression ramp, 24 deg, isothermal wall, "
+                        f"tanh wall-normal stretching, first cell 1e-3 delta", "steps": steps,
+            "timed_steps": steps - 1,
+            "fp64": {"value": 3 * cells / (t64 * 1e3), "unit": UNIT, "ms_per_step": t64},
+            "mixed": {"value": 3 * cells / (t32 * 1e3), "unit": UNIT, "ms_per_step": t32},
+            "speedup_mixed_vs_fp64": t64 / t32, "mixed_vs_fp64": ramp.deviations(Q64, Q32, case)}
+
+
+def adjoint_cost(args, n: int = 128, steps: int = 4, character: int = 0) -> dict:
     """Adjoint / forward cost of one SSP-RK3 step on the viscous curvilinear Taylor-Green
-    vortex (128^3, Re 1600, Mach 0.1, FP64, component-wise hybrid): the adjoint step
-    recomputes two stage states and applies three RHS VJPs (f3d_rk3_step_vjp)."""
+    vortex (128^3, Re 1600, Mach 0.1, FP64, hybrid; component-wise or, with character=1,
+    characteristic-wise): the adjoint step recomputes two stage states and applies three RHS
+    VJPs (f3d_rk3_step_vjp)."""
     import numpy as np
     import torch
 
     from flame3d_mhd_gb300 import cases
+    from flame3d_mhd_gb300.cases import params_copy
     from flame3d_mhd_gb300.solver import Flame3D, side_stream
     c = cases.tgv_viscous_curvilinear(n)
-    P = c["params"]
+    P = params_copy(c["params"], character=character)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     s = Flame3D(P)
     ms, J = s.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
@@ -280,7 +302,8 @@ def adjoint_cost(args, n: int = 128, steps: int = 4) -> dict:
     adj = e[2].elapsed_time(e[3]) / steps
     s.close()
     cells = n ** 3
-    return {"workload": f"tgv{n}^3 viscous, curvilinear amp 0.05, Re 1600, Mach 0.1, FP64, component-wise hybrid",
+    mode = "characteristic" if character else "component-wise"
+    return {"workload": f"tgv{n}^3 viscous, curvilinear amp 0.05, Re 1600, Mach 0.1, FP64, {mode} hybrid",
             "forward_ms_per_step": fwd, "adjoint_ms_per_step": adj, "adjoint_over_forward": adj / fwd,
             "forward_mcell_rhs_per_s": cells * 3 / (fwd / 1e3) / 1e6,
             "adjoint_includes": "recompute of 2 stage states + 3 RHS VJPs per step"}
@@ -417,6 +440,11 @@ def run_ours(args):
            "of U + HLLC (FVM.jl)", "state_finite": bool(sf.check_finite(Uf))}
     sf.close()
     adjoint = adjoint_cost(args)
+    adjoint["characteristic"] = adjoint_cost(args, character=1)
+    # the configurations the metric is quoted on: the compression ramp at 512x256x128 and at
+    # 1024x384x192, FP64 and mixed precision from the same state
+    ramps = {} if args.no_ramp else {"config3_ramp_512x256x128": ramp_leg(512, 256, 128, 30),
+                                     "config5_ramp_1024x384x192": ramp_leg(1024, 384, 192, 10)}
 
     # per-kernel device times of single steps (events between launches, outside the timed loop)
     prof = {}
@@ -517,6 +545,7 @@ def run_ours(args):
         "ref32": ref32,
         "fvm": fvm,
         "adjoint": adjoint,
+        **ramps,
         "clocks": clocks,
         "state_finite": bool(ok),
     }
@@ -549,6 +578,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-ramp", action="store_true", help="skip the compression-ramp legs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

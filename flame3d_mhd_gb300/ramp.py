@@ -50,14 +50,16 @@ def skin_friction(Q: np.ndarray, x: np.ndarray, y: np.ndarray, wall: dict) -> np
 
 
 def run(case: dict, precision: int, steps: int, dev: str = "cuda", perturb: float = 0.0,
-        seed: int = 7, out_dir: str | None = None) -> tuple[np.ndarray, float]:
+        seed: int = 7, out_dir: str | None = None, wall_only: bool = False) -> tuple[np.ndarray, float]:
     """Advance `steps` SSP-RK3 steps (graph-captured) and return (Q, ms per step). With
     perturb > 0 the initial interior primitive state is multiplied by 1 + perturb * N(0,1)
     (seeded): an FP64 run perturbed at FP32 rounding level measures how far the flow itself
     amplifies last-bit differences (the yardstick for the mixed form's deviation).
     With `out_dir` the reference's files are written there: metrics.h5 and mesh.h5 from the
     device metrics and the grid, and after the last step PLT/plt-<steps>.h5 + .xmf and
-    CHK/chk-<steps>.h5 from the primitives of the final state and their shock sensor."""
+    CHK/chk-<steps>.h5 from the primitives of the final state and their shock sensor.
+    wall_only: return only the eta layers 0..NG of Q (all wall_pressure and skin_friction
+    read), which keeps the host copy small on large grids."""
     from .cases import params_copy
     P = params_copy(case["params"], precision=precision)
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
@@ -85,7 +87,7 @@ def run(case: dict, precision: int, steps: int, dev: str = "cuda", perturb: floa
         e1.record(stream)
         e1.synchronize()
     s.check_finite(U)
-    out = Q.cpu().numpy()
+    out = (Q[:, :, :NG + 1, :] if wall_only else Q).cpu().numpy()
     if out_dir:
         Qf = s.q_from_u(U)
         phi = s.field(1)
