@@ -262,19 +262,20 @@ def ramp_leg(nx: int, ny: int, nz: int, steps: int) -> dict:
             "speedup_mixed_vs_fp64": t64 / t32, "mixed_vs_fp64": ramp.deviations(Q64, Q32, case)}
 
 
-def adjoint_cost(args, n: int = 128, steps: int = 4, character: int = 0) -> dict:
-    """Adjoint / forward cost of one SSP-RK3 step on the viscous curvilinear Taylor-Green
-    vortex (128^3, Re 1600, Mach 0.1, FP64, hybrid; component-wise or, with character=1,
-    characteristic-wise): the adjoint step recomputes two stage states and applies three RHS
-    VJPs (f3d_rk3_step_vjp)."""
+def adjoint_cost(args, n: int = 128, steps: int = 4, workload: str = "tgv") -> dict:
+    """Adjoint / forward cost of one SSP-RK3 step: the adjoint step recomputes two stage states
+    and applies three RHS VJPs (f3d_rk3_step_vjp). workload "tgv": the viscous curvilinear
+    Taylor-Green vortex of the adjoint configuration (n^3, Re 1600, Mach 0.1, FP64,
+    component-wise hybrid; its faces all take UP7); "sod": the bench workload (shock tube
+    256x64x64, characteristic-wise hybrid, inviscid), whose WENO faces exercise the
+    characteristic reverse."""
     import numpy as np
     import torch
 
     from flame3d_mhd_gb300 import cases
-    from flame3d_mhd_gb300.cases import params_copy
     from flame3d_mhd_gb300.solver import Flame3D, side_stream
-    c = cases.tgv_viscous_curvilinear(n)
-    P = params_copy(c["params"], character=character)
+    c = cases.tgv_viscous_curvilinear(n) if workload == "tgv" else cases.sod(**WORKLOAD)
+    P = c["params"]
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     s = Flame3D(P)
     ms, J = s.compute_metrics(dev(c["x"]), dev(c["y"]), dev(c["z"]))
@@ -301,9 +302,10 @@ def adjoint_cost(args, n: int = 128, steps: int = 4, character: int = 0) -> dict
     fwd = e[0].elapsed_time(e[1]) / steps
     adj = e[2].elapsed_time(e[3]) / steps
     s.close()
-    cells = n ** 3
-    mode = "characteristic" if character else "component-wise"
-    return {"workload": f"tgv{n}^3 viscous, curvilinear amp 0.05, Re 1600, Mach 0.1, FP64, {mode} hybrid",
+    desc = (f"tgv{n}^3 viscous, curvilinear amp 0.05, Re 1600, Mach 0.1, FP64, component-wise hybrid"
+            if workload == "tgv" else "sod_curvilinear_256x64x64, FP64, characteristic-wise hybrid, inviscid")
+    cells = P.nx * P.ny * P.nz
+    return {"workload": desc,
             "forward_ms_per_step": fwd, "adjoint_ms_per_step": adj, "adjoint_over_forward": adj / fwd,
             "forward_mcell_rhs_per_s": cells * 3 / (fwd / 1e3) / 1e6,
             "adjoint_includes": "recompute of 2 stage states + 3 RHS VJPs per step"}
@@ -440,7 +442,7 @@ def run_ours(args):
            "of U + HLLC (FVM.jl)", "state_finite": bool(sf.check_finite(Uf))}
     sf.close()
     adjoint = adjoint_cost(args)
-    adjoint["characteristic"] = adjoint_cost(args, character=1)
+    adjoint["characteristic"] = adjoint_cost(args, workload="sod")
     # the configurations the metric is quoted on: the compression ramp at 512x256x128 and at
     # 1024x384x192, FP64 and mixed precision from the same state
     ramps = {} if args.no_ramp else {"config3_ramp_512x256x128": ramp_leg(512, 256, 128, 30),

@@ -58,13 +58,42 @@ __global__ void k_prim_interior(const DevParams P, const double* U, double* Q, d
     }
 }
 
+// Ghost cell number g (0 .. plane - interior - 1) -> (i, j, k): the two z slabs of NG planes
+// (every i, j), then the y slabs within the interior z range (every i), then the x slabs of
+// the interior (j, k) lines; i runs fastest in the first two, so their accesses coalesce.
+__device__ __forceinline__ void ghost_ijk(const DevParams& P, long long g, int& i, int& j, int& k) {
+    const long long zs = 2LL * NG * P.nxt * P.nyt;
+    const long long ys = 2LL * NG * P.nxt * P.nz;
+    if (g < zs) {
+        const unsigned q = fdiv((unsigned)g, P.dnxt);
+        i = (int)((unsigned)g - q * P.dnxt.d);
+        const unsigned kk = fdiv(q, P.dnyt);
+        j = (int)(q - kk * P.dnyt.d);
+        k = kk < (unsigned)NG ? (int)kk : P.nz + (int)kk;
+    } else if (g < zs + ys) {
+        const unsigned h = (unsigned)(g - zs);
+        const unsigned q = fdiv(h, P.dnxt);
+        i = (int)(h - q * P.dnxt.d);
+        const unsigned jj = q % (2u * NG), kz = q / (2u * NG);
+        j = jj < (unsigned)NG ? (int)jj : P.ny + (int)jj;
+        k = (int)kz + NG;
+    } else {
+        const unsigned h = (unsigned)(g - zs - ys);
+        const unsigned ii = h % (2u * NG), q = h / (2u * NG);
+        const unsigned kq = fdiv(q, P.dny);
+        j = (int)(q - kq * P.dny.d) + NG;
+        k = (int)kq + NG;
+        i = ii < (unsigned)NG ? (int)ii : P.nx + (int)ii;
+    }
+}
+
 __global__ void k_prim_ghost(const DevParams P, const double* U, double* Q, double* Ug, double* csnd, float* Q32) {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= P.plane) return;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= P.plane - (long long)P.nx * P.ny * P.nz) return;
     const long long pl = P.plane;
     int i, j, k;
-    cell_ijk(P, c, i, j, k);
-    if (is_interior(P, i, j, k)) return;
+    ghost_ijk(P, g, i, j, k);
+    const long long c = lin3(P, i, j, k);
     double q[6];
     const GhostChain ch = resolve_ghost(P, i, j, k);
     const long long s = lin3(P, ch.si, ch.sj, ch.sk);
@@ -97,7 +126,7 @@ cudaError_t launch_prim_fill(const DevParams& P, const double* U, double* Q, dou
                              cudaStream_t st, float* Q32) {
     const long long ni = (long long)P.nx * P.ny * P.nz;
     if (!from_q || csnd || Q32) k_prim_interior<<<pw_blocks(ni), PW_THREADS, 0, st>>>(P, U, Q, csnd, Q32, from_q);
-    k_prim_ghost<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, U, Q, Ug, csnd, Q32);
+    k_prim_ghost<<<pw_blocks(P.plane - ni), PW_THREADS, 0, st>>>(P, U, Q, Ug, csnd, Q32);
     return cudaGetLastError();
 }
 

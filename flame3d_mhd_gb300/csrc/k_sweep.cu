@@ -32,6 +32,10 @@ namespace f3d {
 #define SW_D_TL0 8
 #define SW_D_TL12 16
 #endif
+#ifndef SW_D_TC0
+#define SW_D_TC0 64
+#define SW_D_TC12 32
+#endif
 template <int DIR, class R> struct Tile;
 #ifndef SW_F_THREADS
 #define SW_F_THREADS 128
@@ -42,9 +46,9 @@ template <int DIR, class R> struct Tile;
 template <> struct Tile<0, float> { static constexpr int TL = SW_F_TL0, TC = 64, NT = SW_F_THREADS, MINB = SW_F_BLOCKS; };
 template <> struct Tile<1, float> { static constexpr int TL = SW_F_TL12, TC = 32, NT = SW_F_THREADS, MINB = SW_F_BLOCKS; };
 template <> struct Tile<2, float> { static constexpr int TL = SW_F_TL12, TC = 32, NT = SW_F_THREADS, MINB = SW_F_BLOCKS; };
-template <> struct Tile<0, double> { static constexpr int TL = SW_D_TL0, TC = 64, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
-template <> struct Tile<1, double> { static constexpr int TL = SW_D_TL12, TC = 32, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
-template <> struct Tile<2, double> { static constexpr int TL = SW_D_TL12, TC = 32, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
+template <> struct Tile<0, double> { static constexpr int TL = SW_D_TL0, TC = SW_D_TC0, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
+template <> struct Tile<1, double> { static constexpr int TL = SW_D_TL12, TC = SW_D_TC12, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
+template <> struct Tile<2, double> { static constexpr int TL = SW_D_TL12, TC = SW_D_TC12, NT = SW_D_THREADS, MINB = SW_D_BLOCKS; };
 
 template <int DIR, class R> constexpr size_t sweep_smem_bytes(bool hybrid) {
     using T = Tile<DIR, R>;

@@ -170,6 +170,35 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
         tma_load_3d(rphi, &maps.phi, bar, x, y, z);
     };
 
+    // L2 prefetch of the rows Phase C reads for tile tid (the accumulators, J and, for a
+    // stage, U and Un): one prefetch per row of the tile's first and last line (rows of TL
+    // x-adjacent cells for eta / zeta; for xi, every 16 cells of a line)
+    auto prefetch_epilogue = [&](int tid) {
+        if (tid >= ntiles) return;
+        int c0, l0, other;
+        decode(tid, c0, l0, other);
+        const bool stage = a.out_mode == OUT_STAGE;
+        const int narr = 11 + (stage ? 10 : 0);  // acc 5, acc2 5, J 1, U 5, Un 5
+        const int nrow = DIR == 0 ? TL * (TC / 16) : 2 * TC;
+        for (int it = threadIdx.x; it < nrow * narr; it += NT) {
+            const int row = it % nrow, k = it / nrow;
+            int l, t;
+            if (DIR == 0) { l = row / (TC / 16); t = (row % (TC / 16)) * 16; }
+            else { t = row >> 1; l = (row & 1) ? TL - 1 : 0; }
+            long long c;
+            if (DIR == 0) c = lin3(P, c0 + t + NG, l0 + l + NG, other + NG);
+            else if (DIR == 1) c = lin3(P, l0 + l + NG, c0 + t + NG, other + NG);
+            else c = lin3(P, l0 + l + NG, other + NG, c0 + t + NG);
+            if (c >= P.plane) continue;  // lines beyond the grid on a ragged last tile
+            const void* addr;
+            if (k < 5) addr = static_cast<const float*>(a.acc) + c + k * P.plane;
+            else if (k < 10) addr = a.acc2 ? a.acc2 + c + (k - 5) * P.plane : nullptr;
+            else if (k == 10) addr = a.J + c;
+            else if (k < 16) addr = a.U + c + (k - 11) * P.plane;
+            else addr = a.combine ? a.Un + c + (k - 16) * P.plane : nullptr;
+            if (addr) asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
+        }
+    };
     unsigned* ctr = a.tile_ctr + DIR;  // zeroed before the three sweeps of an RHS
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
@@ -272,6 +301,8 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
             }
         }
         __syncthreads();
+        // the next tile's Phase C inputs into L2 while this tile finishes (last sweep only)
+        if (a.out_mode == OUT_RHS || a.out_mode == OUT_STAGE) prefetch_epilogue(counts[4]);
 
         // ---- Phase C: differences, viscous terms and the accumulation of out_mode
         sweep_epilogue<DIR, TL, TC, NT, float>(a, sF, c0, l0, other, nc, nl, cell, fidx);
