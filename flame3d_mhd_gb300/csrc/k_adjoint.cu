@@ -32,19 +32,32 @@ namespace f3d {
 #define V_NT12 192
 #define V_MB12 2
 #endif
-template <int DIR> struct VTile;
-template <> struct VTile<0> { static constexpr int TL = V_TL0, TC = 64, NT = V_NT0, MINB = V_MB0; };
-template <> struct VTile<1> { static constexpr int TL = V_TL12, TC = 64, NT = V_NT12, MINB = V_MB12; };
-template <> struct VTile<2> { static constexpr int TL = V_TL12, TC = 64, NT = V_NT12, MINB = V_MB12; };
+// characteristic-wise reverse sweeps: the reverse of a characteristic WENO face holds more
+// state (its eigenvectors, both sides' stencils of one field and their cotangents)
+#ifndef V_C_TL0
+#define V_C_TL0 4
+#define V_C_NT0 96
+#define V_C_MB0 4
+#define V_C_TL12 8
+#define V_C_NT12 192
+#define V_C_MB12 2
+#endif
+template <int DIR, bool CHAR = false> struct VTile;
+template <> struct VTile<0, false> { static constexpr int TL = V_TL0, TC = 64, NT = V_NT0, MINB = V_MB0; };
+template <> struct VTile<1, false> { static constexpr int TL = V_TL12, TC = 64, NT = V_NT12, MINB = V_MB12; };
+template <> struct VTile<2, false> { static constexpr int TL = V_TL12, TC = 64, NT = V_NT12, MINB = V_MB12; };
+template <> struct VTile<0, true> { static constexpr int TL = V_C_TL0, TC = 64, NT = V_C_NT0, MINB = V_C_MB0; };
+template <> struct VTile<1, true> { static constexpr int TL = V_C_TL12, TC = 64, NT = V_C_NT12, MINB = V_C_MB12; };
+template <> struct VTile<2, true> { static constexpr int TL = V_C_TL12, TC = 64, NT = V_C_NT12, MINB = V_C_MB12; };
 
-template <int DIR> constexpr size_t vjp_smem_bytes() {
-    return sizeof(double) * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 8) * 21 +
-           sizeof(int) * (2 * (size_t)VTile<DIR>::TL * (VTile<DIR>::TC + 1) + 4);
+template <int DIR, bool CHAR> constexpr size_t vjp_smem_bytes() {
+    using T = VTile<DIR, CHAR>;
+    return sizeof(double) * (size_t)T::TL * (T::TC + 8) * 21 + sizeof(int) * (2 * (size_t)T::TL * (T::TC + 1) + 4);
 }
 
 template <int DIR, bool CHAR>
-__global__ void __launch_bounds__(VTile<DIR>::NT, VTile<DIR>::MINB) k_sweep_vjp(const AdjArgs a) {
-    constexpr int TL = VTile<DIR>::TL, TC = VTile<DIR>::TC, NP = TC + 8, NT = VTile<DIR>::NT;
+__global__ void __launch_bounds__(VTile<DIR, CHAR>::NT, VTile<DIR, CHAR>::MINB) k_sweep_vjp(const AdjArgs a) {
+    constexpr int TL = VTile<DIR, CHAR>::TL, TC = VTile<DIR, CHAR>::TC, NP = TC + 8, NT = VTile<DIR, CHAR>::NT;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -574,19 +587,19 @@ __global__ void k_axpby(const DevParams P, double* out, const double* x, double 
 
 // ---- launchers --------------------------------------------------------------------------
 template <int DIR, bool CHAR> static cudaError_t launch_vjp_dir(const AdjArgs& a, cudaStream_t st) {
-    constexpr int TL = VTile<DIR>::TL, TC = VTile<DIR>::TC;
+    constexpr int TL = VTile<DIR, CHAR>::TL, TC = VTile<DIR, CHAR>::TC;
     const DevParams& P = a.P;
     dim3 grid;
     if (DIR == 0) grid = dim3(cdiv(P.nx, TC), cdiv(P.ny, TL), P.nz);
     else if (DIR == 1) grid = dim3(cdiv(P.nx, TL), cdiv(P.ny, TC), P.nz);
     else grid = dim3(cdiv(P.nx, TL), cdiv(P.nz, TC), P.ny);
-    k_sweep_vjp<DIR, CHAR><<<grid, VTile<DIR>::NT, vjp_smem_bytes<DIR>(), st>>>(a);
+    k_sweep_vjp<DIR, CHAR><<<grid, VTile<DIR, CHAR>::NT, vjp_smem_bytes<DIR, CHAR>(), st>>>(a);
     return cudaGetLastError();
 }
 
 template <int DIR, bool CHAR> static cudaError_t configure_vjp() {
     return cudaFuncSetAttribute(k_sweep_vjp<DIR, CHAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)vjp_smem_bytes<DIR>());
+                                (int)vjp_smem_bytes<DIR, CHAR>());
 }
 
 cudaError_t adjoint_configure() {

@@ -29,11 +29,21 @@
 namespace f3d {
 
 // Tiles of the TMA sweeps: xi 4 lines x 64 cells, eta / zeta 8 x-adjacent lines x 32 cells,
-// 128 threads (as the direct-load FP32 sweeps).
+// 128 threads (as the direct-load FP32 sweeps). The x extent of an eta / zeta box (TL floats)
+// must be a multiple of 4 and its x origin (first line + 4) too: TL a multiple of 4.
+#ifndef TMA_NT
+#define TMA_NT 128
+#define TMA_MINB 5
+#define TMA_TL0 4
+#define TMA_TC0 64
+#define TMA_TL12 8
+#define TMA_TC12 32
+#endif
 template <int DIR> struct TTile;
-template <> struct TTile<0> { static constexpr int TL = 4, TC = 64, NT = 128, MINB = 5; };
-template <> struct TTile<1> { static constexpr int TL = 8, TC = 32, NT = 128, MINB = 5; };
-template <> struct TTile<2> { static constexpr int TL = 8, TC = 32, NT = 128, MINB = 5; };
+template <> struct TTile<0> { static constexpr int TL = TMA_TL0, TC = TMA_TC0, NT = TMA_NT, MINB = TMA_MINB; };
+template <> struct TTile<1> { static constexpr int TL = TMA_TL12, TC = TMA_TC12, NT = TMA_NT, MINB = TMA_MINB; };
+template <> struct TTile<2> { static constexpr int TL = TMA_TL12, TC = TMA_TC12, NT = TMA_NT, MINB = TMA_MINB; };
+static_assert(TMA_TL12 % 4 == 0 && TMA_TC0 % 4 == 0, "TMA boxes need 16-byte x extents and origins");
 
 constexpr int kQVars = 6;     // rho, u, v, w, p, T
 constexpr int kMetVars = 7;   // A1, A2, A3, A1/|A|, A2/|A|, A3/|A|, |A| of the sweep direction
