@@ -204,6 +204,9 @@ struct f3d_ctx {
     // mixed form: the TMA-staged sweeps and their tensor maps (three directions)
     bool use_tma = false;
     void* tma_maps = nullptr;
+    // the last sweep's staged Phase C maps, encoded for the arrays of epi_key (U, Un, J)
+    void* epi_maps = nullptr;
+    const void* epi_key[3] = {};
     Prof* prof = nullptr;
     // adjoint scratch, allocated by the first VJP call
     void* adj_slab = nullptr;
@@ -417,8 +420,24 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
             a.stage1_copy = last.stage1_copy;
             a.dtl = last.dtl;
         }
-        if (ctx->use_tma) F3D_CUDA(ctx, launch_sweep_tma(d, a, ctx->tma_maps, st));
-        else F3D_CUDA(ctx, launch_sweep(d, a, st));
+        if (ctx->use_tma) {
+            // the last sweep stages its Phase C inputs too (not with a per-cell time step)
+            const void* epi = nullptr;
+            if (d == 2 && !a.dtl && (a.out_mode == OUT_RHS || a.out_mode == OUT_STAGE)) {
+                const double* Ue = a.out_mode == OUT_STAGE ? a.U : nullptr;
+                const double* Une = a.out_mode == OUT_STAGE ? a.Un : nullptr;
+                const void* key[3] = {Ue, Une, ctx->J};
+                if (std::memcmp(key, ctx->epi_key, sizeof(key)) != 0) {
+                    ctx->epi_key[0] = nullptr;  // invalid until encoded
+                    F3D_CUDA(ctx, make_epi_maps(ctx->dp, ctx->acc32, ctx->acc32b, ctx->J, Ue, Une, ctx->epi_maps));
+                    std::memcpy(ctx->epi_key, key, sizeof(key));
+                }
+                epi = ctx->epi_maps;
+            }
+            F3D_CUDA(ctx, launch_sweep_tma(d, a, ctx->tma_maps, epi, st));
+        } else {
+            F3D_CUDA(ctx, launch_sweep(d, a, st));
+        }
         mark(ctx, K_SWEEP_X + d, st);
     }
     return F3D_OK;
@@ -766,12 +785,14 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     if (want_tma) {
         ctx->tma_maps = std::aligned_alloc(64, (sweep_maps_bytes() + 63) & ~(size_t)63);
         const float* pack[3] = {ctx->m32.A[0], ctx->m32.A[3], ctx->m32.A[6]};
-        if (ctx->tma_maps &&
+        ctx->epi_maps = std::aligned_alloc(64, (epi_maps_bytes() + 63) & ~(size_t)63);
+        if (ctx->tma_maps && ctx->epi_maps &&
             make_sweep_maps(ctx->dp, ctx->Q32, pack, up(nc * 4), ctx->phi32, ctx->tma_maps) == cudaSuccess) {
             ctx->use_tma = true;
         } else {  // no tensor maps on this driver: the direct-load sweeps
             std::free(ctx->tma_maps);
-            ctx->tma_maps = nullptr;
+            std::free(ctx->epi_maps);
+            ctx->tma_maps = ctx->epi_maps = nullptr;
         }
     }
     *out = ctx;
@@ -786,6 +807,7 @@ int f3d_destroy(f3d_ctx* ctx) {
     if (ctx->lsave) cudaFree(ctx->lsave);
     if (ctx->extra) cudaFree(ctx->extra);
     std::free(ctx->tma_maps);
+    std::free(ctx->epi_maps);
     cudaError_t e = cudaFree(ctx->slab);
     delete ctx;
     return e == cudaSuccess ? F3D_OK : F3D_ERR_CUDA;

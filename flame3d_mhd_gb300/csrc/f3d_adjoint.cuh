@@ -341,7 +341,7 @@ __device__ __forceinline__ void split_mach_vjp(int method, const Cst<double>& K,
 // IS_k is a quadratic form whose gradient is formed from the coefficient table.
 // s0b (optional): += the cotangent of the scale s0 (t_k = eps + IS_k s0).
 __device__ __forceinline__ void weno5_vjp(const double V[5], double s0, double fb, double Vb[5],
-                                          double* s0b = nullptr) {
+                                          double* s0b = nullptr, double* fval = nullptr) {
     const double V1 = V[0], V2 = V[1], V3 = V[2], V4 = V[3], V5 = V[4];
     const double a1_ = V1 - 2 * V2 + V3, b1_ = V1 - 4 * V2 + 3 * V3;
     const double a2_ = V2 - 2 * V3 + V4, b2_ = V2 - V4;
@@ -361,6 +361,7 @@ __device__ __forceinline__ void weno5_vjp(const double V[5], double s0, double f
     const double rs = 1.0 / sum;
     double f = 0;
     for (int k = 0; k < 3; k++) f += al[k] * rs * q[k];
+    if (fval) *fval = f;  // the forward value (6x the reconstruction)
     double qb[3], ISb[3];
     for (int k = 0; k < 3; k++) {
         const double wk = al[k] * rs;
@@ -394,7 +395,7 @@ __device__ __constant__ const double kW7IS[4][4][4] = {
 __device__ __constant__ const double kW7Q[4][4] = {{-3, 13, -23, 25}, {1, -5, 13, 3}, {-1, 7, 7, -1}, {3, 13, -5, 1}};
 
 __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double fb, double Vb[7],
-                                          double* s0b = nullptr) {
+                                          double* s0b = nullptr, double* fval = nullptr) {
     const double d[4] = {1.0, 12.0, 18.0, 4.0};
     double q[4], t[4], IS[4];
     for (int k = 0; k < 4; k++) {
@@ -418,6 +419,7 @@ __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double f
     const double rs = 1.0 / sum;
     double f = 0;
     for (int k = 0; k < 4; k++) f += al[k] * rs * q[k];
+    if (fval) *fval = f;  // the forward value (12x the reconstruction)
     for (int j = 0; j < 7; j++) Vb[j] = 0.0;
     for (int k = 0; k < 4; k++) {
         const double wk = al[k] * rs;
@@ -447,10 +449,10 @@ __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double f
 // value) / addM(n, pos, value); stb[7] += cotangents of (u, v, w, T, A1, A2, A3) of the face
 // state; *s0b += the cotangent of s0 (weights' scale and n = A s0) when s0b is set.
 // br: 1 = WENO7, 2 = WENO5; t: the face's stencil origin (positions t..t+7).
-template <class FPA, class FMA, class ADDP, class ADDM>
-__device__ __forceinline__ void char_face_vjp(const DevParams& P, int br, int t, double s0, const double st[7],
-                                              const double Fb[5], FPA FP, FMA FM, ADDP addP, ADDM addM,
-                                              double stb[7], double* s0b) {
+template <bool W7, class FPA, class FMA, class ADDP, class ADDM>
+__device__ __forceinline__ void char_face_vjp_t(int t, const DevParams& P, double s0, const double st[7],
+                                                const double Fb[5], FPA FP, FMA FM, ADDP addP, ADDM addM,
+                                                double stb[7], double* s0b) {
     const Cst<double>& K = P.cd;
     const double u = st[0], v = st[1], w = st[2], T = st[3];
     const double nx = st[4] * s0, ny = st[5] * s0, nz = st[6] * s0;
@@ -464,9 +466,9 @@ __device__ __forceinline__ void char_face_vjp(const DevParams& P, int br, int t,
     const double gT = K.grg * T;
     const double rc = 1.0 / sqrt(gT), c = gT * rc, c2 = 0.5 * rc, Kc = K.gm1 * (rc * rc), K2 = 0.5 * Kc;
     const double H = gT * K.inv_gm1 + q2;
-    const bool w7 = br == 1;
+    constexpr bool w7 = W7;
     const double tmp = w7 ? 1.0 / 12.0 : 1.0 / 6.0;
-    const int np = w7 ? 7 : 5;
+    constexpr int np = w7 ? 7 : 5;  // stencil points a side (compile time: the arrays stay in registers)
     auto Lrow = [&](int k, double l[5]) {
         if (k == 0) { l[0] = K2 * q2 + qn * c2; l[1] = -(K2 * u + nx * c2); l[2] = -(K2 * v + ny * c2); l[3] = -(K2 * w + nz * c2); l[4] = K2; }
         else if (k == 1) { l[0] = 1.0 - Kc * q2; l[1] = Kc * u; l[2] = Kc * v; l[3] = Kc * w; l[4] = -Kc; }
@@ -477,70 +479,55 @@ __device__ __forceinline__ void char_face_vjp(const DevParams& P, int br, int t,
     // stencil positions of the two sides, in upwind order
     auto posP = [&](int k) { return w7 ? t + k : t + 1 + k; };
     auto posM = [&](int k) { return w7 ? t + 7 - k : t + 6 - k; };
-    // forward characteristic fluxes
-    double f[5];
-#pragma unroll 1
-    for (int k = 0; k < 5; k++) {
-        double l[5];
-        Lrow(k, l);
-        double VP[7], VM[7];
-        for (int j = 0; j < np; j++) {
-            const int a = posP(j), b = posM(j);
-            VP[j] = FP(0, a) * l[0] + FP(1, a) * l[1] + FP(2, a) * l[2] + FP(3, a) * l[3] + FP(4, a) * l[4];
-            VM[j] = FM(0, b) * l[0] + FM(1, b) * l[1] + FM(2, b) * l[2] + FM(3, b) * l[3] + FM(4, b) * l[4];
-        }
-        f[k] = w7 ? (weno7(VP[0], VP[1], VP[2], VP[3], VP[4], VP[5], VP[6], s0) +
-                     weno7(VM[0], VM[1], VM[2], VM[3], VM[4], VM[5], VM[6], s0)) * tmp
-                  : (weno5(VP[0], VP[1], VP[2], VP[3], VP[4], s0) + weno5(VM[0], VM[1], VM[2], VM[3], VM[4], s0)) * tmp;
-    }
-    // ---- reverse of out = R f (the right eigenvectors, schemes.jl:983-999)
+    // ---- reverse of out = R f (the right eigenvectors, schemes.jl:983-999): the cotangents of
+    // the characteristic fluxes f need R only; the terms that need f itself (R's dependence on
+    // the face state) are linear in f and added once the field loop has formed each f_k
     const double fb[5] = {
         Fb[0] + Fb[1] * (u - c * nx) + Fb[2] * (v - c * ny) + Fb[3] * (w - c * nz) + Fb[4] * (H - qn * c),
         Fb[0] + Fb[1] * u + Fb[2] * v + Fb[3] * w + Fb[4] * q2,
         Fb[0] + Fb[1] * (u + c * nx) + Fb[2] * (v + c * ny) + Fb[3] * (w + c * nz) + Fb[4] * (H + qn * c),
         Fb[1] * lx + Fb[2] * ly + Fb[3] * lz + Fb[4] * ql,
         Fb[1] * mx + Fb[2] * my + Fb[3] * mz + Fb[4] * qm};
-    const double s012 = f[0] + f[1] + f[2], d20 = f[2] - f[0];
-    double ub = s012 * Fb[1], vb = s012 * Fb[2], wb = s012 * Fb[3];
-    double cb = d20 * (nx * Fb[1] + ny * Fb[2] + nz * Fb[3] + qn * Fb[4]);
-    double nxb = c * d20 * Fb[1], nyb = c * d20 * Fb[2], nzb = c * d20 * Fb[3];
-    double qnb = c * d20 * Fb[4];
-    double Hb = (f[0] + f[2]) * Fb[4];
-    double q2b = f[1] * Fb[4];
-    double lxb = f[3] * Fb[1], lyb = f[3] * Fb[2], lzb = f[3] * Fb[3], qlb = f[3] * Fb[4];
-    double mxb = f[4] * Fb[1], myb = f[4] * Fb[2], mzb = f[4] * Fb[3], qmb = f[4] * Fb[4];
-    double K2b = 0.0, Kcb = 0.0, c2b = 0.0;
+    double f[5];
+    double ub = 0.0, vb = 0.0, wb = 0.0, nxb = 0.0, nyb = 0.0, nzb = 0.0, qnb = 0.0, q2b = 0.0;
+    double lxb = 0.0, lyb = 0.0, lzb = 0.0, qlb = 0.0, mxb = 0.0, myb = 0.0, mzb = 0.0, qmb = 0.0;
+    double K2b = 0.0, Kcb = 0.0, c2b = 0.0, cb = 0.0, Hb = 0.0;
     // ---- reverse of the WENO of each field and of the projections L_k . F
 #pragma unroll 1
     for (int k = 0; k < 5; k++) {
         const double g = fb[k] * tmp;
-        if (g == 0.0) continue;
         double l[5];
         Lrow(k, l);
-        double VP[7], VM[7], VPb[7], VMb[7];
-        for (int j = 0; j < np; j++) {
-            const int a = posP(j), b = posM(j);
-            VP[j] = FP(0, a) * l[0] + FP(1, a) * l[1] + FP(2, a) * l[2] + FP(3, a) * l[3] + FP(4, a) * l[4];
-            VM[j] = FM(0, b) * l[0] + FM(1, b) * l[1] + FM(2, b) * l[2] + FM(3, b) * l[3] + FM(4, b) * l[4];
-        }
-        if (w7) {
-            weno7_vjp(VP, s0, g, VPb, s0b);
-            weno7_vjp(VM, s0, g, VMb, s0b);
-        } else {
-            weno5_vjp(VP, s0, g, VPb, s0b);
-            weno5_vjp(VM, s0, g, VMb, s0b);
-        }
+        // the two sides one after the other (fewer live registers): projections L_k . F on the
+        // side's stencil, the WENO reverse (with the side's forward value), the cotangents of the
+        // split fluxes and of row k of L
         double lb[5] = {0, 0, 0, 0, 0};
-        for (int j = 0; j < np; j++) {
-            const int a = posP(j), b = posM(j);
-            for (int e = 0; e < 5; e++) {
-                lb[e] += FP(e, a) * VPb[j] + FM(e, b) * VMb[j];
-                if (l[e] != 0.0) {
-                    addP(e, a, l[e] * VPb[j]);
-                    addM(e, b, l[e] * VMb[j]);
+        double fs[2];
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            double V[np], Vb[np];
+#pragma unroll
+            for (int j = 0; j < np; j++) {
+                const int a = side == 0 ? posP(j) : posM(j);
+                V[j] = side == 0 ? FP(0, a) * l[0] + FP(1, a) * l[1] + FP(2, a) * l[2] + FP(3, a) * l[3] + FP(4, a) * l[4]
+                                 : FM(0, a) * l[0] + FM(1, a) * l[1] + FM(2, a) * l[2] + FM(3, a) * l[3] + FM(4, a) * l[4];
+            }
+            if constexpr (W7) weno7_vjp(V, s0, g, Vb, s0b, &fs[side]);
+            else weno5_vjp(V, s0, g, Vb, s0b, &fs[side]);
+#pragma unroll
+            for (int j = 0; j < np; j++) {
+                const int a = side == 0 ? posP(j) : posM(j);
+#pragma unroll
+                for (int e = 0; e < 5; e++) {
+                    lb[e] += (side == 0 ? FP(e, a) : FM(e, a)) * Vb[j];
+                    if (l[e] != 0.0) {
+                        if (side == 0) addP(e, a, l[e] * Vb[j]);
+                        else addM(e, a, l[e] * Vb[j]);
+                    }
                 }
             }
         }
+        f[k] = (fs[0] + fs[1]) * tmp;
         // row k of L in terms of the face quantities
         if (k == 0 || k == 2) {
             const double sg = k == 0 ? 1.0 : -1.0;
@@ -571,6 +558,22 @@ __device__ __forceinline__ void char_face_vjp(const DevParams& P, int br, int t,
             myb += lb[2];
             mzb += lb[3];
         }
+    }
+    // R's dependence on the face state (out = R f)
+    {
+        const double s012 = f[0] + f[1] + f[2], d20 = f[2] - f[0];
+        ub += s012 * Fb[1];
+        vb += s012 * Fb[2];
+        wb += s012 * Fb[3];
+        cb += d20 * (nx * Fb[1] + ny * Fb[2] + nz * Fb[3] + qn * Fb[4]);
+        nxb += c * d20 * Fb[1];
+        nyb += c * d20 * Fb[2];
+        nzb += c * d20 * Fb[3];
+        qnb += c * d20 * Fb[4];
+        Hb += (f[0] + f[2]) * Fb[4];
+        q2b += f[1] * Fb[4];
+        lxb += f[3] * Fb[1]; lyb += f[3] * Fb[2]; lzb += f[3] * Fb[3]; qlb += f[3] * Fb[4];
+        mxb += f[4] * Fb[1]; myb += f[4] * Fb[2]; mzb += f[4] * Fb[3]; qmb += f[4] * Fb[4];
     }
     // ---- the face quantities in terms of (u, v, w, T, n)
     Kcb += 0.5 * K2b;                                  // K2 = Kc / 2
@@ -619,6 +622,14 @@ __device__ __forceinline__ void char_face_vjp(const DevParams& P, int br, int t,
     stb[5] += nyb * s0;
     stb[6] += nzb * s0;
     if (s0b) *s0b += nxb * st[4] + nyb * st[5] + nzb * st[6];
+}
+
+template <class FPA, class FMA, class ADDP, class ADDM>
+__device__ __forceinline__ void char_face_vjp(const DevParams& P, int br, int t, double s0, const double st[7],
+                                              const double Fb[5], FPA FP, FMA FM, ADDP addP, ADDM addM,
+                                              double stb[7], double* s0b) {
+    if (br == 1) char_face_vjp_t<true>(t, P, s0, st, Fb, FP, FM, addP, addM, stb, s0b);
+    else char_face_vjp_t<false>(t, P, s0, st, Fb, FP, FM, addP, addM, stb, s0b);
 }
 
 }  // namespace f3d

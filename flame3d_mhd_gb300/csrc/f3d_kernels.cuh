@@ -95,7 +95,11 @@ cudaError_t sweep_tma_configure();
 size_t sweep_maps_bytes();
 cudaError_t make_sweep_maps(const DevParams& P, const float* q32, const float* const pack[3], size_t pack_stride,
                             const float* phi, void* maps3);
-cudaError_t launch_sweep_tma(int dir, const SweepArgs& a, const void* maps3, cudaStream_t st);
+// epi: the last sweep's staged Phase C maps (make_epi_maps) or null (direct loads)
+cudaError_t launch_sweep_tma(int dir, const SweepArgs& a, const void* maps3, const void* epi, cudaStream_t st);
+size_t epi_maps_bytes();
+cudaError_t make_epi_maps(const DevParams& P, const float* acc, const float* acc2, const double* J,
+                          const double* U, const double* Un, void* out);
 
 // finite-volume scheme (k_fvm.cu): geo = (nx, ny, nz, area) of the faces of x, y, z at
 // their left cells; U the conserved state the faces reconstruct from

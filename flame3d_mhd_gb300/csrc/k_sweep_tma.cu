@@ -8,6 +8,9 @@
 //    lines x (TC + 8) positions with their 4-cell halos, copied by cp.async.bulk.tensor into
 //    shared memory and completed on an mbarrier; the boxes land in the [var][line][pos] /
 //    [var][pos][line] layouts the phases index, so no thread issues a global load for them;
+//  - in the last sweep of an RHS (the zeta sweep), the inputs of Phase C (the two FP32
+//    direction sums, J and, for a stage, U and Un) arrive the same way on a second mbarrier,
+//    issued as soon as the previous tile's Phase C is done;
 //  - blocks are persistent: each takes its next tile from a counter of the launch (atomicAdd;
 //    the shock-capturing faces cluster in a few tile columns, so a static assignment would
 //    leave some blocks with all of them) and issues that tile's copies as soon as Phase A has
@@ -48,7 +51,7 @@ static_assert(TMA_TL12 % 4 == 0 && TMA_TC0 % 4 == 0, "TMA boxes need 16-byte x e
 constexpr int kQVars = 6;     // rho, u, v, w, p, T
 constexpr int kMetVars = 7;   // A1, A2, A3, A1/|A|, A2/|A|, A3/|A|, |A| of the sweep direction
 
-template <int DIR> struct TmaLayout {
+template <int DIR, bool EPI = false> struct TmaLayout {
     static constexpr int TL = TTile<DIR>::TL, TC = TTile<DIR>::TC, NP = TC + 8, NF = TC + 1;
     static constexpr int BOX = TL * NP;                                   // floats per variable
     static constexpr size_t raw_q = 0;                                    // 6 x BOX
@@ -61,7 +64,17 @@ template <int DIR> struct TmaLayout {
     static constexpr size_t sabs = phi + sizeof(float) * BOX;             // |A|, BOX
     static constexpr size_t lists = sabs + sizeof(float) * BOX;           // 2 x TL x NF ints + 4
     static constexpr size_t bar = (lists + sizeof(int) * (2 * TL * NF + 6) + 7) & ~(size_t)7;
-    static constexpr size_t total = bar + 8;
+    // staged Phase C inputs of the last sweep (EPI): boxes of the tile's TL x TC interior cells
+    static constexpr int CELLS = TL * TC;
+    static constexpr size_t e_acc = (bar + 16 + 127) & ~(size_t)127;       // 5 x CELLS floats
+    static constexpr size_t e_acc2 = e_acc + sizeof(float) * 5 * CELLS;    // 5 x CELLS floats
+    static constexpr size_t e_J = e_acc2 + sizeof(float) * 5 * CELLS;      // CELLS doubles
+    static constexpr size_t e_U = e_J + sizeof(double) * CELLS;            // 5 x CELLS doubles
+    static constexpr size_t e_Un = e_U + sizeof(double) * 5 * CELLS;       // 5 x CELLS doubles
+    static constexpr size_t total = EPI ? e_Un + sizeof(double) * 5 * CELLS : bar + 16;
+    static constexpr unsigned epi_rhs_bytes = (unsigned)(sizeof(float) * 10 * CELLS + sizeof(double) * CELLS);
+    static constexpr unsigned epi_u_bytes = (unsigned)(sizeof(double) * 5 * CELLS);
+    static_assert((sizeof(float) * CELLS) % 128 == 0, "staged Phase C boxes must start 128-byte aligned");
     // bytes one tile's copies deliver (complete_tx counts whole boxes, filled or not)
     static constexpr unsigned tx_bytes = (unsigned)(sizeof(float) * (kQVars + kMetVars + 1) * BOX);
     static_assert((sizeof(float) * BOX) % 128 == 0, "every box must start 128-byte aligned");
@@ -127,13 +140,20 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 struct SweepMaps {  // CUtensorMap is 64-byte aligned
     CUtensorMap q, m, phi;
 };
+// Phase C inputs of the last sweep: the FP32 direction sums (x, y, z, 5) x 2, J (x, y, z) and
+// U, Un (x, y, z, 5) in FP64; box (TL, 1, TC[, n]) of the zeta tile's interior cells
+struct EpiMaps {
+    CUtensorMap acc, acc2, J, U, Un;
+};
 
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s: a tile copy takes microseconds
 
-template <int DIR, bool CHAR>
+template <int DIR, bool CHAR, bool EPI>
 __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
-    k_sweep_tma(const __grid_constant__ SweepArgs a, const __grid_constant__ SweepMaps maps) {
-    using L = TmaLayout<DIR>;
+    k_sweep_tma(const __grid_constant__ SweepArgs a, const __grid_constant__ SweepMaps maps,
+                const __grid_constant__ EpiMaps em) {
+    static_assert(!EPI || DIR == 2, "Phase C is staged in the last (zeta) sweep only");
+    using L = TmaLayout<DIR, EPI>;
     constexpr int TL = L::TL, TC = L::TC, NP = L::NP, NF = L::NF, BOX = L::BOX, NT = TTile<DIR>::NT;
     const DevParams& P = a.P;
     const bool hybrid = P.fixed_branch < 0;
@@ -150,6 +170,8 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
     int* list5 = list7 + TL * NF;
     int* counts = list5 + TL * NF;  // counts[0..1]: WENO7 / WENO5 queue lengths; counts[4]: next tile
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem_raw + L::bar);
+    unsigned long long* ebar = bar + 1;  // the staged Phase C inputs (EPI)
+    const bool stage = a.out_mode == OUT_STAGE;
 
     const int Nd = DIR == 0 ? P.nx : (DIR == 1 ? P.ny : P.nz);
     const int Nl = DIR == 0 ? P.ny : P.nx;
@@ -180,6 +202,20 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
         tma_load_3d(rphi, &maps.phi, bar, x, y, z);
     };
 
+    auto issue_epi = [&](int tid) {  // one thread: the Phase C copies of tile tid (EPI)
+        int c0, l0, other;
+        decode(tid, c0, l0, other);
+        const int x = l0 + NG, y = other + NG, z = c0 + NG;
+        fence_proxy_async();
+        mbar_expect_tx(ebar, L::epi_rhs_bytes + (stage ? L::epi_u_bytes * (a.combine ? 2u : 1u) : 0u));
+        tma_load_4d(smem_raw + L::e_acc, &em.acc, ebar, x, y, z, 0);
+        tma_load_4d(smem_raw + L::e_acc2, &em.acc2, ebar, x, y, z, 0);
+        tma_load_3d(smem_raw + L::e_J, &em.J, ebar, x, y, z);
+        if (stage) {
+            tma_load_4d(smem_raw + L::e_U, &em.U, ebar, x, y, z, 0);
+            if (a.combine) tma_load_4d(smem_raw + L::e_Un, &em.Un, ebar, x, y, z, 0);
+        }
+    };
     // L2 prefetch of the rows Phase C reads for tile tid (the accumulators, J and, for a
     // stage, U and Un): one prefetch per row of the tile's first and last line (rows of TL
     // x-adjacent cells for eta / zeta; for xi, every 16 cells of a line)
@@ -209,13 +245,69 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
             if (addr) asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
         }
     };
+    // Phase C of the last sweep from the staged boxes ([n][t][l]: cell (l, t) of the tile):
+    // the face-flux difference and the CD4 viscous divergence (Fv from global memory), the
+    // compensated sum of the three directions, then J x L (OUT_RHS) or the RK update in FP64
+    auto staged_epilogue = [&](int c0, int l0, int other, int nc, int nl) {
+        const float* eacc = reinterpret_cast<const float*>(smem_raw + L::e_acc);
+        const float* eacc2 = reinterpret_cast<const float*>(smem_raw + L::e_acc2);
+        const double* eJ = reinterpret_cast<const double*>(smem_raw + L::e_J);
+        const double* eU = reinterpret_cast<const double*>(smem_raw + L::e_U);
+        const double* eUn = reinterpret_cast<const double*>(smem_raw + L::e_Un);
+        constexpr int CELLS = L::CELLS;
+        const long long pl = P.plane;
+        const int vxt = P.nxt - 4, vyt = P.nyt - 4, vzt = P.nzt - 4;
+        const long long vplane = (long long)vxt * vyt * vzt;
+        const float* Fvr = static_cast<const float*>(a.Fv);
+        for (int it = threadIdx.x; it < CELLS; it += NT) {
+            const int t = it / TL, l = it - t * TL;
+            if (l >= nl || t >= nc) continue;
+            const long long c = lin3(P, l0 + l + NG, other + NG, c0 + t + NG);
+            float d[5];
+#pragma unroll
+            for (int n = 0; n < 5; n++) d[n] = sF[n * TL * NF + fidx(l, t)] - sF[n * TL * NF + fidx(l, t + 1)];
+            if (Fvr) {  // Fv index = full index - 2 in every dimension (viscous.jl:119, div.jl:14-39)
+                const long long vc = (l0 + l + NG - 2) + (long long)vxt * ((other + NG - 2) + (long long)vyt * (c0 + t + NG - 2));
+                const long long vs = (long long)vxt * vyt;
+                const float k1 = 1.f / 12.f, k2 = -2.f / 3.f;
+#pragma unroll
+                for (int n = 0; n < 4; n++) {
+                    const float* F = Fvr + n * vplane + vc;
+                    d[n + 1] += k1 * (F[-2 * vs] - F[2 * vs]) + k2 * (F[-vs] - F[vs]);
+                }
+            }
+            double L5[5];
+#pragma unroll
+            for (int n = 0; n < 5; n++)
+                L5[n] = to_f64(sum3_compensated(eacc[n * CELLS + it], eacc2[n * CELLS + it], d[n]));
+            if (!stage) {
+                const double Jc = eJ[it];
+#pragma unroll
+                for (int n = 0; n < 5; n++) a.out[c + n * pl] = Jc * L5[n];
+            } else {
+                const double Jact = eJ[it] * a.dt;
+#pragma unroll
+                for (int n = 0; n < 5; n++) {
+                    const double u = eU[n * CELLS + it];
+                    if (a.stage1_copy) a.Un[c + n * pl] = u;
+                    double un = u + L5[n] * Jact;
+                    if (a.combine) un = un * a.ca + eUn[n * CELLS + it] * a.cb;
+                    a.U[c + n * pl] = un;
+                }
+            }
+        }
+    };
     unsigned* ctr = a.tile_ctr + DIR;  // zeroed before the three sweeps of an RHS
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
+        if (EPI) mbar_init(ebar, 1);
         fence_mbar_init();
         const int first = (int)atomicAdd(ctr, 1u);
         counts[4] = first;
-        if (first < ntiles) issue(first);
+        if (first < ntiles) {
+            issue(first);
+            if (EPI) issue_epi(first);
+        }
     }
     __syncthreads();
     int tile = counts[4];
@@ -233,9 +325,10 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
         int timed_out = 0;
         if (threadIdx.x == 0) {
             timed_out = !mbar_wait_bounded(bar, parity, kWaitLimitNs);
-            if (timed_out) {
+            if (timed_out) {  // drain what may be in flight (this tile's copies), bounded again
                 atomicOr(a.kstat, 1u);
-                mbar_wait_bounded(bar, parity, kWaitLimitNs);  // the copy in flight, bounded again
+                mbar_wait_bounded(bar, parity, kWaitLimitNs);
+                if (EPI) mbar_wait_bounded(ebar, parity, kWaitLimitNs);
             }
             counts[0] = 0;
             counts[1] = 0;
@@ -311,12 +404,29 @@ __global__ void __launch_bounds__(TTile<DIR>::NT, TTile<DIR>::MINB)
             }
         }
         __syncthreads();
-        // the next tile's Phase C inputs into L2 while this tile finishes (last sweep only)
-        if (a.out_mode == OUT_RHS || a.out_mode == OUT_STAGE) prefetch_epilogue(counts[4]);
+        if constexpr (EPI) {
+            // ---- Phase C from the staged boxes: wait for this tile's copies (bounded)
+            int eto = 0;
+            if (threadIdx.x == 0) {
+                eto = !mbar_wait_bounded(ebar, parity, kWaitLimitNs);
+                if (eto) {  // drain: this tile's Phase C copies and the next tile's staged inputs
+                    atomicOr(a.kstat, 1u);
+                    mbar_wait_bounded(ebar, parity, kWaitLimitNs);
+                    if (counts[4] < ntiles) mbar_wait_bounded(bar, parity ^ 1u, kWaitLimitNs);
+                }
+            }
+            if (__syncthreads_or(eto)) return;
+            staged_epilogue(c0, l0, other, nc, nl);
+            __syncthreads();  // sF, the lists and the staged boxes are rewritten by the next tile
+            if (threadIdx.x == 0 && counts[4] < ntiles) issue_epi(counts[4]);
+        } else {
+            // the next tile's Phase C inputs into L2 while this tile finishes (last sweep only)
+            if (a.out_mode == OUT_RHS || a.out_mode == OUT_STAGE) prefetch_epilogue(counts[4]);
 
-        // ---- Phase C: differences, viscous terms and the accumulation of out_mode
-        sweep_epilogue<DIR, TL, TC, NT, float>(a, sF, c0, l0, other, nc, nl, cell, fidx);
-        __syncthreads();  // sF, sPhi and the lists are rewritten by the next tile
+            // ---- Phase C: differences, viscous terms and the accumulation of out_mode
+            sweep_epilogue<DIR, TL, TC, NT, float>(a, sF, c0, l0, other, nc, nl, cell, fidx);
+            __syncthreads();  // sF, sPhi and the lists are rewritten by the next tile
+        }
         tile = counts[4];
     }
 }
@@ -338,16 +448,19 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// rank-3 or rank-4 FP32 tensor (x, y, z[, n]) with component stride cstride bytes
-bool encode(CUtensorMap* map, const DevParams& P, const void* base, int ncomp, size_t cstride, const unsigned box[3]) {
+// rank-3 or rank-4 tensor (x, y, z[, n]) over the full grid with component stride cstride
+// bytes; FP32 (esize 4) or FP64 (esize 8) elements
+bool encode(CUtensorMap* map, const DevParams& P, const void* base, int ncomp, size_t cstride, const unsigned box[3],
+            int esize = 4) {
     auto fn = encode_fn();
-    if (!fn) return false;
+    if (!fn || !base) return false;
     const int rank = ncomp > 1 ? 4 : 3;
     cuuint64_t dims[4] = {(cuuint64_t)P.nxt, (cuuint64_t)P.nyt, (cuuint64_t)P.nzt, (cuuint64_t)ncomp};
-    cuuint64_t strides[3] = {(cuuint64_t)P.nxt * 4, (cuuint64_t)P.nxt * P.nyt * 4, (cuuint64_t)cstride};
+    cuuint64_t strides[3] = {(cuuint64_t)P.nxt * esize, (cuuint64_t)P.nxt * P.nyt * esize, (cuuint64_t)cstride};
     cuuint32_t bdim[4] = {box[0], box[1], box[2], (cuuint32_t)ncomp};
     cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<void*>(base), dims, strides, bdim, estr,
+    CUresult r = fn(map, esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank,
+                    const_cast<void*>(base), dims, strides, bdim, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
@@ -363,30 +476,33 @@ template <int DIR> void box_of(unsigned box[3]) {
 constexpr int kMaxDev = 32;
 int g_blocks[kMaxDev][3][2] = {};  // resident blocks per SM x SMs, per device, direction, char flag
 
-template <int DIR, bool CHAR> cudaError_t configure_one(int dev) {
-    auto k = k_sweep_tma<DIR, CHAR>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TmaLayout<DIR>::total);
+int g_blocks_epi[kMaxDev][2] = {};  // the same for the staged-epilogue zeta sweep
+
+template <int DIR, bool CHAR, bool EPI> cudaError_t configure_one(int dev) {
+    auto k = k_sweep_tma<DIR, CHAR, EPI>;
+    constexpr size_t smem = TmaLayout<DIR, EPI>::total;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0, nsm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TTile<DIR>::NT, TmaLayout<DIR>::total)) !=
-        cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TTile<DIR>::NT, smem)) != cudaSuccess)
         return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    g_blocks[dev][DIR][CHAR ? 1 : 0] = (per_sm > 0 ? per_sm : 1) * nsm;
+    (EPI ? g_blocks_epi[dev][CHAR ? 1 : 0] : g_blocks[dev][DIR][CHAR ? 1 : 0]) = (per_sm > 0 ? per_sm : 1) * nsm;
     return cudaSuccess;
 }
 
-template <int DIR, bool CHAR> cudaError_t launch_one(const SweepArgs& a, const SweepMaps& m, int dev, cudaStream_t st) {
-    using L = TmaLayout<DIR>;
+template <int DIR, bool CHAR, bool EPI>
+cudaError_t launch_one(const SweepArgs& a, const SweepMaps& m, const EpiMaps& em, int dev, cudaStream_t st) {
+    using L = TmaLayout<DIR, EPI>;
     const DevParams& P = a.P;
     const int Nd = DIR == 0 ? P.nx : (DIR == 1 ? P.ny : P.nz);
     const int Nl = DIR == 0 ? P.ny : P.nx;
     const int No = DIR == 2 ? P.ny : P.nz;
     const long long ntiles = (long long)((Nd + L::TC - 1) / L::TC) * ((Nl + L::TL - 1) / L::TL) * No;
-    int blocks = g_blocks[dev][DIR][CHAR ? 1 : 0];
+    int blocks = EPI ? g_blocks_epi[dev][CHAR ? 1 : 0] : g_blocks[dev][DIR][CHAR ? 1 : 0];
     if (blocks <= 0) return cudaErrorNotReady;
     if (ntiles < blocks) blocks = (int)ntiles;
-    k_sweep_tma<DIR, CHAR><<<blocks, TTile<DIR>::NT, L::total, st>>>(a, m);
+    k_sweep_tma<DIR, CHAR, EPI><<<blocks, TTile<DIR>::NT, L::total, st>>>(a, m, em);
     return cudaGetLastError();
 }
 
@@ -401,12 +517,14 @@ cudaError_t sweep_tma_configure() {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
-    if ((e = configure_one<0, false>(dev)) != cudaSuccess) return e;
-    if ((e = configure_one<0, true>(dev)) != cudaSuccess) return e;
-    if ((e = configure_one<1, false>(dev)) != cudaSuccess) return e;
-    if ((e = configure_one<1, true>(dev)) != cudaSuccess) return e;
-    if ((e = configure_one<2, false>(dev)) != cudaSuccess) return e;
-    return configure_one<2, true>(dev);
+    if ((e = configure_one<0, false, false>(dev)) != cudaSuccess) return e;
+    if ((e = configure_one<0, true, false>(dev)) != cudaSuccess) return e;
+    if ((e = configure_one<1, false, false>(dev)) != cudaSuccess) return e;
+    if ((e = configure_one<1, true, false>(dev)) != cudaSuccess) return e;
+    if ((e = configure_one<2, false, false>(dev)) != cudaSuccess) return e;
+    if ((e = configure_one<2, true, false>(dev)) != cudaSuccess) return e;
+    if ((e = configure_one<2, false, true>(dev)) != cudaSuccess) return e;
+    return configure_one<2, true, true>(dev);
 }
 
 // Tensor maps of the three directions over the context's FP32 arrays: Q32 (6 planes of
@@ -428,17 +546,39 @@ cudaError_t make_sweep_maps(const DevParams& P, const float* q32, const float* c
 }
 
 size_t sweep_maps_bytes() { return sizeof(SweepMaps) * 3; }
+size_t epi_maps_bytes() { return sizeof(EpiMaps); }
 
-cudaError_t launch_sweep_tma(int dir, const SweepArgs& a, const void* maps3, cudaStream_t st) {
+// Phase C maps of the last (zeta) sweep: the FP32 direction sums acc, acc2 (5 planes of
+// P.plane floats each), J and, when given, U and Un (5 planes of P.plane doubles).
+cudaError_t make_epi_maps(const DevParams& P, const float* acc, const float* acc2, const double* J,
+                          const double* U, const double* Un, void* out) {
+    EpiMaps* m = static_cast<EpiMaps*>(out);
+    using L = TmaLayout<2, true>;
+    const unsigned box[3] = {(unsigned)L::TL, 1u, (unsigned)L::TC};
+    const size_t p4 = (size_t)P.plane * 4, p8 = (size_t)P.plane * 8;
+    if (!encode(&m->acc, P, acc, 5, p4, box) || !encode(&m->acc2, P, acc2, 5, p4, box) ||
+        !encode(&m->J, P, J, 1, 0, box, 8))
+        return cudaErrorInvalidValue;
+    if (U && !encode(&m->U, P, U, 5, p8, box, 8)) return cudaErrorInvalidValue;
+    if (Un && !encode(&m->Un, P, Un, 5, p8, box, 8)) return cudaErrorInvalidValue;
+    return cudaSuccess;
+}
+
+cudaError_t launch_sweep_tma(int dir, const SweepArgs& a, const void* maps3, const void* epi, cudaStream_t st) {
     const SweepMaps* m = static_cast<const SweepMaps*>(maps3);
+    static const EpiMaps none{};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
     const bool ch = a.P.character != 0;
-    if (dir == 0) return ch ? launch_one<0, true>(a, m[0], dev, st) : launch_one<0, false>(a, m[0], dev, st);
-    if (dir == 1) return ch ? launch_one<1, true>(a, m[1], dev, st) : launch_one<1, false>(a, m[1], dev, st);
-    return ch ? launch_one<2, true>(a, m[2], dev, st) : launch_one<2, false>(a, m[2], dev, st);
+    if (dir == 0) return ch ? launch_one<0, true, false>(a, m[0], none, dev, st) : launch_one<0, false, false>(a, m[0], none, dev, st);
+    if (dir == 1) return ch ? launch_one<1, true, false>(a, m[1], none, dev, st) : launch_one<1, false, false>(a, m[1], none, dev, st);
+    if (epi) {
+        const EpiMaps& em = *static_cast<const EpiMaps*>(epi);
+        return ch ? launch_one<2, true, true>(a, m[2], em, dev, st) : launch_one<2, false, true>(a, m[2], em, dev, st);
+    }
+    return ch ? launch_one<2, true, false>(a, m[2], none, dev, st) : launch_one<2, false, false>(a, m[2], none, dev, st);
 }
 
 }  // namespace f3d
