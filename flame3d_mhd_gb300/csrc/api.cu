@@ -1284,7 +1284,7 @@ int f3d_check_finite(f3d_ctx* ctx, const double* U, f3d_stream stream) {
 int f3d_debug_sensor(f3d_ctx* ctx, const double* Q, double* phi, f3d_stream stream) {
     int rc = check_ctx(ctx, false);
     if (rc || (rc = check_ptrs(ctx, {Q, phi}))) return rc;
-    F3D_CUDA(ctx, launch_sensor(ctx->dp, Q, phi, (cudaStream_t)stream));
+    F3D_CUDA(ctx, launch_sensor(ctx->dp, Q, phi, (cudaStream_t)stream, true));
     return F3D_OK;
 }
 

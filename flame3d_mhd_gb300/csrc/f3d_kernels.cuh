@@ -148,7 +148,9 @@ cudaError_t launch_c2prim_interior(const DevParams& P, const double* U, double* 
 cudaError_t launch_prim2c(const DevParams& P, const double* Q, double* U, cudaStream_t st);
 cudaError_t launch_lincomb(const DevParams& P, double* U, const double* Un, double a, double b, cudaStream_t st);
 cudaError_t launch_sound(const DevParams& P, const double* Q, double* csnd, cudaStream_t st);
-cudaError_t launch_sensor(const DevParams& P, const double* Q, double* phi, cudaStream_t st);
+// exact: phi bit for bit as the oracle's; otherwise values that give the same branch map
+// (FP32 away from the thresholds, FP64 near them)
+cudaError_t launch_sensor(const DevParams& P, const double* Q, double* phi, cudaStream_t st, bool exact = false);
 cudaError_t launch_metric_prep(const DevParams& P, const double* const m[9], double* S[3], double* Ah[9],
                                cudaStream_t st);
 cudaError_t launch_split_debug(const DevParams& P, const double* Q, const double* csnd, const double* const A[3],

@@ -33,13 +33,16 @@ namespace f3d {
 #define V_MB12 2
 #endif
 // characteristic-wise reverse sweeps: the reverse of a characteristic WENO face holds more
-// state (its eigenvectors, both sides' stencils of one field and their cotangents)
+// state (its eigenvectors, a side's stencil of one field and its cotangents). Smaller blocks
+// (xi 4 x 64 on 64 threads, three per SM; eta / zeta 4 x 64 on 96 threads, two per SM):
+// adjoint / forward 3.70 on the 256x64x64 shock tube against 3.78 for the component-wise
+// shape and 3.90 for 192-thread blocks with 255 registers (same box, alternating builds)
 #ifndef V_C_TL0
 #define V_C_TL0 4
-#define V_C_NT0 96
-#define V_C_MB0 4
-#define V_C_TL12 8
-#define V_C_NT12 192
+#define V_C_NT0 64
+#define V_C_MB0 3
+#define V_C_TL12 4
+#define V_C_NT12 96
 #define V_C_MB12 2
 #endif
 template <int DIR, bool CHAR = false> struct VTile;

@@ -262,7 +262,16 @@ __device__ __forceinline__ double sensor_term(double a, double b, double c) {
     double den = __dadd_rn(__dadd_rn(a, __dmul_rn(2.0, b)), c);
     return fabs(num) / den;
 }
-__global__ void k_sensor(const DevParams P, const double* Q, double* phi) {
+// EXACT: every cell's phi bit for bit as the oracle's (f3d_debug_sensor). Otherwise the
+// sensor feeds only the branch of each face, i.e. comparisons of the largest phi of six cells
+// with the thresholds phi1 < phi2 < phi3: phi is first formed in FP32 from the FP32-rounded
+// pressures, and kept (widened exactly) when it lies more than a margin of 1e-5 max(1, t)
+// from every threshold t and all seven pressures are positive; otherwise the FP64 value is
+// computed as above. With positive pressures each of the three terms lies in [0, 1] and its
+// FP32 evaluation is within 1e-6 of the exact value (pressure rounding 2^-24 relative, five
+// FP32 roundings), so a kept value is on the same side of every threshold as the FP64 value:
+// the branch map is the FP64 sensor's, with three FP64 divisions saved at almost every cell.
+template <bool EXACT> __global__ void k_sensor(const DevParams P, const double* Q, double* phi) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
     int i, j, k;
@@ -270,14 +279,29 @@ __global__ void k_sensor(const DevParams P, const double* Q, double* phi) {
     if (i < 1 || i > P.nxt - 2 || j < 1 || j > P.nyt - 2 || k < 1 || k > P.nzt - 2) return;
     const double* p = Q + 4 * P.plane;
     const long long sy = P.nxt, sz = (long long)P.nxt * P.nyt;
-    const double pc = p[c];
-    double fx = sensor_term(p[c - 1], pc, p[c + 1]);
-    double fy = sensor_term(p[c - sy], pc, p[c + sy]);
-    double fz = sensor_term(p[c - sz], pc, p[c + sz]);
+    const double pc = p[c], pxm = p[c - 1], pxp = p[c + 1], pym = p[c - sy], pyp = p[c + sy], pzm = p[c - sz],
+                 pzp = p[c + sz];
+    if (!EXACT) {
+        const float b = f64_to_f32_rn(pc), xm = f64_to_f32_rn(pxm), xp = f64_to_f32_rn(pxp), ym = f64_to_f32_rn(pym),
+                    yp = f64_to_f32_rn(pyp), zm = f64_to_f32_rn(pzm), zp = f64_to_f32_rn(pzp);
+        const bool positive = b > 0.f && xm > 0.f && xp > 0.f && ym > 0.f && yp > 0.f && zm > 0.f && zp > 0.f;
+        auto term = [](float a, float bb, float d) { return fabsf(-a + 2.f * bb - d) / (a + 2.f * bb + d); };
+        const float f = term(xm, b, xp) + term(ym, b, yp) + term(zm, b, zp);
+        const Cst<float>& K = P.cf;
+        auto clear = [&](float t) { return fabsf(f - t) > 1e-5f * fmaxf(1.f, t); };
+        if (positive && clear(K.phi1) && clear(K.phi2) && clear(K.phi3)) {
+            phi[c] = f32_to_f64(f);
+            return;
+        }
+    }
+    double fx = sensor_term(pxm, pc, pxp);
+    double fy = sensor_term(pym, pc, pyp);
+    double fz = sensor_term(pzm, pc, pzp);
     phi[c] = __dadd_rn(__dadd_rn(fx, fy), fz);
 }
-cudaError_t launch_sensor(const DevParams& P, const double* Q, double* phi, cudaStream_t st) {
-    k_sensor<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, Q, phi);
+cudaError_t launch_sensor(const DevParams& P, const double* Q, double* phi, cudaStream_t st, bool exact) {
+    if (exact) k_sensor<true><<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, Q, phi);
+    else k_sensor<false><<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, Q, phi);
     return cudaGetLastError();
 }
 

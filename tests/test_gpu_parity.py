@@ -160,6 +160,27 @@ def test_sensor_bitwise(gpu_lib):
     c.close()
 
 
+def test_branch_map_with_thresholds_on_cell_values(gpu_lib):
+    """The stage and RHS paths form the sensor in FP32 and fall back to FP64 only near the
+    thresholds; with thresholds placed one ulp beside the sensor values of chosen cells (so
+    those cells' branches hinge on the last bit of phi), the RHS must still equal the
+    oracle's: a single face taking another branch would move it by ~1e-3."""
+    c0 = random_case(seed=61, spikes=30)
+    phi = orc.sensor(c0.P, c0.Q)
+    vals = np.sort(phi[NG:-NG, NG:-NG, NG:-NG].ravel())
+    picks = [vals[len(vals) // 5], vals[len(vals) // 2], vals[(9 * len(vals)) // 10]]
+    th = [float(np.nextafter(picks[0], np.inf)), float(picks[1]), float(np.nextafter(picks[2], -np.inf))]
+    c0.close()
+    c = random_case(seed=61, spikes=30, phi1=th[0], phi2=th[1], phi3=th[2])
+    r = host(c.s.rhs(dev(c.Q)))
+    _, br = orc.face_flux(c.P, 0, orc.sensor(c.P, c.Q), orc.metric_norm(c.P, *c.m[0:3]),
+                          *orc.split(c.P, c.Q, *c.m[0:3], orc.metric_norm(c.P, *c.m[0:3])), c.Q, *c.m[0:3],
+                          with_branch=True)
+    assert (np.bincount(br.ravel(), minlength=4) > 0).all()
+    assert_rhs_parity(rhs_parity(c.P, c.Q, c.m, c.J, r), strict=True)
+    c.close()
+
+
 # ---------------------------------------------------------------------------------- stages
 @pytest.mark.parametrize("split", ["SW", "LF", "VL", "AUSM"])
 def test_split_parity(gpu_lib, split):
