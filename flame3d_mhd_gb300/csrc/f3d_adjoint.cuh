@@ -396,46 +396,58 @@ __device__ __constant__ const double kW7Q[4][4] = {{-3, 13, -23, 25}, {1, -5, 13
 
 __device__ __forceinline__ void weno7_vjp(const double V[7], double s0, double fb, double Vb[7],
                                           double* s0b = nullptr, double* fval = nullptr) {
-    const double d[4] = {1.0, 12.0, 18.0, 4.0};
-    double q[4], t[4], IS[4];
+    // smoothness indicators in the difference form of weno7_is (f3d_flux.cuh):
+    // IS_k = D1 y1^2 + D2 y2^2 + D3 d3^2, y1 = d1 + a d2 + b d3, y2 = d2 + c d3, d_j the first
+    // differences of sub-stencil k; equal to the reference's quadratic form (schemes.jl:160-175)
+    using C = W7Ldl<double>;
+    const double dk[4] = {1.0, 12.0, 18.0, 4.0};
+    double q[4], t[4], IS[4], y1[4], y2[4], d3[4];
+#pragma unroll
     for (int k = 0; k < 4; k++) {
-        double is = 0, qq = 0;
-        for (int i = 0; i < 4; i++) {
-            qq += kW7Q[k][i] * V[k + i];
-            for (int j = i; j < 4; j++) is += kW7IS[k][i][j] * V[k + i] * V[k + j];
-        }
+        double qq = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) qq += kW7Q[k][i] * V[k + i];
         q[k] = qq;
-        IS[k] = is;
-        t[k] = 1e-20 + is * s0;
+        const double e1 = V[k + 1] - V[k], e2 = V[k + 2] - V[k + 1], e3 = V[k + 3] - V[k + 2];
+        y1[k] = e1 + C::a(k) * e2 + C::b(k) * e3;
+        y2[k] = e2 + C::c(k) * e3;
+        d3[k] = e3;
+        IS[k] = C::D1(k) * (y1[k] * y1[k]) + C::D2(k) * (y2[k] * y2[k]) + C::D3(k) * (e3 * e3);
+        t[k] = 1e-20 + IS[k] * s0;
     }
     // two FP64 divisions: 1/t_k from 1/(t1 t2 t3 t4), and 1/sum alpha
     const double t01 = t[0] * t[1], t23 = t[2] * t[3], rall = 1.0 / (t01 * t23);
     const double it[4] = {t[1] * t23 * rall, t[0] * t23 * rall, t01 * t[3] * rall, t01 * t[2] * rall};
     double al[4], sum = 0;
+#pragma unroll
     for (int k = 0; k < 4; k++) {
-        al[k] = d[k] * it[k] * it[k];
+        al[k] = dk[k] * it[k] * it[k];
         sum += al[k];
     }
     const double rs = 1.0 / sum;
     double f = 0;
+#pragma unroll
     for (int k = 0; k < 4; k++) f += al[k] * rs * q[k];
     if (fval) *fval = f;  // the forward value (12x the reconstruction)
+#pragma unroll
     for (int j = 0; j < 7; j++) Vb[j] = 0.0;
+#pragma unroll
     for (int k = 0; k < 4; k++) {
         const double wk = al[k] * rs;
         const double qb = fb * wk;
         const double tb = -2.0 * fb * (q[k] - f) * wk * it[k];
         const double ISb = s0 * tb;
         if (s0b) *s0b += IS[k] * tb;
-        for (int i = 0; i < 4; i++) {
-            Vb[k + i] += kW7Q[k][i] * qb;
-            double g = 0;  // dIS/dV_{k+i}
-            for (int j = 0; j < 4; j++) {
-                if (j >= i) g += kW7IS[k][i][j] * V[k + j];
-                if (j <= i) g += kW7IS[k][j][i] * V[k + j];
-            }
-            Vb[k + i] += g * ISb;
-        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) Vb[k + i] += kW7Q[k][i] * qb;
+        // IS_k through y1, y2, d3 back to the differences and the stencil values
+        const double y1b = 2.0 * C::D1(k) * y1[k] * ISb, y2b = 2.0 * C::D2(k) * y2[k] * ISb;
+        const double e3b = 2.0 * C::D3(k) * d3[k] * ISb + C::b(k) * y1b + C::c(k) * y2b;
+        const double e2b = C::a(k) * y1b + y2b, e1b = y1b;
+        Vb[k] -= e1b;
+        Vb[k + 1] += e1b - e2b;
+        Vb[k + 2] += e2b - e3b;
+        Vb[k + 3] += e3b;
     }
 }
 
