@@ -20,17 +20,16 @@
 namespace f3d {
 
 // Tile of TL lines x TC cells; NT threads cover the TL x (TC + 8) stencil positions of
-// phases A and C in whole rounds. About 150 registers a thread: xi 4 x 64 on 96 threads,
-// four blocks per SM; eta / zeta 8 x 64 on 192 threads, two blocks per SM (97 KB of shared
-// memory each). Several blocks per SM overlap one block's barrier waits with the others'
-// work: 2.7% per step VJP over one block of 288 / 384 threads and twice the lines.
+// phases A and C. About 140 registers a thread (component-wise) and 59.5 KB of shared
+// memory a block for 4-line tiles (the split fluxes, their cotangents, the sensor and the UP7
+// face cotangents gathered in Phase C): three blocks per SM.
 #ifndef V_TL0
 #define V_TL0 4
 #define V_NT0 96
-#define V_MB0 4
-#define V_TL12 8
-#define V_NT12 192
-#define V_MB12 2
+#define V_MB0 3
+#define V_TL12 4
+#define V_NT12 96
+#define V_MB12 3
 #endif
 // characteristic-wise reverse sweeps: the reverse of a characteristic WENO face holds more
 // state (its eigenvectors, a side's stencil of one field and its cotangents). Smaller blocks
@@ -55,7 +54,8 @@ template <> struct VTile<2, true> { static constexpr int TL = V_C_TL12, TC = 64,
 
 template <int DIR, bool CHAR> constexpr size_t vjp_smem_bytes() {
     using T = VTile<DIR, CHAR>;
-    return sizeof(double) * (size_t)T::TL * (T::TC + 8) * 21 + sizeof(int) * (2 * (size_t)T::TL * (T::TC + 1) + 4);
+    return sizeof(double) * ((size_t)T::TL * (T::TC + 8) * 21 + 5 * (size_t)T::TL * (T::TC + 1)) +
+           sizeof(int) * (2 * (size_t)T::TL * (T::TC + 1) + 4);
 }
 
 template <int DIR, bool CHAR>
@@ -69,6 +69,12 @@ __global__ void __launch_bounds__(VTile<DIR, CHAR>::NT, VTile<DIR, CHAR>::MINB) 
     double* sFpb = sFm + 5 * TL * NP;
     double* sFmb = sFpb + 5 * TL * NP;
     double* sPhi = sFmb + 5 * TL * NP;
+    // cotangents of the UP7 faces (zero elsewhere): UP7 is linear, so its transpose is applied
+    // as a gather in Phase C (each stencil position sums its seven faces) instead of 70
+    // shared-memory atomics per face
+    double* sG = sPhi + TL * NP;
+    constexpr int NFV = TC + 1;
+    auto gidx = [&](int l, int t) { return DIR == 0 ? l * NFV + t : t * TL + l; };
 
     const int Nd = DIR == 0 ? P.nx : (DIR == 1 ? P.ny : P.nz);
     const int Nl = DIR == 0 ? P.ny : P.nx;
@@ -88,10 +94,11 @@ __global__ void __launch_bounds__(VTile<DIR, CHAR>::NT, VTile<DIR, CHAR>::MINB) 
     auto sidx = [&](int l, int p) { return DIR == 0 ? l * NP + p : p * TL + l; };
     const long long pl = P.plane;
 
-    int* list7 = reinterpret_cast<int*>(sPhi + TL * NP);
+    int* list7 = reinterpret_cast<int*>(sG + 5 * TL * NFV);
     int* list5 = list7 + TL * (TC + 1);
     int* counts = list5 + TL * (TC + 1);
     if (threadIdx.x < 2) counts[threadIdx.x] = 0;
+    for (int it = threadIdx.x; it < 5 * TL * NFV; it += NT) sG[it] = 0.0;
     // Phase A: forward split at positions 0..nc+7 (full index c0 + p); zero the cotangents
     for (int it = threadIdx.x; it < TL * NP; it += NT) {
         int l, p;
@@ -130,6 +137,10 @@ __global__ void __launch_bounds__(VTile<DIR, CHAR>::NT, VTile<DIR, CHAR>::MINB) 
         if (f >= 1) {
             const double j = a.J[cl];
             for (int n = 0; n < 5; n++) Fb[n] -= j * a.Lb[cl + n * pl];
+        }
+        if (br == 0) {  // UP7 (schemes.jl:119-142): the face cotangent, gathered in Phase C
+            for (int n = 0; n < 5; n++) sG[n * TL * NFV + gidx(l, t)] = Fb[n];
+            return;
         }
         const double s0 = (br == 1 || br == 2) ? 2.0 / (a.S[cl] + a.S[cr]) : 0.0;
         double s0b_ = 0.0;
@@ -170,12 +181,7 @@ __global__ void __launch_bounds__(VTile<DIR, CHAR>::NT, VTile<DIR, CHAR>::MINB) 
             const double* vm = sFm + n * TL * NP;
             auto P_ = [&](int pos) { return vp[sidx(l, pos)]; };
             auto M_ = [&](int pos) { return vm[sidx(l, pos)]; };
-            if (br == 0) {  // UP7: Fp at positions t..t+6, Fm at t+7..t+1 (schemes.jl:119-142)
-                for (int k = 0; k < 7; k++) {
-                    atomicAdd(&pb[sidx(l, t + k)], P.cd.lin[k] * g);
-                    atomicAdd(&mb[sidx(l, t + 7 - k)], P.cd.lin[k] * g);
-                }
-            } else if (br == 1) {  // WENO7, (fp + fm)/12
+            if (br == 1) {  // WENO7, (fp + fm)/12
                 double V[7], Vb[7];
                 for (int k = 0; k < 7; k++) V[k] = P_(t + k);
                 weno7_vjp(V, s0, g * (1.0 / 12.0), Vb, s0b);
@@ -269,8 +275,18 @@ __global__ void __launch_bounds__(VTile<DIR, CHAR>::NT, VTile<DIR, CHAR>::MINB) 
         double fpb[5], fmb[5];
         bool any = false;
         for (int n = 0; n < 5; n++) {
-            fpb[n] = sFpb[n * TL * NP + s];
-            fmb[n] = sFmb[n * TL * NP + s];
+            // UP7 faces t = p - k take Fp here with coefficient lin[k], faces t = p - 7 + k
+            // take Fm here with lin[k] (positions t..t+6 and t+7..t+1 of face t)
+            const double* G = sG + n * TL * NFV;
+            double gp = 0.0, gm = 0.0;
+#pragma unroll
+            for (int k = 0; k < 7; k++) {
+                const int tp = p - k, tm = p - 7 + k;
+                if (tp >= 0 && tp < NFV) gp += P.cd.lin[k] * G[gidx(l, tp)];
+                if (tm >= 0 && tm < NFV) gm += P.cd.lin[k] * G[gidx(l, tm)];
+            }
+            fpb[n] = sFpb[n * TL * NP + s] + gp;
+            fmb[n] = sFmb[n * TL * NP + s] + gm;
             any |= fpb[n] != 0.0 || fmb[n] != 0.0;
         }
         if (!any) continue;
