@@ -177,7 +177,6 @@ struct f3d_ctx {
     double* S[3] = {};
     double* Ah[9] = {};
     double* csnd = nullptr;
-    double* spk = nullptr;  // FP64 Steger-Warming: the split's per-cell factors (3 planes)
     double* phi = nullptr;
     double* acc = nullptr;
     double* Fv[3] = {};
@@ -388,8 +387,7 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
             mark(ctx, K_VISCOUS, st);
         }
     } else {
-        // the split's per-cell factors with the sound speed (FP64 Steger-Warming)
-        F3D_CUDA(ctx, launch_sound(P, Q, ctx->csnd, st, P.split == F3D_SPLIT_SW ? ctx->spk : nullptr));
+        F3D_CUDA(ctx, launch_sound(P, Q, ctx->csnd, st));
         mark(ctx, K_SOUND, st);
         if (hybrid) {
             F3D_CUDA(ctx, launch_sensor(P, Q, ctx->phi, st));
@@ -404,7 +402,6 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
     for (int d = 0; d < 3; d++) {
         SweepArgs a = sweep_args(ctx, d, Q, hybrid);
         a.acc = mx ? (void*)ctx->acc32 : (void*)acc;
-        if (!mx && P.split == F3D_SPLIT_SW) a.spk = ctx->spk;  // formed by launch_sound above
         if (d == 0) a.out_mode = OUT_SET;
         else if (d == 1) {
             // mixed: the eta differences go to their own array; the last sweep sums in FP64
@@ -715,8 +712,8 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
     const bool r32 = p->precision == F3D_PREC_REF32;
     size_t total = 256;
     const bool fvm = p->scheme != F3D_SCHEME_FDM;
-    if (!mx) {  // S(3) + A/|A|(9) + sound speed + split factors(3) + phi + acc(5) [+ viscous 12] [+ FVM 12 + 5]
-        total += up(nc * 8) * (3 + 9 + 1 + 3 + 1 + 5 + (fvm ? 17 : 0)) + (p->viscous ? 3 * up(nv * 4 * 8) : 0);
+    if (!mx) {  // S(3) + A/|A|(9) + sound speed + phi + acc(5) [+ viscous 12] [+ FVM 12 + 5]
+        total += up(nc * 8) * (3 + 9 + 1 + 1 + 5 + (fvm ? 17 : 0)) + (p->viscous ? 3 * up(nv * 4 * 8) : 0);
     } else {    // [Q32(6) + A32(9) + J32 + acc32b(5), mixed only] + H32(9) + S32(3) + phi32 + acc32(5) [+ viscous 12]
         total += up(nc * 4) * ((r32 ? 0 : 21) + 9 + 3 + 1 + 5) + (p->viscous ? 3 * up(nv * 4 * 4) : 0);
     }
@@ -735,7 +732,6 @@ int f3d_create(const f3d_params* p, f3d_ctx** out) {
         for (int d = 0; d < 3; d++) { ctx->S[d] = (double*)q; q += b1; }
         for (int n = 0; n < 9; n++) { ctx->Ah[n] = (double*)q; q += b1; }
         ctx->csnd = (double*)q; q += b1;
-        ctx->spk = (double*)q; q += 3 * b1;
         ctx->phi = (double*)q; q += b1;
         ctx->acc = (double*)q; q += 5 * b1;
         if (p->viscous)

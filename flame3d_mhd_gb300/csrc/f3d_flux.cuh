@@ -25,12 +25,9 @@ __device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
 // ss = |A|; c = sound speed (sqrt(gamma Rg T) for SW, split.jl:22; sqrt(gamma p/rho) for
 // LF/VL/AUSM, split.jl:90,130,205). Constant quotients such as 1/(2 gamma) and
 // (3-gamma)/(2(gamma-1)) come precomputed in K instead of being divided per cell.
-// pre (FP64 Steger-Warming only, optional): the cell's direction-independent factors
-// {rho / (2 gamma), (gamma-1)|u|^2, (3-gamma)/(2(gamma-1)) c^2}, formed once per cell by the
-// sound-speed kernel instead of in each of the three sweeps.
 template <class R>
 __device__ __forceinline__ void split_cell(int method, const Cst<R>& K, const R q[6], R c, R A1, R A2, R A3, R Ah1,
-                                           R Ah2, R Ah3, R ss, R fp[5], R fm[5], const R* pre = nullptr) {
+                                           R Ah2, R Ah3, R ss, R fp[5], R fm[5]) {
     const R rho = q[0], u = q[1], v = q[2], w = q[3], p = q[4];
     const R half = R(0.5), one = R(1), two = R(2);
     const R g = K.gamma;
@@ -39,7 +36,7 @@ __device__ __forceinline__ void split_cell(int method, const Cst<R>& K, const R 
         // their sign split (it keeps each sign, -0 included), so no flux component needs its own
         // final multiplication: equal to the reference's expression up to rounding, seven FP64
         // operations fewer per cell.
-        const R t1 = pre ? pre[0] : rho * K.inv_2g;
+        const R t1 = rho * K.inv_2g;
         const R tE1 = t1 * (A1 * u + A2 * v + A3 * w);
         const R tcs = t1 * (c * ss);
         R e1p, e2p, e3p, e1m, e2m, e3m;
@@ -51,8 +48,8 @@ __device__ __forceinline__ void split_cell(int method, const Cst<R>& K, const R 
         const R wc1 = w - c * Ah3, wc2 = w + c * Ah3;
         const R vvc1 = (uc1 * uc1 + vc1 * vc1 + wc1 * wc1) * half;
         const R vvc2 = (uc2 * uc2 + vc2 * vc2 + wc2 * wc2) * half;
-        const R vv = pre ? pre[1] : K.gm1 * (u * u + v * v + w * w);
-        const R W2 = pre ? pre[2] : K.w2c * (c * c);
+        const R vv = K.gm1 * (u * u + v * v + w * w);
+        const R W2 = K.w2c * (c * c);
         const R a1 = K.two_gm1 * e1p, b1 = K.two_gm1 * e1m;
         fp[0] = a1 + e2p + e3p;
         fp[1] = a1 * u + e2p * uc1 + e3p * uc2;

@@ -16,7 +16,6 @@ struct SweepArgs {
     DevParams P;
     const void* Q;        // primitive state (Nt^3 x 6), ghost-filled
     const void* csnd;     // FP64 form: sound speed per cell for the split
-    const double* spk;    // FP64 Steger-Warming: the split's per-cell factors (3 planes) or null
     const void* A[3];     // metric row of the sweep direction (J^-1 scaled)
     const void* Ah[3];    // A * (1/|A|)
     const void* S;        // |A|
@@ -148,8 +147,7 @@ cudaError_t launch_metric_prep32(const DevParams& P, const MetricPtrs& m, const 
 cudaError_t launch_c2prim_interior(const DevParams& P, const double* U, double* Q, cudaStream_t st);
 cudaError_t launch_prim2c(const DevParams& P, const double* Q, double* U, cudaStream_t st);
 cudaError_t launch_lincomb(const DevParams& P, double* U, const double* Un, double a, double b, cudaStream_t st);
-// spk (optional, FP64 Steger-Warming): also the split's per-cell factors (3 planes)
-cudaError_t launch_sound(const DevParams& P, const double* Q, double* csnd, cudaStream_t st, double* spk = nullptr);
+cudaError_t launch_sound(const DevParams& P, const double* Q, double* csnd, cudaStream_t st);
 // exact: phi bit for bit as the oracle's; otherwise values that give the same branch map
 // (FP32 away from the thresholds, FP64 near them)
 cudaError_t launch_sensor(const DevParams& P, const double* Q, double* phi, cudaStream_t st, bool exact = false);

@@ -242,26 +242,16 @@ cudaError_t launch_lincomb(const DevParams& P, double* U, const double* Un, doub
     return cudaGetLastError();
 }
 
-// The split's sound speed per cell and, when spk is given (FP64 Steger-Warming), the split's
-// direction-independent factors rho/(2 gamma), (gamma-1)|u|^2, (3-gamma)/(2(gamma-1)) c^2
-// (three planes of spk), which the three sweeps then read instead of forming them.
-__global__ void k_sound(const DevParams P, const double* Q, double* csnd, double* spk) {
+__global__ void k_sound(const DevParams P, const double* Q, double* csnd) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.plane) return;
     double q[6];
 #pragma unroll
     for (int n = 0; n < 6; n++) q[n] = Q[c + n * P.plane];
-    const double cs = sound_speed(P, q);
-    csnd[c] = cs;
-    if (spk) {
-        const Cst<double>& K = P.cd;
-        spk[c] = q[0] * K.inv_2g;
-        spk[c + P.plane] = K.gm1 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-        spk[c + 2 * P.plane] = K.w2c * (cs * cs);
-    }
+    csnd[c] = sound_speed(P, q);
 }
-cudaError_t launch_sound(const DevParams& P, const double* Q, double* csnd, cudaStream_t st, double* spk) {
-    k_sound<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, Q, csnd, spk);
+cudaError_t launch_sound(const DevParams& P, const double* Q, double* csnd, cudaStream_t st) {
+    k_sound<<<pw_blocks(P.plane), PW_THREADS, 0, st>>>(P, Q, csnd);
     return cudaGetLastError();
 }
 

@@ -105,12 +105,8 @@ __global__ void __launch_bounds__(Tile<DIR, R>::NT, Tile<DIR, R>::MINB) k_sweep(
 #pragma unroll
         for (int n = 0; n < 6; n++) q[n] = Qr[c + n * pl];
         R fp[5], fm[5];
-        R pre[3];
-        const bool have_pre = sizeof(R) == 8 && a.spk;
-        if (have_pre)
-            for (int k = 0; k < 3; k++) pre[k] = (R)a.spk[c + k * pl];
         split_cell<R>(P.split, cst<R>(P), q, split_sound<R>(P, a, c, q), Ar[0][c], Ar[1][c], Ar[2][c], Hr[0][c],
-                      Hr[1][c], Hr[2][c], Sr[c], fp, fm, have_pre ? pre : nullptr);
+                      Hr[1][c], Hr[2][c], Sr[c], fp, fm);
         const int s = sidx(l, p);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
