@@ -20,21 +20,25 @@
 namespace f3d {
 
 // Tile (lines TL x cells TC), threads and resident blocks per SM of a sweep, by type.
-// FP64: 8 x 64 (xi) and 16 x 32 (eta, zeta) on 256 threads, two blocks per SM (~75 KB of
-// shared memory each); half-height tiles on 128 threads, four per SM, timed 3% slower per
-// RK3 step on the 256x64x64 shock tube (quarter tiles on 64 threads slower still). FP32:
+// FP64: 8 x 64 in every direction on 288 threads, two blocks per SM (~76 KB of shared memory
+// each): the tile's 8 x 72 split positions take exactly two rounds of 288 threads. Against
+// 256 threads on 8 x 64 (xi) and 16 x 32 (eta, zeta) tiles, whose 576 / 640 positions took
+// 2.25 / 2.5 rounds: +0.7% per RK3 step on the 256x64x64 shock tube (same box, three rounds
+// of alternating builds), though two blocks of nine warps leave 96 registers a thread (five
+// warps on one of the SM's four register-file quarters) and the characteristic-wise
+// instantiations spill 112-144 bytes (74-90 registers and no spills component-wise). FP32:
 // half-height tiles on 128 threads, six blocks per SM (~20 KB each): the same step time as
 // three 256-thread blocks on that tube, 6% less per RHS on the component-wise tube and on
 // the viscous vortex.
 #ifndef SW_D_THREADS
-#define SW_D_THREADS 256
+#define SW_D_THREADS 288
 #define SW_D_BLOCKS 2
 #define SW_D_TL0 8
-#define SW_D_TL12 16
+#define SW_D_TL12 8
 #endif
 #ifndef SW_D_TC0
 #define SW_D_TC0 64
-#define SW_D_TC12 32
+#define SW_D_TC12 64
 #endif
 template <int DIR, class R> struct Tile;
 #ifndef SW_F_THREADS
