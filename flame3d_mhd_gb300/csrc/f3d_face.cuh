@@ -7,6 +7,139 @@
 
 namespace f3d {
 
+// ---- Characteristic-wise reconstruction, schemes.jl:756-999, in three parts: the face's basis,
+// one field's characteristic flux, one component of the face flux. The face's eigenvectors
+// come from the arithmetic mean of u, v, w, T and of the metric row at the two adjacent cells
+// (cl, cr linear indices), read from global memory. Rows of L and of R are selected by a
+// runtime index, and the field loop is not unrolled: one copy of the WENO code serves the
+// five fields (the FP64 characteristic sweeps hold 96 registers with no spills this way).
+// Spreading a face over five lanes, one field each, with the fluxes exchanged by shuffles
+// ran 7.5% slower per RK3 step on the 256x64x64 shock tube than one thread per face: the
+// five copies of the basis cost more than the idle lanes of a short WENO queue.
+template <class R> struct CharBasis {
+    R u, v, w, c, q2, H, qn, ql, qm, nx, ny, nz, lx, ly, lz, mx, my, mz, c2, K2, Kc;
+};
+
+template <class R>
+__device__ __forceinline__ void char_basis(const DevParams& P, const SweepArgs& a, R s0, long long cl, long long cr,
+                                           CharBasis<R>& b) {
+    const Cst<R>& K = cst<R>(P);
+    const long long pl = P.plane;
+    const R* Qr = static_cast<const R*>(a.Q);
+    const R* A0 = static_cast<const R*>(a.A[0]);
+    const R* A1p = static_cast<const R*>(a.A[1]);
+    const R* A2p = static_cast<const R*>(a.A[2]);
+    const R u = R(0.5) * (Qr[cr + pl] + Qr[cl + pl]);
+    const R v = R(0.5) * (Qr[cr + 2 * pl] + Qr[cl + 2 * pl]);
+    const R w = R(0.5) * (Qr[cr + 3 * pl] + Qr[cl + 3 * pl]);
+    const R T = R(0.5) * (Qr[cr + 5 * pl] + Qr[cl + 5 * pl]);
+    const R A1 = (A0[cr] + A0[cl]) * R(0.5);
+    const R A2 = (A1p[cr] + A1p[cl]) * R(0.5);
+    const R A3 = (A2p[cr] + A2p[cl]) * R(0.5);
+    const R nx = A1 * s0, ny = A2 * s0, nz = A3 * s0;
+    R lx, ly, lz;
+    if (fabs(nz) <= fabs(ny)) {
+        R ss = rsq(nx * nx + ny * ny);
+        lx = -ny * ss;
+        ly = nx * ss;
+        lz = R(0);
+    } else {
+        R ss = rsq(nx * nx + nz * nz);
+        lx = -nz * ss;
+        ly = R(0);
+        lz = nx * ss;
+    }
+    const R mx = ny * lz - nz * ly, my = nz * lx - nx * lz, mz = nx * ly - ny * lx;
+    b.u = u; b.v = v; b.w = w;
+    b.nx = nx; b.ny = ny; b.nz = nz;
+    b.lx = lx; b.ly = ly; b.lz = lz;
+    b.mx = mx; b.my = my; b.mz = mz;
+    b.qn = u * nx + v * ny + w * nz;
+    b.ql = u * lx + v * ly + w * lz;
+    b.qm = u * mx + v * my + w * mz;
+    b.q2 = R(0.5) * (u * u + v * v + w * w);
+    const R gT = K.grg * T;
+    const R rc = rsq(gT);                // 1/c
+    b.c = gT * rc;                       // c = sqrt(gamma Rg T)
+    b.c2 = R(0.5) * rc;                  // 1/(2c)
+    b.Kc = K.gm1 * (rc * rc);            // (gamma-1)/c^2
+    b.K2 = b.Kc * R(0.5);
+    b.H = gT * K.inv_gm1 + b.q2;         // 1/K + q2
+}
+
+// Row n of the left eigenvectors L (schemes.jl:800-830), written for a runtime n as
+// alpha_n (q2, -u, -v, -w, 1) + beta_n t_n + (n == 1) e_0 with t_n = (qn, -n) for the
+// acoustic rows 0 and 2 (beta = +-1/(2c), alpha = K2), (-ql, l) and (-qm, m) for the shear
+// rows 3 and 4 (beta = 1, alpha = 0), and alpha = -Kc, beta = 0 for the entropy row 1.
+template <class R>
+__device__ __forceinline__ void char_left_row(const CharBasis<R>& b, int n, R l[5]) {
+    const R al = n == 0 || n == 2 ? b.K2 : n == 1 ? -b.Kc : R(0);
+    const R be = n == 0 ? b.c2 : n == 2 ? -b.c2 : n == 1 ? R(0) : R(1);
+    const R t0 = n <= 2 ? b.qn : n == 3 ? -b.ql : -b.qm;
+    const R t1 = n <= 2 ? -b.nx : n == 3 ? b.lx : b.mx;
+    const R t2 = n <= 2 ? -b.ny : n == 3 ? b.ly : b.my;
+    const R t3 = n <= 2 ? -b.nz : n == 3 ? b.lz : b.mz;
+    l[0] = al * b.q2 + be * t0 + (n == 1 ? R(1) : R(0));
+    l[1] = be * t1 - al * b.u;
+    l[2] = be * t2 - al * b.v;
+    l[3] = be * t3 - al * b.w;
+    l[4] = al;
+}
+
+// The characteristic flux of field n at the face: the field's projection L_n F of the stencil's
+// split fluxes, reconstructed by WENO7 (br 1) or WENO5 (br 2) on each side.
+template <class R, class FPA, class FMA>
+__device__ __forceinline__ R char_field_flux(const DevParams& P, const CharBasis<R>& b, int n, int br, int p0, R s0,
+                                             FPA FP, FMA FM) {
+    const R tmp1 = R(1) / R(12), tmp2 = R(1) / R(6);
+    R l[5];
+    char_left_row<R>(b, n, l);
+    auto projP = [&](int pos) {
+        return FP(0, pos) * l[0] + FP(1, pos) * l[1] + FP(2, pos) * l[2] + FP(3, pos) * l[3] + FP(4, pos) * l[4];
+    };
+    auto projM = [&](int pos) {
+        return FM(0, pos) * l[0] + FM(1, pos) * l[1] + FM(2, pos) * l[2] + FM(3, pos) * l[3] + FM(4, pos) * l[4];
+    };
+    if constexpr (sizeof(R) == 4) {
+        if (P.ref32) {  // the reference's Float32 reconstruction of the characteristic fields
+            if (br == 1) {
+                const double fp = weno7_ref32(projP(p0), projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4),
+                                              projP(p0 + 5), projP(p0 + 6), s0);
+                const double fm = weno7_ref32(projM(p0 + 7), projM(p0 + 6), projM(p0 + 5), projM(p0 + 4),
+                                              projM(p0 + 3), projM(p0 + 2), projM(p0 + 1), s0);
+                return (float)((fp + fm) * (double)tmp1);
+            }
+            return (weno5_ref32(projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5), s0) +
+                    weno5_ref32(projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3), projM(p0 + 2), s0)) *
+                   tmp2;
+        }
+    }
+    if (br == 1) {
+        R fp = weno7(projP(p0), projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5),
+                     projP(p0 + 6), s0);
+        R fm = weno7(projM(p0 + 7), projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3), projM(p0 + 2),
+                     projM(p0 + 1), s0);
+        return (fp + fm) * tmp1;
+    }
+    R fp = weno5(projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5), s0);
+    R fm = weno5(projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3), projM(p0 + 2), s0);
+    return (fp + fm) * tmp2;
+}
+
+// Component k of the face flux R f from the five characteristic fluxes (schemes.jl:960-999):
+// f0 (a - c n) + f1 a' + f2 (a + c n) + f3 l + f4 m with (a, a', n, l, m) the k-th entries of
+// (1, u, v, w, H), (1, u, v, w, q2), (0, nx, ny, nz, qn), (0, lx, ly, lz, ql), (0, mx, my, mz, qm).
+template <class R>
+__device__ __forceinline__ R char_right_row(const CharBasis<R>& b, int k, const R f[5]) {
+    if (k == 0) return f[0] + f[1] + f[2];
+    const R ak = k == 1 ? b.u : k == 2 ? b.v : k == 3 ? b.w : b.H;
+    const R ap = k == 4 ? b.q2 : ak;
+    const R nk = k == 1 ? b.nx : k == 2 ? b.ny : k == 3 ? b.nz : b.qn;
+    const R lk = k == 1 ? b.lx : k == 2 ? b.ly : k == 3 ? b.lz : b.ql;
+    const R mk = k == 1 ? b.mx : k == 2 ? b.my : k == 3 ? b.mz : b.qm;
+    return f[0] * (ak - b.c * nk) + f[1] * ap + f[2] * (ak + b.c * nk) + f[3] * lk + f[4] * mk;
+}
+
 // Face flux of one face from the split fluxes of the 8 cells around it, positions
 // p0..p0+7 of the line (face between positions p0+3 and p0+4). FP/FM(n, pos) read shared
 // memory. For characteristic mode the face state comes from global memory at the two
@@ -81,95 +214,14 @@ __device__ __forceinline__ void face_flux(const DevParams& P, const SweepArgs& a
         }
         return;
     }
-    // characteristic-wise, schemes.jl:756-999: eigenvectors of the face from the arithmetic
-    // mean of u,v,w,T and of the metric row at the two adjacent cells.
-    const long long pl = P.plane;
-    const R* Qr = static_cast<const R*>(a.Q);
-    const R* A0 = static_cast<const R*>(a.A[0]);
-    const R* A1p = static_cast<const R*>(a.A[1]);
-    const R* A2p = static_cast<const R*>(a.A[2]);
-    const R u = R(0.5) * (Qr[cr + pl] + Qr[cl + pl]);
-    const R v = R(0.5) * (Qr[cr + 2 * pl] + Qr[cl + 2 * pl]);
-    const R w = R(0.5) * (Qr[cr + 3 * pl] + Qr[cl + 3 * pl]);
-    const R T = R(0.5) * (Qr[cr + 5 * pl] + Qr[cl + 5 * pl]);
-    const R A1 = (A0[cr] + A0[cl]) * R(0.5);
-    const R A2 = (A1p[cr] + A1p[cl]) * R(0.5);
-    const R A3 = (A2p[cr] + A2p[cl]) * R(0.5);
-    const R nx = A1 * s0, ny = A2 * s0, nz = A3 * s0;
-    R lx, ly, lz;
-    if (fabs(nz) <= fabs(ny)) {
-        R ss = rsq(nx * nx + ny * ny);
-        lx = -ny * ss;
-        ly = nx * ss;
-        lz = R(0);
-    } else {
-        R ss = rsq(nx * nx + nz * nz);
-        lx = -nz * ss;
-        ly = R(0);
-        lz = nx * ss;
-    }
-    const R mx = ny * lz - nz * ly, my = nz * lx - nx * lz, mz = nx * ly - ny * lx;
-    const R qn = u * nx + v * ny + w * nz;
-    const R ql = u * lx + v * ly + w * lz;
-    const R qm = u * mx + v * my + w * mz;
-    const R q2 = R(0.5) * (u * u + v * v + w * w);
-    const R gT = K.grg * T;
-    const R rc = rsq(gT);              // 1/c
-    const R c = gT * rc;               // c = sqrt(gamma Rg T)
-    const R c2 = R(0.5) * rc;          // 1/(2c)
-    const R Kc = K.gm1 * (rc * rc);    // (gamma-1)/c^2
-    const R K2 = Kc * R(0.5);
-    const R H = gT * K.inv_gm1 + q2;   // 1/K + q2
+    // characteristic-wise, schemes.jl:756-999
+    CharBasis<R> cb;
+    char_basis<R>(P, a, s0, cl, cr, cb);
     R flux[5];
 #pragma unroll 1
-    for (int n = 0; n < 5; n++) {
-        R l0, l1, l2, l3, l4;  // row n of L
-        if (n == 0) { l0 = K2 * q2 + qn * c2; l1 = -(K2 * u + nx * c2); l2 = -(K2 * v + ny * c2); l3 = -(K2 * w + nz * c2); l4 = K2; }
-        else if (n == 1) { l0 = R(1) - Kc * q2; l1 = Kc * u; l2 = Kc * v; l3 = Kc * w; l4 = -Kc; }
-        else if (n == 2) { l0 = K2 * q2 - qn * c2; l1 = -(K2 * u - nx * c2); l2 = -(K2 * v - ny * c2); l3 = -(K2 * w - nz * c2); l4 = K2; }
-        else if (n == 3) { l0 = -ql; l1 = lx; l2 = ly; l3 = lz; l4 = R(0); }
-        else { l0 = -qm; l1 = mx; l2 = my; l3 = mz; l4 = R(0); }
-        auto projP = [&](int pos) {
-            return FP(0, pos) * l0 + FP(1, pos) * l1 + FP(2, pos) * l2 + FP(3, pos) * l3 + FP(4, pos) * l4;
-        };
-        auto projM = [&](int pos) {
-            return FM(0, pos) * l0 + FM(1, pos) * l1 + FM(2, pos) * l2 + FM(3, pos) * l3 + FM(4, pos) * l4;
-        };
-        if constexpr (sizeof(R) == 4) {
-            if (P.ref32) {  // the reference's Float32 reconstruction of the characteristic fields
-                if (br == 1) {
-                    const double fp = weno7_ref32(projP(p0), projP(p0 + 1), projP(p0 + 2), projP(p0 + 3),
-                                                  projP(p0 + 4), projP(p0 + 5), projP(p0 + 6), s0);
-                    const double fm = weno7_ref32(projM(p0 + 7), projM(p0 + 6), projM(p0 + 5), projM(p0 + 4),
-                                                  projM(p0 + 3), projM(p0 + 2), projM(p0 + 1), s0);
-                    flux[n] = (float)((fp + fm) * (double)tmp1);
-                } else {
-                    flux[n] = (weno5_ref32(projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4),
-                                           projP(p0 + 5), s0) +
-                               weno5_ref32(projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3),
-                                           projM(p0 + 2), s0)) *
-                              tmp2;
-                }
-                continue;
-            }
-        }
-        if (br == 1) {
-            R fp = weno7(projP(p0), projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5),
-                         projP(p0 + 6), s0);
-            R fm = weno7(projM(p0 + 7), projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3), projM(p0 + 2),
-                         projM(p0 + 1), s0);
-            flux[n] = (fp + fm) * tmp1;
-        } else {
-            R fp = weno5(projP(p0 + 1), projP(p0 + 2), projP(p0 + 3), projP(p0 + 4), projP(p0 + 5), s0);
-            R fm = weno5(projM(p0 + 6), projM(p0 + 5), projM(p0 + 4), projM(p0 + 3), projM(p0 + 2), s0);
-            flux[n] = (fp + fm) * tmp2;
-        }
-    }
-    out[0] = flux[0] + flux[1] + flux[2];
-    out[1] = flux[0] * (u - c * nx) + flux[1] * u + flux[2] * (u + c * nx) + flux[3] * lx + flux[4] * mx;
-    out[2] = flux[0] * (v - c * ny) + flux[1] * v + flux[2] * (v + c * ny) + flux[3] * ly + flux[4] * my;
-    out[3] = flux[0] * (w - c * nz) + flux[1] * w + flux[2] * (w + c * nz) + flux[3] * lz + flux[4] * mz;
-    out[4] = flux[0] * (H - qn * c) + flux[1] * q2 + flux[2] * (H + qn * c) + flux[3] * ql + flux[4] * qm;
+    for (int n = 0; n < 5; n++) flux[n] = char_field_flux<R>(P, cb, n, br, p0, s0, FP, FM);
+#pragma unroll
+    for (int k = 0; k < 5; k++) out[k] = char_right_row<R>(cb, k, flux);
 }
 
 // Sound speed for the split: precomputed per cell in FP64; computed in place in FP32.

@@ -24,9 +24,9 @@ namespace f3d {
 // each): the tile's 8 x 72 split positions take exactly two rounds of 288 threads. Against
 // 256 threads on 8 x 64 (xi) and 16 x 32 (eta, zeta) tiles, whose 576 / 640 positions took
 // 2.25 / 2.5 rounds: +0.7% per RK3 step on the 256x64x64 shock tube (same box, three rounds
-// of alternating builds), though two blocks of nine warps leave 96 registers a thread (five
-// warps on one of the SM's four register-file quarters) and the characteristic-wise
-// instantiations spill 112-144 bytes (74-90 registers and no spills component-wise). FP32:
+// of alternating builds); two blocks of nine warps leave 96 registers a thread (five warps on
+// one of the SM's four register-file quarters), which the characteristic-wise instantiations
+// use without spilling (72-92 component-wise). FP32:
 // half-height tiles on 128 threads, six blocks per SM (~20 KB each): the same step time as
 // three 256-thread blocks on that tube, 6% less per RHS on the component-wise tube and on
 // the viscous vortex.
