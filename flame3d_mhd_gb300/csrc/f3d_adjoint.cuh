@@ -41,85 +41,89 @@ __device__ __forceinline__ void c2prim_vjp(const DevParams& P, const double U[5]
 // q = (rho,u,v,w,p,T); c = the split's sound speed; fpb/fmb cotangents of Fp/Fm.
 // Accumulates into qb[6] (the sound-speed dependence goes to T for SW, to p and rho for LF).
 // mg (optional): cotangents of the metric inputs, {A1, A2, A3, H1, H2, H3, |A|} += .
+// Steger-Warming: the reverse of split_cell's FP64 form (the same function of q, c and the
+// metric row as split.jl:2-68): E1 = |A| (Ah.u), the eigenvalues scaled by t1 = rho/(2 gamma)
+// and routed by their sign pattern, the eigenvectors' velocities u -+ c Ah and enthalpies
+// H -+ c Un. The metric enters only through Ah and |A| (A's own cotangent stays 0; the caller
+// folds Ah and |A| back onto A).
 __device__ __forceinline__ void split_sw_vjp(const Cst<double>& K, const double q[6], double c, double A1, double A2,
                                              double A3, double H1, double H2, double H3, double ss,
                                              const double fpb[5], const double fmb[5], double qb[6],
                                              double* mg = nullptr) {
+    (void)A1; (void)A2; (void)A3;
     const double rho = q[0], u = q[1], v = q[2], w = q[3];
-    const double E1 = A1 * u + A2 * v + A3 * w;
-    const double E[3] = {E1, E1 - c * ss, E1 + c * ss};
-    double EP[3], EM[3];
-    for (int k = 0; k < 3; k++) sign_split(E[k], EP[k], EM[k]);
-    const double uc[2] = {u - c * H1, u + c * H1}, vc[2] = {v - c * H2, v + c * H2}, wc[2] = {w - c * H3, w + c * H3};
-    const double vvc[2] = {0.5 * (uc[0] * uc[0] + vc[0] * vc[0] + wc[0] * wc[0]),
-                           0.5 * (uc[1] * uc[1] + vc[1] * vc[1] + wc[1] * wc[1])};
-    const double vv = K.gm1 * (u * u + v * v + w * w);
-    const double W2 = K.w2c * c * c;
-    const double t1 = rho * K.inv_2g, t2 = K.two_gm1;
-    double t1b = 0, ub = 0, vb = 0, wb = 0, cb = 0, vvb = 0, W2b = 0;
-    double Eb[3] = {0, 0, 0};
-    double ucb[2] = {0, 0}, vcb[2] = {0, 0}, wcb[2] = {0, 0}, vvcb[2] = {0, 0};
-    for (int side = 0; side < 2; side++) {
-        const double* g = side == 0 ? fpb : fmb;
-        const double* e = side == 0 ? EP : EM;
-        // brackets B_n with f_n = t1 * B_n
-        const double B0 = t2 * e[0] + e[1] + e[2];
-        const double B1 = t2 * e[0] * u + e[1] * uc[0] + e[2] * uc[1];
-        const double B2 = t2 * e[0] * v + e[1] * vc[0] + e[2] * vc[1];
-        const double B3 = t2 * e[0] * w + e[1] * wc[0] + e[2] * wc[1];
-        const double B4 = e[0] * vv + e[1] * vvc[0] + e[2] * vvc[1] + W2 * (e[1] + e[2]);
-        t1b += g[0] * B0 + g[1] * B1 + g[2] * B2 + g[3] * B3 + g[4] * B4;
-        const double b0 = t1 * g[0], b1 = t1 * g[1], b2 = t1 * g[2], b3 = t1 * g[3], b4 = t1 * g[4];
-        double eb0 = t2 * (b0 + u * b1 + v * b2 + w * b3) + vv * b4;
-        double eb1 = b0 + uc[0] * b1 + vc[0] * b2 + wc[0] * b3 + (vvc[0] + W2) * b4;
-        double eb2 = b0 + uc[1] * b1 + vc[1] * b2 + wc[1] * b3 + (vvc[1] + W2) * b4;
-        ub += t2 * e[0] * b1;
-        vb += t2 * e[0] * b2;
-        wb += t2 * e[0] * b3;
-        ucb[0] += e[1] * b1; ucb[1] += e[2] * b1;
-        vcb[0] += e[1] * b2; vcb[1] += e[2] * b2;
-        wcb[0] += e[1] * b3; wcb[1] += e[2] * b3;
-        vvb += e[0] * b4;
-        vvcb[0] += e[1] * b4;
-        vvcb[1] += e[2] * b4;
-        W2b += (e[1] + e[2]) * b4;
-        // E+ = max(E,0), E- = min(E,0): each passes its cotangent to E on its own side
-        const double ebs[3] = {eb0, eb1, eb2};
-        for (int k = 0; k < 3; k++) {
-            const bool pos = __double2hiint(E[k]) >= 0;
-            Eb[k] += (side == 0) == pos ? ebs[k] : 0.0;
-        }
+    const double tss = (rho * ss) * K.inv_2g;
+    const double Un = H1 * u + H2 * v + H3 * w;
+    const double e1 = tss * Un, tcs = tss * c;
+    const double e2 = e1 - tcs, e3 = e1 + tcs;
+    const double q2 = u * u + v * v + w * w;
+    const double vv = K.gm1 * q2;
+    const double Hh = 0.5 * q2 + (K.inv_gm1 * c) * c;
+    const double cUn = c * Un;
+    const bool e2pos = __double2hiint(e2) >= 0, e3pos = __double2hiint(e3) >= 0;
+    double ub = 0, vb = 0, wb = 0, cb = 0, Hb1 = 0, Hb2 = 0, Hb3 = 0, vvb = 0, Hhb = 0, cUnb = 0;
+    double e1b, e2b, e3b;
+    if (e2pos || !e3pos) {  // f = a1 + e2 + e3, (a1 + e2 + e3) u + c (e3 - e2) Ah, e1 vv + (e2 + e3) H + (e3 - e2) c Un
+        const double* g = e2pos ? fpb : fmb;
+        const double a1 = K.two_gm1 * e1, s23 = e2 + e3, d23 = e3 - e2;
+        const double f0 = a1 + s23, dc = d23 * c;
+        const double f0b = g[0] + g[1] * u + g[2] * v + g[3] * w;
+        const double dcb = g[1] * H1 + g[2] * H2 + g[3] * H3;
+        ub += g[1] * f0; vb += g[2] * f0; wb += g[3] * f0;
+        Hb1 += g[1] * dc; Hb2 += g[2] * dc; Hb3 += g[3] * dc;
+        vvb += g[4] * e1;
+        Hhb += g[4] * s23;
+        cUnb += g[4] * d23;
+        cb += dcb * d23;
+        const double s23b = g[4] * Hh + f0b, d23b = g[4] * cUn + dcb * c;
+        e1b = g[4] * vv + K.two_gm1 * f0b;
+        e2b = s23b - d23b;
+        e3b = s23b + d23b;
+    } else {  // e2 < 0 <= e3: Fp from e3 (and e1 >= 0), Fm from e2 (and e1 < 0)
+        const bool e1pos = __double2hiint(e1) >= 0;
+        const double e1p = e1pos ? e1 : 0.0, e1m = e1pos ? 0.0 : e1;
+        const double fp0 = K.two_gm1 * e1p + e3, e3c = e3 * c;
+        const double fm0 = K.two_gm1 * e1m + e2, e2c = e2 * c;
+        const double* g = fpb;
+        const double* h = fmb;
+        const double fp0b = g[0] + g[1] * u + g[2] * v + g[3] * w;
+        const double fm0b = h[0] + h[1] * u + h[2] * v + h[3] * w;
+        const double e3cb = g[1] * H1 + g[2] * H2 + g[3] * H3;
+        const double e2cb = -(h[1] * H1 + h[2] * H2 + h[3] * H3);
+        ub += g[1] * fp0 + h[1] * fm0;
+        vb += g[2] * fp0 + h[2] * fm0;
+        wb += g[3] * fp0 + h[3] * fm0;
+        Hb1 += g[1] * e3c - h[1] * e2c;
+        Hb2 += g[2] * e3c - h[2] * e2c;
+        Hb3 += g[3] * e3c - h[3] * e2c;
+        vvb += g[4] * e1p + h[4] * e1m;
+        Hhb += g[4] * e3 + h[4] * e2;
+        cUnb += g[4] * e3 - h[4] * e2;
+        cb += e3cb * e3 + e2cb * e2;
+        e3b = fp0b + e3cb * c + g[4] * (Hh + cUn);
+        e2b = fm0b + e2cb * c + h[4] * (Hh - cUn);
+        // e1+ = max(e1, 0), e1- = min(e1, 0): the cotangent of the side e1 lies on
+        e1b = e1pos ? g[4] * vv + K.two_gm1 * fp0b : h[4] * vv + K.two_gm1 * fm0b;
     }
-    double rhob = t1b * K.inv_2g;
-    cb += W2b * K.w2c * 2.0 * c;
-    ub += vvb * K.gm1 * 2.0 * u;
-    vb += vvb * K.gm1 * 2.0 * v;
-    wb += vvb * K.gm1 * 2.0 * w;
-    for (int s = 0; s < 2; s++) {
-        ucb[s] += vvcb[s] * uc[s];
-        vcb[s] += vvcb[s] * vc[s];
-        wcb[s] += vvcb[s] * wc[s];
+    // e2 = e1 - tcs, e3 = e1 + tcs; e1 = tss Un, tcs = tss c; cUn = c Un
+    e1b += e2b + e3b;
+    const double tcsb = e3b - e2b;
+    const double tssb = e1b * Un + tcsb * c;
+    const double Unb = e1b * tss + cUnb * c;
+    cb += tcsb * tss + cUnb * Un;
+    // Hh = q2/2 + c^2/(gamma-1), vv = (gamma-1) q2, q2 = |u|^2, Un = Ah.u
+    const double q2b = 0.5 * Hhb + K.gm1 * vvb;
+    cb += 2.0 * (K.inv_gm1 * c) * Hhb;
+    ub += 2.0 * u * q2b + H1 * Unb;
+    vb += 2.0 * v * q2b + H2 * Unb;
+    wb += 2.0 * w * q2b + H3 * Unb;
+    if (mg) {
+        mg[3] += Hb1 + u * Unb;
+        mg[4] += Hb2 + v * Unb;
+        mg[5] += Hb3 + w * Unb;
+        mg[6] += tssb * rho * K.inv_2g;
     }
-    ub += ucb[0] + ucb[1];
-    vb += vcb[0] + vcb[1];
-    wb += wcb[0] + wcb[1];
-    cb += (ucb[1] - ucb[0]) * H1 + (vcb[1] - vcb[0]) * H2 + (wcb[1] - wcb[0]) * H3;
-    // E2 = E1 - c ss, E3 = E1 + c ss
-    const double E1b = Eb[0] + Eb[1] + Eb[2];
-    cb += (Eb[2] - Eb[1]) * ss;
-    if (mg) {  // E1 = A . u; uc = u -+ c H; E2, E3 = E1 -+ c ss
-        mg[0] += E1b * u;
-        mg[1] += E1b * v;
-        mg[2] += E1b * w;
-        mg[3] += (ucb[1] - ucb[0]) * c;
-        mg[4] += (vcb[1] - vcb[0]) * c;
-        mg[5] += (wcb[1] - wcb[0]) * c;
-        mg[6] += (Eb[2] - Eb[1]) * c;
-    }
-    ub += A1 * E1b;
-    vb += A2 * E1b;
-    wb += A3 * E1b;
-    qb[0] += rhob;
+    qb[0] += tssb * ss * K.inv_2g;
     qb[1] += ub;
     qb[2] += vb;
     qb[3] += wb;
