@@ -326,8 +326,8 @@ SweepArgs sweep_args(f3d_ctx* ctx, int dir, const double* Q, bool hybrid, const 
 }
 
 // Sensor, viscous fluxes and the three sweeps. last.out_mode is OUT_RHS or OUT_STAGE.
-// Mixed precision: the FP32 copy of Q is made first unless q32_current says the previous
-// stage's primitive fill already wrote it.
+// fill_current: the previous stage's primitive fill already wrote what the sweeps read besides
+// Q (mixed precision: the FP32 copy of Q; FP64: the sound speed), so it is not made again.
 // Finite-volume RHS (FVM.jl): sensor, viscous fluxes, three face sweeps reconstructing the
 // conserved state (the stage's U, or prim2c(Q) for f3d_rhs) and, for a stage, the RK update
 // after the last sweep (the sweeps read U, so it cannot be updated inside them).
@@ -366,13 +366,13 @@ int run_rhs_fvm(f3d_ctx* ctx, const double* Q, double* acc, const SweepArgs& las
     return F3D_OK;
 }
 
-int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStream_t st, bool q32_current = false) {
+int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStream_t st, bool fill_current = false) {
     if (ctx->params.scheme != F3D_SCHEME_FDM) return run_rhs_fvm(ctx, Q, acc, last, st);
     const DevParams& P = ctx->dp;
     const bool hybrid = P.fixed_branch < 0;
     const bool mx = mixed(ctx);
     if (mx) {
-        if (!q32_current) {
+        if (!fill_current) {
             F3D_CUDA(ctx, launch_to_f32(Q, ctx->Q32, 6 * P.plane, st));
             mark(ctx, K_SOUND, st);
         }
@@ -387,8 +387,10 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
             mark(ctx, K_VISCOUS, st);
         }
     } else {
-        F3D_CUDA(ctx, launch_sound(P, Q, ctx->csnd, st));
-        mark(ctx, K_SOUND, st);
+        if (!fill_current) {
+            F3D_CUDA(ctx, launch_sound(P, Q, ctx->csnd, st));
+            mark(ctx, K_SOUND, st);
+        }
         if (hybrid) {
             F3D_CUDA(ctx, launch_sensor(P, Q, ctx->phi, st));
             mark(ctx, K_SENSOR, st);
@@ -443,8 +445,10 @@ int run_rhs(f3d_ctx* ctx, const double* Q, double* acc, SweepArgs last, cudaStre
     return F3D_OK;
 }
 
+// The stage's primitive fill also writes the FP32 copy of Q (mixed precision) or the sound
+// speed (FP64 finite differences) that the next stage's sweeps read.
 int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double* Q, cudaStream_t st,
-              bool q32_current = false) {
+              bool fill_current = false) {
     SweepArgs last;
     std::memset(&last, 0, sizeof(last));
     last.out_mode = OUT_STAGE;
@@ -459,9 +463,10 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
         F3D_CUDA(ctx, launch_local_dt(ctx->dp, Q, ctx->m, ctx->J, ctx->params.lts_cfl, ctx->dtl, st));
         last.dtl = ctx->dtl;
     }
-    int rc = run_rhs(ctx, Q, ctx->acc, last, st, q32_current);
+    int rc = run_rhs(ctx, Q, ctx->acc, last, st, fill_current);
     if (rc) return rc;
-    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, nullptr, 0, st, mixed(ctx) ? ctx->Q32 : nullptr));
+    const bool mx = mixed(ctx), fdm64 = !mx && ctx->params.scheme == F3D_SCHEME_FDM;
+    F3D_CUDA(ctx, launch_prim_fill(ctx->dp, U, Q, U, fdm64 ? ctx->csnd : nullptr, 0, st, mx ? ctx->Q32 : nullptr));
     mark(ctx, K_PRIM_FILL, st, 2);  // interior and ghost passes
     return F3D_OK;
 }
@@ -908,10 +913,14 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
     if (rc || (rc = check_ptrs(ctx, {U, Un, Q}))) return rc;
     if (nsteps < 0) return fail(ctx, F3D_ERR_ARG, "nsteps must be >= 0");
     cudaStream_t st = (cudaStream_t)stream;
-    // Mixed precision: Q's FP32 copy is made once here; afterwards every stage's primitive
-    // fill rewrites it, so the stages inside the step (and the graph) skip the conversion.
+    // Q's FP32 copy (mixed precision) or the sound speed (FP64) is made once here; afterwards
+    // every stage's primitive fill rewrites it, so the stages inside the step (and the graph)
+    // skip it. The filter between steps changes U only, not Q.
     const bool mx = mixed(ctx);
-    if (mx && nsteps > 0) F3D_CUDA(ctx, launch_to_f32(Q, ctx->Q32, 6 * ctx->dp.plane, st));
+    if (nsteps > 0) {
+        if (mx) F3D_CUDA(ctx, launch_to_f32(Q, ctx->Q32, 6 * ctx->dp.plane, st));
+        else if (ctx->params.scheme == F3D_SCHEME_FDM) F3D_CUDA(ctx, launch_sound(ctx->dp, Q, ctx->csnd, st));
+    }
     const int filt = ctx->params.filter, every = ctx->params.filter_interval;
     auto after_step = [&]() {  // solver.jl:446-470: filter after every `every`-th step
         ctx->tt++;
@@ -920,7 +929,7 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
     if (st == nullptr) {  // the legacy stream cannot be captured: plain launches
         for (int t = 0; t < nsteps; t++) {
             for (int s = 1; s <= 3; s++)
-                if ((rc = run_stage(ctx, s, dt, U, Un, Q, st, mx))) return rc;
+                if ((rc = run_stage(ctx, s, dt, U, Un, Q, st, true))) return rc;
             if ((rc = after_step())) return rc;
         }
         return F3D_OK;
@@ -936,7 +945,7 @@ int f3d_rk3_steps(f3d_ctx* ctx, int nsteps, double dt, double* U, double* Un, do
         cudaGraph_t g;
         F3D_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         int src = F3D_OK;
-        for (int s = 1; s <= 3 && !src; s++) src = run_stage(ctx, s, dt, U, Un, Q, st, mx);
+        for (int s = 1; s <= 3 && !src; s++) src = run_stage(ctx, s, dt, U, Un, Q, st, true);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (src) return src;
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
@@ -1232,9 +1241,9 @@ int f3d_profile_step(f3d_ctx* ctx, double dt, double* U, double* Un, double* Q, 
     for (int i = 0; i < Prof::kMax; i++) F3D_CUDA(ctx, cudaEventCreate(&prof.ev[i]));
     ctx->prof = &prof;
     mark(ctx, -1, st);
-    // as inside f3d_rk3_steps, the mixed form's FP32 copy of Q is made before the first stage
-    // only: every stage's primitive fill rewrites it
-    for (int s = 1; s <= 3 && !rc; s++) rc = run_stage(ctx, s, dt, U, Un, Q, st, mixed(ctx) && s > 1);
+    // as inside f3d_rk3_steps, the mixed form's FP32 copy of Q and the FP64 sound speed are
+    // made for the first stage only: every stage's primitive fill rewrites them
+    for (int s = 1; s <= 3 && !rc; s++) rc = run_stage(ctx, s, dt, U, Un, Q, st, s > 1);
     ctx->prof = nullptr;
     cudaError_t e = cudaStreamSynchronize(st);
     for (int k = 0; k < K_NKIND; k++) {

@@ -66,7 +66,8 @@ def setup(case: str, nx: int, ny: int, nz: int, character: int = 1, precision: i
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="sod", choices=["sod", "tgv", "tgv_viscous"])
+    ap.add_argument("--case", default=None, choices=["sod", "tgv", "tgv_viscous"],
+                    help="default: sod, or tgv_viscous with --adjoint")
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--ny", type=int, default=64)
     ap.add_argument("--nz", type=int, default=64)
@@ -75,10 +76,10 @@ def main(argv=None):
     ap.add_argument("--scheme", type=int, default=0, help="0 FDM, 1 FVM eigen, 2 FVM component-wise")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--step", action="store_true", help="profile_step instead of rhs (per-kernel event times)")
-    ap.add_argument("--adjoint", action="store_true", help="RK3 step VJPs on the viscous curvilinear TGV")
+    ap.add_argument("--adjoint", action="store_true", help="RK3 step VJPs")
     a = ap.parse_args(argv)
-    if a.adjoint:
-        a.case = "tgv_viscous"
+    if a.case is None:
+        a.case = "tgv_viscous" if a.adjoint else "sod"
     s, c, U, Q = setup(a.case, a.nx, a.ny, a.nz, a.character, a.precision, a.scheme)
     out = s.field(5)
     torch.cuda.synchronize()
