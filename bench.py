@@ -59,7 +59,7 @@ STEP_BYTES_PER_CELL = 3 * 160 + 2 * 40
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_sweep
 #       python -m flame3d_mhd_gb300.profile --case sod --nx 256 --ny 64 --nz 64 --reps 2 --step
 # (read + write bytes of each sweep divided by the interior cell count)
-KERNEL_TRAFFIC_PER_CELL = {"sweep_xi": 135.2, "sweep_eta": 191.8, "sweep_zeta": 291.4}
+KERNEL_TRAFFIC_PER_CELL = {"sweep_xi": 135.2, "sweep_eta": 195.7, "sweep_zeta": 297.1}
 
 
 def load_peaks() -> dict:
