@@ -102,16 +102,24 @@ __host__ __device__ inline long long lin3(const DevParams& P, int i, int j, int 
 // keep nvcc from contracting into FMA so that c2Prim and the ghost rules are bitwise
 // equal to the CPU restatement; the flux arithmetic is free to contract.
 
+// Julia's max(x, e) (a NaN x passes through) for a floor e > 0, on the bit patterns with
+// integer instructions instead of FP64-pipe compares: for x >= 0 the order of doubles is the
+// integer order of their patterns, a negative x (sign bit set) is a negative integer, and a
+// NaN has all exponent bits set and a nonzero mantissa. The same value as fmax for every x.
+__device__ __forceinline__ double max_floor(double x, double e) {
+    const long long bx = __double_as_longlong(x), be = __double_as_longlong(e);
+    if (be <= 0) return x != x ? x : fmax(x, e);  // a floor of 0 or below
+    return (bx > be || (bx & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) ? x : e;
+}
+
 // utils.jl:2-30 c2Prim of one cell. q = (rho,u,v,w,p,T).
 __device__ __forceinline__ void c2prim_cell(const DevParams& P, const double U[5], double q[6]) {
-    double rho = fmax(U[0], P.eps_clamp);
-    if (U[0] != U[0]) rho = U[0];  // Julia max propagates NaN
+    const double rho = max_floor(U[0], P.eps_clamp);
     double rinv = 1.0 / rho;
     double u = __dmul_rn(U[1], rinv), v = __dmul_rn(U[2], rinv), w = __dmul_rn(U[3], rinv);
     double ke = __dadd_rn(__dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v)), __dmul_rn(w, w));
     double eraw = __dadd_rn(U[4], -__dmul_rn(__dmul_rn(0.5, rho), ke));
-    double ei = fmax(eraw, P.eps_clamp);
-    if (eraw != eraw) ei = eraw;
+    const double ei = max_floor(eraw, P.eps_clamp);
     double p = __dmul_rn(P.gm1, ei);
     double T = p / __dmul_rn(rho, P.rg);
     q[0] = rho; q[1] = u; q[2] = v; q[3] = w; q[4] = p; q[5] = T;
@@ -151,23 +159,23 @@ __device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
 
 // 1/x: an FP32 reciprocal refined by two Newton-Raphson steps r <- r + r (1 - x r) in FP64
 // (quadratic convergence from 2^-24 to below FP64 rounding), within an ulp of the FP64
-// quotient; IEEE division outside 2^-120 < |x| < 2^120 (and for NaN).
+// quotient; IEEE division outside 2^-119 <= |x| < 2^120 (and for 0, infinities and NaN).
 __device__ __forceinline__ double recip_nr(double x) {
-    const double ax = fabs(x);
-    if (!(ax > 7.52316384526264e-37 && ax < 1.329227995784916e36)) return 1.0 / x;
+    // the range test on the biased exponent (integer instructions): 2^-119 <= |x| < 2^120
+    const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+    if (ex - 904u > 238u) return 1.0 / x;
     double r = f32_to_f64(__frcp_rn(f64_to_f32_rn(x)));
     r = fma(r, fma(-x, r, 1.0), r);
     return fma(r, fma(-x, r, 1.0), r);
 }
 
 __device__ __forceinline__ void c2prim_cell_fast(const DevParams& P, const double U[5], double q[6]) {
-    double rho = fmax(U[0], P.eps_clamp);
-    if (U[0] != U[0]) rho = U[0];
+    const double rho = max_floor(U[0], P.eps_clamp);
     const double rinv = recip_nr(rho);
     const double u = U[1] * rinv, v = U[2] * rinv, w = U[3] * rinv;
-    const double eraw = U[4] - 0.5 * rho * (u * u + v * v + w * w);
-    double ei = fmax(eraw, P.eps_clamp);
-    if (eraw != eraw) ei = eraw;
+    // rho |u|^2 / 2 as (momentum . velocity) / 2, folded into the subtraction from E
+    const double eraw = fma(-0.5, U[1] * u + U[2] * v + U[3] * w, U[4]);
+    const double ei = max_floor(eraw, P.eps_clamp);
     const double p = P.gm1 * ei;
     q[0] = rho; q[1] = u; q[2] = v; q[3] = w; q[4] = p; q[5] = p * (rinv * P.inv_rg);
 }
