@@ -169,6 +169,13 @@ def mixed_forward(R: "RampAdjoint", cells: int, J0: float, area0: torch.Tensor) 
             "J_rel_diff_vs_fp64": abs(Jm - J0) / abs(J0)}
 
 
+
+def progress(what: str, obj) -> None:
+    """One JSON line on stderr as each part of a long run completes (the full result is
+    printed on stdout at the end)."""
+    print(json.dumps({"progress": what, **({"out": obj} if not isinstance(obj, dict) else obj)}),
+          file=sys.stderr, flush=True)
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--nx", type=int, default=1024)
@@ -245,6 +252,7 @@ def main(argv=None):
     t_fwd = time.perf_counter() - t0
     out["fp64_forward"] = {"s": t_fwd, "mcell_rhs_per_s": 3 * cells * a.steps / t_fwd / 1e6}
     out["J"] = J0
+    progress("fp64_forward", out)
 
     # memory: slots of one state each
     state_b = R.U0.numel() * 8
@@ -334,6 +342,7 @@ def main(argv=None):
     out["cost"] = {"gradient_s": t_grad, "angle_stage_differences_s": sink_s[0],
                    "adjoint_over_forward": t_grad / t_fwd,
                    "adjoint_over_forward_without_angle": (t_grad - sink_s[0]) / t_fwd}
+    progress("gradient", out)
 
     # central differences in FP64
     rng = np.random.default_rng(a.seed)
@@ -351,6 +360,7 @@ def main(argv=None):
             fd = (Jp - Jm) / (2 * h)
             checks.append({"param": "s", "dir": k, "h": h, "adjoint": ad, "central_difference": fd,
                            "rel_diff": abs(fd - ad) / max(abs(ad), 1e-300)})
+            progress("check", checks[-1])
     for h in [float(v) for v in a.fd_angle_h.split(",") if v]:
         Jp = R.J(R._metrics(a.angle + h))
         Jm = R.J(R._metrics(a.angle - h))

@@ -109,6 +109,33 @@ def test_c2prim_prim2c_bitwise(gpu_lib):
     c.close()
 
 
+@pytest.mark.parametrize("clamp_eps", [0.0, 1e-3])
+def test_c2prim_clamps_bitwise(gpu_lib, clamp_eps):
+    """c2Prim's clamps of rho and e_int (utils.jl:12,18: Julia's max, a NaN passes through) at
+    NaN, signed zeros, negative, infinite and below-the-floor values: the oracle's bits at
+    every cell whose result is not NaN, NaN where the oracle's is."""
+    c = random_case(seed=3, clamp_eps=clamp_eps)
+    eps = clamp_eps if clamp_eps else 2.0 ** -23
+    U = c.U.copy()
+    rho_vals = [np.nan, -1.0, -0.0, 0.0, eps, eps / 2, eps * (1 + 2 ** -52), np.inf, -np.inf, 1e-300]
+    e_vals = [0.0, -5.0, np.nan, np.inf, -np.inf, eps * 1e-3]
+    cells = [(NG + 3, NG + 2, NG + 1 + i) for i in range(len(rho_vals) + len(e_vals))]  # (k, j, i)
+    for (k, j, i), r in zip(cells, rho_vals):
+        U[0, k, j, i] = r
+    for (k, j, i), e in zip(cells[len(rho_vals):], e_vals):
+        U[4, k, j, i] = e  # total energy below (or at) the kinetic energy: e_int clamped
+    Q = torch.zeros_like(dev(c.Q))
+    c.s.c2Prim(dev(U), Q)
+    Qo = orc.c2prim(c.P, U)
+    I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+    g, o = host(Q)[I], Qo[I]
+    nan = np.isnan(o)
+    assert np.array_equal(np.isnan(g), nan)
+    assert np.array_equal(g[~nan].view(np.uint64), o[~nan].view(np.uint64))
+    assert nan.any() and (~nan).all(axis=0).any()
+    c.close()
+
+
 @pytest.mark.parametrize("bcs", [
     "default",
     "periodic",
