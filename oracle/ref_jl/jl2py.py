@@ -1,0 +1,306 @@
+"""Mechanical translation of the reference's Julia GPU kernels into Python (test infrastructure).
+
+The reference's hot path is Julia (CUDA.jl kernels) and no Julia is available, so the oracle
+(oracle/f3d_oracle.hpp) is a restatement written by hand. To check that restatement against
+the reference's own source, this script translates the kernel files (split.jl, schemes.jl,
+viscous.jl, div.jl, utils.jl) statement by statement, with fixed rules and no hand edits:
+
+- comments dropped; a line ending in an operator, a comma or an open bracket continues;
+  ';' separates statements;
+- `function f(args)` .. `end`, `if` / `elseif` / `else`, `for v = a:b` become Python blocks; a
+  bare expression ending a function body is returned, as Julia returns it;
+- `@inbounds`, `@fastmath`, `@inline` and type annotations (`x::Float32 = ...`) are dropped;
+- literals: `12f0` -> `12e0`, `1i32` -> `1`, implicit products `547V1` -> `547*V1`;
+- `x^2` / `x^3` -> `_p2(x)` / `_p3(x)` (products, as Julia's literal powers), other `^` -> `**`,
+  `&&` / `||` / `!` -> `and` / `or` / `not`, `c ? a : b` -> `(a if c else b)`,
+  `x .= v` -> `x._fill(v)`, `MMatrix{n, m, ...}(undef)` / `MVector{n, ...}(undef)` -> 1-based
+  arrays, `CUDA.eps(Float32)` -> 2^-23, `÷` -> `//`, a character Julia allows in names and
+  Python does not (the ∂ of ∂ξ∂x) -> `_u2202_`;
+- array indexing is left as written: the runtime (runtime.py) passes arrays that take
+  Julia's 1-based, column-major subscripts.
+
+In this FP64 reading every value is a Python float (binary64); the reference's Float32
+annotations and f0 literals select the element type only, so the result is the reference's
+algorithm evaluated in FP64 in the reference's own operation order, the form the FP64 oracle
+restates. The generated module is written next to the compiled reference program
+(oracle/_ref/, not tracked).
+
+    python -m oracle.ref_jl.jl2py <reference root> [out.py]
+"""
+from __future__ import annotations
+
+import re
+import sys
+from pathlib import Path
+
+FILES = ("split.jl", "schemes.jl", "viscous.jl", "div.jl", "utils.jl")
+
+_OPEN = "([{"
+_CLOSE = ")]}"
+
+
+def _depth_delta(s: str) -> int:
+    d = 0
+    for ch in s:
+        if ch in _OPEN:
+            d += 1
+        elif ch in _CLOSE:
+            d -= 1
+    return d
+
+
+def _strip_comment(line: str) -> str:
+    out, in_str = [], False
+    for ch in line:
+        if ch == '"':
+            in_str = not in_str
+        if ch == "#" and not in_str:
+            break
+        out.append(ch)
+    return "".join(out).rstrip()
+
+
+def logical_lines(src: str) -> list[str]:
+    """Comment-free statements: continuation lines joined, ';'-separated statements split."""
+    phys = [_strip_comment(l) for l in src.splitlines()]
+    joined, buf, depth = [], "", 0
+    cont_end = ("+", "-", "*", "/", ",", "(", "[", "=", "&&", "||", "?", ":", "<", ">", "^")
+    for l in phys:
+        if not l.strip():
+            if buf and depth > 0:
+                continue
+            if buf:
+                joined.append(buf)
+                buf = ""
+            continue
+        buf = (buf + " " + l.strip()) if buf else l
+        depth += _depth_delta(l)
+        if depth > 0 or buf.rstrip().endswith(cont_end):
+            continue
+        joined.append(buf)
+        buf, depth = "", 0
+    if buf:
+        joined.append(buf)
+    out = []
+    for l in joined:
+        parts, cur, d = [], "", 0
+        for ch in l:
+            if ch in _OPEN:
+                d += 1
+            elif ch in _CLOSE:
+                d -= 1
+            if ch == ";" and d == 0:
+                parts.append(cur)
+                cur = ""
+            else:
+                cur += ch
+        parts.append(cur)
+        out.extend(p for p in parts if p.strip())
+    return out
+
+
+_NUM = r"(?<![\w.])(\d+\.\d*|\.\d+|\d+)"
+
+
+def _ternary(s: str) -> str:
+    """Rewrite the innermost `cond ? a : b` (at one bracket depth) until none is left."""
+    while "?" in s:
+        q = s.index("?")
+        # the bracket depth at q, and the span of the enclosing group or argument
+        depth = 0
+        start = 0
+        for i in range(q - 1, -1, -1):
+            ch = s[i]
+            if ch in _CLOSE:
+                depth += 1
+            elif ch in _OPEN:
+                if depth == 0:
+                    start = i + 1
+                    break
+                depth -= 1
+            elif ch == "," and depth == 0:
+                start = i + 1
+                break
+        depth = 0
+        colon = end = None
+        for i in range(q + 1, len(s)):
+            ch = s[i]
+            if ch in _OPEN:
+                depth += 1
+            elif ch in _CLOSE:
+                if depth == 0:
+                    end = i
+                    break
+                depth -= 1
+            elif ch == ":" and depth == 0 and colon is None:
+                colon = i
+            elif ch == "," and depth == 0 and colon is not None:
+                end = i
+                break
+        if end is None:
+            end = len(s)
+        if colon is None:
+            raise ValueError(f"ternary without ':' in {s!r}")
+        cond, a, b = s[start:q].strip(), s[q + 1:colon].strip(), s[colon + 1:end].strip()
+        s = s[:start] + f"(({a}) if ({cond}) else ({b}))" + s[end:]
+    return s
+
+
+def _literal_powers(s: str) -> str:
+    """x^2 -> _p2(x), x^3 -> _p3(x): Julia evaluates a literal integer power as products
+    (Base.literal_pow: x*x, x*x*x), which a libm pow does not always round alike."""
+    while True:
+        m = re.search(r"\*\*([23])(?![\d.eE])", s)
+        if not m:
+            return s
+        end = m.start()
+        i = end - 1
+        if s[i] in ")]":
+            depth = 0
+            while i >= 0:
+                if s[i] in ")]":
+                    depth += 1
+                elif s[i] in "([":
+                    depth -= 1
+                    if depth == 0:
+                        break
+                i -= 1
+            i -= 1
+            while i >= 0 and (s[i].isalnum() or s[i] == "_" or ord(s[i]) > 127):  # a call's or an array's name
+                i -= 1
+        else:
+            while i >= 0 and (s[i].isalnum() or s[i] in "_." or ord(s[i]) > 127):
+                i -= 1
+        start = i + 1
+        s = s[:start] + f"_p{m.group(1)}({s[start:end]})" + s[m.end():]
+
+
+def expr(s: str) -> str:
+    s = s.replace("CUDA.eps(Float32)", "_eps32()")
+    s = re.sub(r"MMatrix\{\s*([^,}]+)\s*,\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1, \2)", s)
+    s = re.sub(r"MVector\{\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1)", s)
+    s = re.sub(r"(\d+\.\d*|\.\d+|\d+)f(-?\d+)", r"\1e\2", s)          # Float32 literals
+    s = re.sub(r"(?<![\w.])(\d+)i32\b", r"\1", s)                       # Int32 literals
+    # implicit products: a numeric literal (possibly with exponent) followed by a name or '('
+    s = re.sub(_NUM + r"((?:[eE][-+]?\d+)?)(?=[A-Za-z_Ͱ-Ͽᴀ-ᶿ(])",
+               lambda m: m.group(1) + m.group(2) + ("*" if not (m.group(2) == "" and
+                                                              re.match(r"[eE]", s[m.end():m.end() + 1] or "x"))
+                                                    else ""), s)
+    s = s.replace("^", "**")
+    s = _literal_powers(s)
+    s = s.replace("&&", " and ").replace("||", " or ")
+    s = re.sub(r"!(?!=)", " not ", s)
+    s = s.replace("÷", "//")
+    s = re.sub(r"\btrue\b", "True", s)
+    s = re.sub(r"\bfalse\b", "False", s)
+    s = re.sub(r"\bnothing\b", "None", s)
+    s = re.sub(r"\bFloat32\(", "_f32(", s)
+    s = re.sub(r"\bFloat64\(", "_f64(", s)
+    s = _ternary(s)
+    # characters Julia allows in names and Python does not (e.g. the ∂ of ∂ξ∂x)
+    s = "".join(c if ord(c) < 128 or ("a" + c).isidentifier() else f"_u{ord(c):04x}_" for c in s)
+    return s
+
+
+def _strip_macros(s: str) -> str:
+    return re.sub(r"@(inbounds|fastmath|inline)\s+", "", s).strip()
+
+
+def _strip_annot(lhs: str) -> str:
+    return re.sub(r"::\s*\w+(\{[^}]*\})?", "", lhs).strip()
+
+
+def translate(src: str) -> str:
+    """Python source of every function of a Julia kernel file (top-level code is skipped)."""
+    out: list[str] = []
+    stack: list[str] = []
+    pad = lambda: "    " * len(stack)
+    last_expr = None  # index in out of the function body's last statement if it is a bare expression
+    for raw in logical_lines(src):
+        s = _strip_macros(raw)
+        if stack and s != "end":
+            last_expr = None
+        if not stack:
+            m = re.match(r"function\s+(\w+)\s*\((.*)\)\s*$", s)
+            if m:
+                out.append(f"def {m.group(1)}({_strip_annot(m.group(2))}):")
+                stack.append("function")
+            continue
+        if s == "end":
+            stack.pop()
+            if not stack:
+                # Julia returns the value of a function's last expression
+                if last_expr is not None:
+                    out[last_expr] = "    return " + out[last_expr].strip()
+                out.append("")
+            last_expr = None
+            continue
+        if re.match(r"function\b", s):
+            raise ValueError(f"nested function: {s}")
+        m = re.match(r"if\s+(.*)$", s)
+        if m:
+            out.append(pad() + f"if {expr(m.group(1))}:")
+            stack.append("if")
+            continue
+        m = re.match(r"elseif\s+(.*)$", s)
+        if m:
+            out.append("    " * (len(stack) - 1) + f"elif {expr(m.group(1))}:")
+            continue
+        if s == "else":
+            out.append("    " * (len(stack) - 1) + "else:")
+            continue
+        m = re.match(r"for\s+(\w+)\s*(?:=|in)\s*(.+?)\s*:\s*(.+)$", s)
+        if m:
+            out.append(pad() + f"for {m.group(1)} in range({expr(m.group(2))}, ({expr(m.group(3))}) + 1):")
+            stack.append("for")
+            continue
+        if s == "return" or s.startswith("return "):
+            rest = s[len("return"):].strip()
+            out.append(pad() + ("return" if not rest else f"return {expr(rest)}"))
+            continue
+        m = re.match(r"(.+?)\s*\.=\s*(.+)$", s)
+        if m:
+            out.append(pad() + f"{expr(m.group(1))}._fill({expr(m.group(2))})")
+            continue
+        m = re.match(r"(.+?)\s*(\+=|-=|\*=|/=)\s*(.+)$", s)
+        if m:
+            out.append(pad() + f"{expr(_strip_annot(m.group(1)))} {m.group(2)} {expr(m.group(3))}")
+            continue
+        m = re.match(r"([^=<>!]+?)\s*=(?!=)\s*(.+)$", s)
+        if m:
+            out.append(pad() + f"{expr(_strip_annot(m.group(1)))} = {expr(m.group(2))}")
+            continue
+        out.append(pad() + expr(s))
+        if len(stack) == 1:
+            last_expr = len(out) - 1
+    if stack:
+        raise ValueError(f"unterminated blocks: {stack}")
+    # a function whose body is empty after translation still needs a statement
+    fixed = []
+    for i, l in enumerate(out):
+        fixed.append(l)
+        if l.rstrip().endswith(":") and (i + 1 == len(out) or len(out[i + 1]) - len(out[i + 1].lstrip()) <=
+                                          len(l) - len(l.lstrip())):
+            fixed.append(" " * (len(l) - len(l.lstrip()) + 4) + "pass")
+    return "\n".join(fixed) + "\n"
+
+
+def translate_tree(root: Path) -> str:
+    parts = ["# Generated by oracle/ref_jl/jl2py.py from the reference's Julia kernels; do not edit.\n"]
+    for name in FILES:
+        parts.append(f"# ---- {name}\n")
+        parts.append(translate((root / name).read_text()))
+    return "\n".join(parts)
+
+
+def main(argv=None) -> None:
+    argv = sys.argv[1:] if argv is None else argv
+    root = Path(argv[0])
+    out = Path(argv[1]) if len(argv) > 1 else Path(__file__).resolve().parent.parent / "_ref" / "jl_kernels.py"
+    out.parent.mkdir(parents=True, exist_ok=True)
+    out.write_text(translate_tree(root))
+    print(out)
+
+
+if __name__ == "__main__":
+    main()

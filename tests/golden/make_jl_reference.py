@@ -1,0 +1,96 @@
+"""Make tests/golden/jl_reference_rhs.npz: the reference's own finite-difference RHS, from its
+Julia kernels translated mechanically into Python (oracle/ref_jl/jl2py.py) and run on the CPU
+(oracle/ref_jl/runtime.py), on
+- the inputs of the golden fixtures (test_oracle.py::test_golden_fixtures: four splits,
+  characteristic and component-wise, hybrid and WENO5-everywhere, periodic, reference and
+  mixed boundary rules; inviscid), and
+- two viscous cases made here the same way (curvilinear random states, Sutherland viscosity
+  large enough for the viscous terms to matter), whose inputs are stored too.
+The file also records SHA-256 digests of the translated Julia files and of the generated
+module. Needs the reference tree (read only):
+
+  python tests/golden/make_jl_reference.py --ref <reference tree>
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import importlib.util
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from flame3d_mhd_gb300.abi import BC_PERIODIC, make_params  # noqa: E402
+from oracle import np_oracle as npo  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+from oracle.ref_jl import jl2py, runtime  # noqa: E402
+
+NG = 4
+I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+VISCOUS = {
+    "curvi_viscous_char_sw_periodic": dict(n=(7, 6, 6), params=dict(
+        character=1, viscous=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0,
+        bc=[dict(kind=BC_PERIODIC)] * 6), seed=35, spikes=4),
+    "curvi_viscous_comp_lf_refbc": dict(n=(6, 6, 5), params=dict(
+        character=0, viscous=1, split_method=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0),
+        seed=36, spikes=4),
+}
+
+
+def _golden():
+    spec = importlib.util.spec_from_file_location("make_golden", HERE / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", required=True, help="root of the reference source tree")
+    a = ap.parse_args()
+    ref = Path(a.ref)
+    module = ROOT / "oracle" / "_ref" / "jl_kernels.py"
+    module.parent.mkdir(parents=True, exist_ok=True)
+    module.write_text(jl2py.translate_tree(ref))
+    out = {"provenance": np.array(json.dumps({
+        "translated": {f: hashlib.sha256((ref / f).read_bytes()).hexdigest() for f in jl2py.FILES},
+        "module_sha256": hashlib.sha256(module.read_bytes()).hexdigest(),
+        "semantics": "every value binary64; Julia's literal powers as products"}))}
+    report = {}
+    for f in sorted(HERE.glob("*.npz")):
+        d = np.load(f, allow_pickle=True)
+        if "rhs" not in d.files:  # RHS fixtures only
+            continue
+        meta = json.loads(str(d["meta"]))
+        P = make_params(*meta["n"], **meta["params"])
+        r = runtime.rhs(module, P, d["Q"], d["metrics"], d["J"])
+        out[f"{f.stem}__rhs"] = r
+        report[f.stem] = r
+    g = _golden()
+    for name, spec in VISCOUS.items():
+        n, params = spec["n"], dict(spec["params"])
+        P = make_params(*n, **params)
+        x, y, z = g.coords(n)
+        Q = g.initial(P, n, spec["seed"], spec["spikes"], False, x, y, z)
+        U = orc.prim2c(P, Q)
+        orc.fill_ghosts(P, Q, U)
+        m, J = npo.metrics(x, y, z)
+        m = np.stack(m)
+        r = runtime.rhs(module, P, Q, m, J)
+        meta = dict(n=list(n), params=params)
+        out.update({f"{name}__Q": Q, f"{name}__metrics": m, f"{name}__J": J, f"{name}__rhs": r,
+                    f"{name}__meta": np.array(json.dumps(meta))})
+        report[name] = r
+    np.savez_compressed(HERE / "jl_reference_rhs.npz", **out)
+    for name, r in report.items():
+        print(name, "max |rhs|", float(np.abs(r[I]).max()))
+
+
+if __name__ == "__main__":
+    main()

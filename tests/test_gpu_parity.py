@@ -136,6 +136,42 @@ def test_c2prim_clamps_bitwise(gpu_lib, clamp_eps):
     c.close()
 
 
+def _jl_reference_cases():
+    """The cases of tests/golden/jl_reference_rhs.npz: the reference's own RHS (its Julia kernels
+    translated mechanically, evaluated in binary64) with the inputs it was computed from."""
+    import json
+    from pathlib import Path
+    gdir = Path(__file__).resolve().parent / "golden"
+    d = np.load(gdir / "jl_reference_rhs.npz", allow_pickle=True)
+    out = {}
+    for name in sorted({k.split("__")[0] for k in d.files if k.endswith("__rhs")}):
+        if f"{name}__Q" in d.files:
+            src, meta = d, json.loads(str(d[f"{name}__meta"]))
+            Q, m, J = d[f"{name}__Q"], d[f"{name}__metrics"], d[f"{name}__J"]
+        else:
+            g = np.load(gdir / f"{name}.npz", allow_pickle=True)
+            meta, Q, m, J = json.loads(str(g["meta"])), g["Q"], g["metrics"], g["J"]
+        out[name] = (meta, Q, m, J, d[f"{name}__rhs"])
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(_jl_reference_cases()))
+def test_rhs_against_the_translated_reference(gpu_lib, name):
+    """The GPU RHS against the reference's own RHS on the same inputs: the FP64 bar of
+    assert_rhs_parity (the oracle it compares with equals the reference's RHS bit for bit here,
+    tests/test_oracle_jl.py), and the plain relative distance to the reference's RHS itself."""
+    meta, Q, m, J, ref = _jl_reference_cases()[name]
+    P = make_params(*meta["n"], **meta["params"])
+    s = Flame3D(P)
+    s.set_metrics([dev(np.ascontiguousarray(a)) for a in m], dev(np.ascontiguousarray(J)))
+    r = host(s.rhs(dev(np.ascontiguousarray(Q))))
+    I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+    e = rhs_parity(P, np.ascontiguousarray(Q), [np.ascontiguousarray(a) for a in m], np.ascontiguousarray(J), r)
+    assert_rhs_parity(e)
+    assert rel_linf(r[I], ref[I]) == e["plain"]
+    s.close()
+
+
 @pytest.mark.parametrize("bcs", [
     "default",
     "periodic",

@@ -1,0 +1,127 @@
+"""The oracle against the reference's own Julia kernels, translated mechanically into Python
+(oracle/ref_jl/jl2py.py, run by oracle/ref_jl/runtime.py; CPU only).
+
+tests/golden/jl_reference_rhs.npz holds the reference's finite-difference RHS, so computed
+(tests/golden/make_jl_reference.py), on the golden fixtures' inputs and on two viscous cases.
+The FP64 oracle must equal it bit for bit: the same statements in the same order, in binary64
+(the oracle is built without FMA contraction). With F3D_REFERENCE naming the reference tree,
+the translation is regenerated and must reproduce the digest recorded with the fixture.
+"""
+import json
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from flame3d_mhd_gb300.abi import make_params
+from oracle import oracle as orc
+from oracle.ref_jl import jl2py
+from oracle.ref_jl.runtime import JArray
+
+ROOT = Path(__file__).resolve().parent.parent
+FIX = ROOT / "tests" / "golden" / "jl_reference_rhs.npz"
+NG = 4
+I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+
+
+def _cases():
+    d = np.load(FIX, allow_pickle=True)
+    names = sorted({k.split("__")[0] for k in d.files if k.endswith("__rhs")})
+    return d, names
+
+
+def _inputs(d, name):
+    if f"{name}__Q" in d.files:
+        meta = json.loads(str(d[f"{name}__meta"]))
+        return meta, d[f"{name}__Q"], d[f"{name}__metrics"], d[f"{name}__J"]
+    g = np.load(ROOT / "tests" / "golden" / f"{name}.npz", allow_pickle=True)
+    return json.loads(str(g["meta"])), g["Q"], g["metrics"], g["J"]
+
+
+@pytest.mark.parametrize("name", _cases()[1])
+def test_oracle_equals_the_translated_reference(name):
+    d, _ = _cases()
+    meta, Q, m, J = _inputs(d, name)
+    P = make_params(*meta["n"], **meta["params"])
+    ro = orc.rhs(P, Q, list(m), J)
+    ref = d[f"{name}__rhs"]
+    assert np.abs(ref[I]).max() > 0
+    assert np.array_equal(ro[I], ref[I]), float(np.abs(ro[I] - ref[I]).max())
+
+
+def test_fixture_covers_the_forms():
+    d, names = _cases()
+    forms = set()
+    for name in names:
+        p = _inputs(d, name)[0]["params"]
+        forms.add((p.get("split_method", 0), p.get("character", 1), p.get("viscous", 0)))
+    assert {s for s, _, _ in forms} == {0, 1, 2, 3}  # SW, LF, VL, AUSM
+    assert {c for _, c, _ in forms} == {0, 1} and {v for _, _, v in forms} == {0, 1}
+
+
+REF = Path(os.environ.get("F3D_REFERENCE", "")) if os.environ.get("F3D_REFERENCE") else None
+
+
+@pytest.mark.skipif(REF is None or not (REF / "schemes.jl").exists(),
+                    reason="F3D_REFERENCE does not name the reference tree")
+def test_translation_reproduces_the_fixture_digest():
+    import hashlib
+    prov = json.loads(str(np.load(FIX, allow_pickle=True)["provenance"]))
+    for f, h in prov["translated"].items():
+        assert hashlib.sha256((REF / f).read_bytes()).hexdigest() == h, f
+    assert hashlib.sha256(jl2py.translate_tree(REF).encode()).hexdigest() == prov["module_sha256"]
+
+
+# ---- the translation rules on small pieces of Julia
+def _py(src):
+    return jl2py.translate(src).strip()
+
+
+def test_rule_literals_and_products():
+    assert jl2py.expr("-3V1+13V2") == "-3*V1+13*V2"
+    assert jl2py.expr("1/12f0") == "1/12e0"
+    assert jl2py.expr("x*1e-20 + 5f-2") == "x*1e-20 + 5e-2"
+    assert jl2py.expr("(blockIdx().x-1i32)") == "(blockIdx().x-1)"
+    assert jl2py.expr("2(a+b)") == "2*(a+b)"
+
+
+def test_rule_powers_and_logic():
+    assert jl2py.expr("u^2 + (a-b)^2 + x^3") == "_p2(u) + _p2((a-b)) + _p3(x)"
+    assert jl2py.expr("F[i, j]^2") == "_p2(F[i, j])"
+    assert jl2py.expr("T^1.5") == "T**1.5"
+    assert jl2py.expr("a > b && !c || d != e") == "a > b  and   not c  or  d != e"
+
+
+def test_rule_ternary_and_names():
+    assert jl2py.expr("ifelse(a*b > 0, (abs(a) > abs(b)) ? b : a, zero(a))") == \
+        "ifelse(a*b > 0,((b) if ((abs(a) > abs(b))) else (a)), zero(a))"
+    assert jl2py.expr("∂ξ∂x") == "_u2202_ξ_u2202_x"
+
+
+def test_rule_blocks_and_implicit_return():
+    src = """
+    # a comment
+    @inline function f(a, b)
+        ifelse(a > b, a, b)
+    end
+    function g(A, n)
+        s::Float32 = 0.f0
+        for m = 1:n
+            @inbounds s += A[m] *
+                           2
+        end
+        if s > 1; s = 1.f0; elseif s < 0
+            s = 0
+        else
+            s = s
+        end
+        return s
+    end
+    """
+    py = _py(src)
+    ns = {"ifelse": lambda c, a, b: a if c else b}
+    exec(py, ns)
+    assert ns["f"](1, 2) == 2
+    assert ns["g"](JArray(np.array([0.1, 0.2])), 2) == pytest.approx(0.6)  # 1-based A[m]
+    assert ns["g"](JArray(np.array([1.0, 1.0])), 2) == 1.0
