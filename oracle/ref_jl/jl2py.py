@@ -3,7 +3,8 @@
 The reference's hot path is Julia (CUDA.jl kernels) and no Julia is available, so the oracle
 (oracle/f3d_oracle.hpp) is a restatement written by hand. To check that restatement against
 the reference's own source, this script translates the kernel files (split.jl, schemes.jl,
-viscous.jl, div.jl, utils.jl) statement by statement, with fixed rules and no hand edits:
+viscous.jl, div.jl, utils.jl, boundary.jl) statement by statement, with fixed rules and no
+hand edits:
 
 - comments dropped; a line ending in an operator, a comma or an open bracket continues;
   ';' separates statements;
@@ -14,7 +15,8 @@ viscous.jl, div.jl, utils.jl) statement by statement, with fixed rules and no ha
 - `x^2` / `x^3` -> `_p2(x)` / `_p3(x)` (products, as Julia's literal powers), other `^` -> `**`,
   `&&` / `||` / `!` -> `and` / `or` / `not`, `c ? a : b` -> `(a if c else b)`,
   `x .= v` -> `x._fill(v)`, `MMatrix{n, m, ...}(undef)` / `MVector{n, ...}(undef)` -> 1-based
-  arrays, `CUDA.eps(Float32)` -> 2^-23, `÷` -> `//`, a character Julia allows in names and
+  arrays, `@cuda <keywords> f(args)` -> `_cuda(f, args)` (a launch the runtime runs over the
+  grid), `CUDA.eps(Float32)` -> 2^-23, `÷` -> `//`, a character Julia allows in names and
   Python does not (the ∂ of ∂ξ∂x) -> `_u2202_`;
 - array indexing is left as written: the runtime (runtime.py) passes arrays that take
   Julia's 1-based, column-major subscripts.
@@ -33,7 +35,7 @@ import re
 import sys
 from pathlib import Path
 
-FILES = ("split.jl", "schemes.jl", "viscous.jl", "div.jl", "utils.jl")
+FILES = ("split.jl", "schemes.jl", "viscous.jl", "div.jl", "utils.jl", "boundary.jl")
 
 _OPEN = "([{"
 _CLOSE = ")]}"
@@ -203,7 +205,21 @@ def expr(s: str) -> str:
 
 
 def _strip_macros(s: str) -> str:
-    return re.sub(r"@(inbounds|fastmath|inline)\s+", "", s).strip()
+    s = re.sub(r"@(inbounds|fastmath|inline)\s+", "", s).strip()
+    # a kernel launch of a host function: @cuda <keyword = value ...> f(args) -> _cuda(f, args)
+    m = re.match(r"@cuda\s+(.*)$", s)
+    if m:
+        rest = m.group(1)
+        while True:
+            k = re.match(r"\w+\s*=\s*[\w.()]+\s+(?=\w)", rest)
+            if not k:
+                break
+            rest = rest[k.end():]
+        c = re.match(r"(\w+)\((.*)\)\s*$", rest)
+        if not c:
+            raise ValueError(f"unrecognised launch: {s}")
+        s = f"_cuda({c.group(1)}, {c.group(2)})"
+    return s
 
 
 def _strip_annot(lhs: str) -> str:

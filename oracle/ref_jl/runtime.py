@@ -11,7 +11,8 @@ and run.jl gave them:
   thresholds, Linear, NG, Nxp, Nyp, Nzp) from an f3d_params;
 - the launch sequence of one finite-difference RHS: the sensor (solver.jl:424), the split and
   the reconstruction of each direction (solver.jl:133-188), the viscous fluxes and div
-  (solver.jl:429) with U = 0 and dt = 1, so U ends holding J times the flux divergence, the RHS.
+  (solver.jl:429) with U = 0 and dt = 1, so U ends holding J times the flux divergence, the RHS;
+- prim2c, c2Prim and the ghost fill of one process for boundary.jl's own boundary set.
 
 Every value is a Python float (binary64): the reference's algorithm in FP64, in its own
 operation order. Slow (one Python call per thread): grids of a few hundred cells.
@@ -103,6 +104,9 @@ def kernels(module_path: Path | str, P) -> dict:
     })
     # Python reads identifiers NFKC-normalised (the ϕ of hybrid_ϕ1 becomes φ): so must the names
     g = {unicodedata.normalize("NFKC", name): v for name, v in g.items()}
+    ext = (int(P.nx) + 2 * NG, int(P.ny) + 2 * NG, int(P.nz) + 2 * NG)
+    g["_cuda"] = lambda fn, *args: launch(fn, ext, *args)  # the grid of every @cuda launch
+    g["Nprocs"] = JArray(np.array([1, 1, 1]))
     exec(compile(Path(module_path).read_text(), str(module_path), "exec"), g)
     return g
 
@@ -117,22 +121,43 @@ def launch(fn, ext, *args):
                 fn(*args)
 
 
-SPLITS = ("fluxSplit_SW", "fluxSplit_LF", "fluxSplit_VL", "fluxSplit_AUSM")
+def is_reference_bcs(P) -> bool:
+    """The boundary set boundary.jl hard-codes: x- the free stream (rho 1, u 0.5, p 1/1.4),
+    x+ zero gradient, y- an adiabatic no-slip wall, y+ the free stream, z periodic."""
+    k = [int(b.kind) for b in P.bc]
+    fs = [P.bc[0], P.bc[3]]
+    return k == [1, 2, 3, 1, 0, 0] and all(
+        (float(b.rho), float(b.u), float(b.v), float(b.w), float(b.p)) == (1.0, 0.5, 0.0, 0.0, 1.0 / 1.4) for b in fs)
 
 
-def rhs(module_path, P, Q: np.ndarray, metrics: np.ndarray, J: np.ndarray) -> np.ndarray:
-    """dU/dt at the interior (zero elsewhere) of the reference's finite-difference RHS from
-    the ghost-filled primitive state Q (6, Nt...), the nine J^-1-scaled metrics and J."""
+def state_and_ghosts(module_path, P, Q: np.ndarray):
+    """U = prim2c(Q) at every cell (utils.jl:33-54); then, as a stage does
+    (solver.jl:438-443), Q = c2Prim(U) at the interior (utils.jl:2-30) and the ghost fill of one
+    process (boundary.jl's fillGhost: fill_x, fill_y, fill_z; the periodic exchange of mpi.jl on
+    one process only copies layers that fill_y and fill_z overwrite afterwards). Returns
+    (U from prim2c, Q after c2Prim and the fill, U after the fill)."""
+    if not is_reference_bcs(P):
+        raise ValueError("boundary.jl hard-codes one boundary set; these parameters have another")
     k = kernels(module_path, P)
     nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
     ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
-    Qj, Jj = JArray(Q.astype(np.float64)), JArray(J.astype(np.float64))
-    m = [JArray(metrics[n].astype(np.float64)) for n in range(9)]
-    # solver.jl:286-288: s = sqrt(a^2 + b^2 + c^2) of each metric row
-    S = [JArray(np.sqrt(metrics[3 * d] ** 2 + metrics[3 * d + 1] ** 2 + metrics[3 * d + 2] ** 2)) for d in range(3)]
-    phi = JArray(np.zeros(Q.shape[1:]))
+    U = JArray(np.zeros((5, *Q.shape[1:])))
+    launch(k["prim2c"], ext, U, JArray(Q.astype(np.float64)))
+    U0 = U.a.copy()
+    Q2 = JArray(np.zeros(Q.shape))
+    launch(k["c2Prim"], ext, U, Q2)
+    k["fillGhost"](Q2, U, 0, 0)  # rank (0, 0) of one process
+    return U0, Q2.a, U.a
+
+
+def _advance(k, P, Qj, m, S, Jj, U, dt):
+    """The sensor, flowAdvance's finite-difference branch and div (U += dt J (...))."""
+    nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
+    ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
+    shape = Qj.a.shape[1:]
+    phi = JArray(np.zeros(shape))
     launch(k["shockSensor"], ext, phi, Qj)
-    Fp, Fm = JArray(np.zeros((5, *Q.shape[1:]))), JArray(np.zeros((5, *Q.shape[1:])))
+    Fp, Fm = JArray(np.zeros((5, *shape))), JArray(np.zeros((5, *shape)))
     F = [JArray(np.zeros((5, nz, ny, nx + 1))), JArray(np.zeros((5, nz, ny + 1, nx))),
          JArray(np.zeros((5, nz + 1, ny, nx)))]
     split = k[SPLITS[int(P.split_method)]]
@@ -145,6 +170,56 @@ def rhs(module_path, P, Q: np.ndarray, metrics: np.ndarray, J: np.ndarray) -> np
     Fv = [JArray(np.zeros((4, nz + 4, ny + 4, nx + 4))) for _ in range(3)]
     if int(P.viscous):
         launch(k["viscousFlux"], ext, *Fv, Qj, *m, Jj)
+    launch(k["div"], (nx, ny, nz), U, *F, *Fv, dt, Jj)
+
+
+def _metric_arrays(metrics, J):
+    m = [JArray(metrics[n].astype(np.float64)) for n in range(9)]
+    # solver.jl:286-288: s = sqrt(a^2 + b^2 + c^2) of each metric row
+    S = [JArray(np.sqrt(metrics[3 * d] ** 2 + metrics[3 * d + 1] ** 2 + metrics[3 * d + 2] ** 2)) for d in range(3)]
+    return m, S, JArray(J.astype(np.float64))
+
+
+def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int, Q0: np.ndarray | None = None):
+    """nsteps SSP-RK3 steps of time_step's loop (solver.jl:416-444; no local time step, no
+    filter) from the conserved state U0 and its ghost-filled primitive state Q0 (formed from U0
+    as a stage forms it when not given), for boundary.jl's boundary set. Returns (U, Q)."""
+    if not is_reference_bcs(P):
+        raise ValueError("boundary.jl hard-codes one boundary set; these parameters have another")
+    k = kernels(module_path, P)
+    nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
+    ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
+    m, S, Jj = _metric_arrays(metrics, J)
+    U = JArray(U0.astype(np.float64).copy())
+    if Q0 is None:
+        Q = JArray(np.zeros((6, *U0.shape[1:])))
+        launch(k["c2Prim"], ext, U, Q)
+        k["fillGhost"](Q, U, 0, 0)
+    else:
+        Q = JArray(Q0.astype(np.float64).copy())
+    for _ in range(nsteps):
+        for krk in (1, 2, 3):
+            if krk == 1:
+                Un = JArray(U.a.copy())
+            _advance(k, P, Q, m, S, Jj, U, dt)
+            if krk == 2:
+                launch(k["linComb"], ext, U, Un, 5, 0.25, 0.75)
+            elif krk == 3:
+                launch(k["linComb"], ext, U, Un, 5, 2 / 3, 1 / 3)
+            launch(k["c2Prim"], ext, U, Q)
+            k["fillGhost"](Q, U, 0, 0)
+    return U.a, Q.a
+
+
+SPLITS = ("fluxSplit_SW", "fluxSplit_LF", "fluxSplit_VL", "fluxSplit_AUSM")
+
+
+def rhs(module_path, P, Q: np.ndarray, metrics: np.ndarray, J: np.ndarray) -> np.ndarray:
+    """dU/dt at the interior (zero elsewhere) of the reference's finite-difference RHS from
+    the ghost-filled primitive state Q (6, Nt...), the nine J^-1-scaled metrics and J: the
+    advance of one stage with U = 0 and dt = 1."""
+    k = kernels(module_path, P)
+    m, S, Jj = _metric_arrays(metrics, J)
     U = JArray(np.zeros((5, *Q.shape[1:])))
-    launch(k["div"], (nx, ny, nz), U, *F, *Fv, 1.0, Jj)
+    _advance(k, P, JArray(Q.astype(np.float64)), m, S, Jj, U, 1.0)
     return U.a

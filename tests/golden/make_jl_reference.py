@@ -4,8 +4,10 @@ Julia kernels translated mechanically into Python (oracle/ref_jl/jl2py.py) and r
 - the inputs of the golden fixtures (test_oracle.py::test_golden_fixtures: four splits,
   characteristic and component-wise, hybrid and WENO5-everywhere, periodic, reference and
   mixed boundary rules; inviscid), and
-- two viscous cases made here the same way (curvilinear random states, Sutherland viscosity
-  large enough for the viscous terms to matter), whose inputs are stored too.
+- three viscous cases made here the same way (curvilinear random states, Sutherland viscosity
+  large enough for the viscous terms to matter), whose inputs are stored too;
+and, for the cases with boundary.jl's own boundary set, the reference's prim2c, c2Prim with
+the ghost fill, and two SSP-RK3 steps (the stage loop of solver.jl).
 The file also records SHA-256 digests of the translated Julia files and of the generated
 module. Needs the reference tree (read only):
 
@@ -40,7 +42,10 @@ VISCOUS = {
     "curvi_viscous_comp_lf_refbc": dict(n=(6, 6, 5), params=dict(
         character=0, viscous=1, split_method=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0),
         seed=36, spikes=4),
+    "curvi_viscous_char_sw_refbc": dict(n=(6, 5, 5), params=dict(
+        character=1, viscous=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0), seed=37, spikes=4),
 }
+RK3_DT, RK3_STEPS = 2e-4, 2
 
 
 def _golden():
@@ -48,6 +53,15 @@ def _golden():
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     return mod
+
+
+def _state_steps(module, P, Q, m, J, name):
+    """For boundary.jl's own boundary set: U = prim2c(Q), then c2Prim and the ghost fill of a
+    stage, and RK3_STEPS SSP-RK3 steps of dt = RK3_DT from (U, Q)."""
+    U0, Qf, Uf = runtime.state_and_ghosts(module, P, Q)
+    U, Qs = runtime.rk3_steps(module, P, U0, m, J, RK3_DT, RK3_STEPS, Q0=Q)
+    return {f"{name}__U_prim2c": U0, f"{name}__Q_filled": Qf, f"{name}__U_filled": Uf,
+            f"{name}__U_rk3": U, f"{name}__Q_rk3": Qs}
 
 
 def main() -> None:
@@ -61,7 +75,8 @@ def main() -> None:
     out = {"provenance": np.array(json.dumps({
         "translated": {f: hashlib.sha256((ref / f).read_bytes()).hexdigest() for f in jl2py.FILES},
         "module_sha256": hashlib.sha256(module.read_bytes()).hexdigest(),
-        "semantics": "every value binary64; Julia's literal powers as products"}))}
+        "semantics": "every value binary64; Julia's literal powers as products",
+        "rk3": {"dt": RK3_DT, "steps": RK3_STEPS}}))}
     report = {}
     for f in sorted(HERE.glob("*.npz")):
         d = np.load(f, allow_pickle=True)
@@ -72,6 +87,8 @@ def main() -> None:
         r = runtime.rhs(module, P, d["Q"], d["metrics"], d["J"])
         out[f"{f.stem}__rhs"] = r
         report[f.stem] = r
+        if runtime.is_reference_bcs(P):
+            out.update(_state_steps(module, P, d["Q"], d["metrics"], d["J"], f.stem))
     g = _golden()
     for name, spec in VISCOUS.items():
         n, params = spec["n"], dict(spec["params"])
@@ -87,6 +104,8 @@ def main() -> None:
         out.update({f"{name}__Q": Q, f"{name}__metrics": m, f"{name}__J": J, f"{name}__rhs": r,
                     f"{name}__meta": np.array(json.dumps(meta))})
         report[name] = r
+        if runtime.is_reference_bcs(P):
+            out.update(_state_steps(module, P, Q, m, J, name))
     np.savez_compressed(HERE / "jl_reference_rhs.npz", **out)
     for name, r in report.items():
         print(name, "max |rhs|", float(np.abs(r[I]).max()))

@@ -151,7 +151,11 @@ def _jl_reference_cases():
         else:
             g = np.load(gdir / f"{name}.npz", allow_pickle=True)
             meta, Q, m, J = json.loads(str(g["meta"])), g["Q"], g["metrics"], g["J"]
-        out[name] = (meta, Q, m, J, d[f"{name}__rhs"])
+        steps = None
+        if f"{name}__U_rk3" in d.files:
+            rk = json.loads(str(d["provenance"]))["rk3"]
+            steps = (d[f"{name}__U_prim2c"], d[f"{name}__U_rk3"], rk["dt"], rk["steps"])
+        out[name] = (meta, Q, m, J, d[f"{name}__rhs"], steps)
     return out
 
 
@@ -160,7 +164,7 @@ def test_rhs_against_the_translated_reference(gpu_lib, name):
     """The GPU RHS against the reference's own RHS on the same inputs: the FP64 bar of
     assert_rhs_parity (the oracle it compares with equals the reference's RHS bit for bit here,
     tests/test_oracle_jl.py), and the plain relative distance to the reference's RHS itself."""
-    meta, Q, m, J, ref = _jl_reference_cases()[name]
+    meta, Q, m, J, ref, _ = _jl_reference_cases()[name]
     P = make_params(*meta["n"], **meta["params"])
     s = Flame3D(P)
     s.set_metrics([dev(np.ascontiguousarray(a)) for a in m], dev(np.ascontiguousarray(J)))
@@ -169,6 +173,25 @@ def test_rhs_against_the_translated_reference(gpu_lib, name):
     e = rhs_parity(P, np.ascontiguousarray(Q), [np.ascontiguousarray(a) for a in m], np.ascontiguousarray(J), r)
     assert_rhs_parity(e)
     assert rel_linf(r[I], ref[I]) == e["plain"]
+    s.close()
+
+
+@pytest.mark.parametrize("name", sorted(n for n, c in _jl_reference_cases().items() if c[5] is not None))
+def test_rk3_steps_against_the_translated_reference(gpu_lib, name):
+    """Two SSP-RK3 steps (f3d_rk3_steps, graph-captured) from the reference's prim2c of the stored
+    state, against the reference's own two steps (its stage loop, boundary.jl's boundary set),
+    with the state bar of test_rk3_steps_parity."""
+    meta, Q, m, J, _, steps = _jl_reference_cases()[name]
+    U0, Uref, dt, n = steps
+    P = make_params(*meta["n"], **meta["params"])
+    s = Flame3D(P)
+    s.set_metrics([dev(np.ascontiguousarray(a)) for a in m], dev(np.ascontiguousarray(J)))
+    U, Un, Qd = dev(U0), torch.zeros_like(dev(U0)), dev(np.ascontiguousarray(Q))
+    with side_stream() as stream:
+        s.time_step(U, Un, Qd, dt, n)
+    stream.synchronize()
+    I = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+    assert rel_linf(host(U)[I], Uref[I], per_var=False) <= 1e-12
     s.close()
 
 

@@ -2,9 +2,10 @@
 (oracle/ref_jl/jl2py.py, run by oracle/ref_jl/runtime.py; CPU only).
 
 tests/golden/jl_reference_rhs.npz holds the reference's finite-difference RHS, so computed
-(tests/golden/make_jl_reference.py), on the golden fixtures' inputs and on two viscous cases.
-The FP64 oracle must equal it bit for bit: the same statements in the same order, in binary64
-(the oracle is built without FMA contraction). With F3D_REFERENCE naming the reference tree,
+(tests/golden/make_jl_reference.py), on the golden fixtures' inputs and on three viscous
+cases, and for the cases with boundary.jl's own boundary set its prim2c, c2Prim with the
+ghost fill and two SSP-RK3 steps. The FP64 oracle must equal all of it bit for bit: the same
+statements in the same order, in binary64 (the oracle is built without FMA contraction). With F3D_REFERENCE naming the reference tree,
 the translation is regenerated and must reproduce the digest recorded with the fixture.
 """
 import json
@@ -48,6 +49,29 @@ def test_oracle_equals_the_translated_reference(name):
     ref = d[f"{name}__rhs"]
     assert np.abs(ref[I]).max() > 0
     assert np.array_equal(ro[I], ref[I]), float(np.abs(ro[I] - ref[I]).max())
+
+
+def _state_cases():
+    d, names = _cases()
+    return [n for n in names if f"{n}__U_rk3" in d.files]
+
+
+@pytest.mark.parametrize("name", _state_cases())
+def test_oracle_state_ghosts_and_steps_equal_the_translated_reference(name):
+    """prim2c, c2Prim with the ghost fill (boundary.jl's own boundary set, every cell including
+    edges and corners) and two SSP-RK3 steps of the stage loop (solver.jl:416-444): bit for bit."""
+    d, _ = _cases()
+    meta, Q, m, J = _inputs(d, name)
+    P = make_params(*meta["n"], **meta["params"])
+    U = orc.prim2c(P, Q)
+    assert np.array_equal(U, d[f"{name}__U_prim2c"])
+    Qf, Uf = orc.c2prim(P, U), U.copy()
+    orc.fill_ghosts(P, Qf, Uf)
+    assert np.array_equal(Qf, d[f"{name}__Q_filled"]) and np.array_equal(Uf, d[f"{name}__U_filled"])
+    rk = json.loads(str(d["provenance"]))["rk3"]
+    Us, Un, Qs = U.copy(), np.zeros_like(U), np.array(Q, dtype=np.float64)
+    orc.rk3(P, rk["steps"], rk["dt"], Us, Un, Qs, list(m), J)
+    assert np.array_equal(Us, d[f"{name}__U_rk3"]) and np.array_equal(Qs, d[f"{name}__Q_rk3"])
 
 
 def test_fixture_covers_the_forms():
