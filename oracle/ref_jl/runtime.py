@@ -12,7 +12,8 @@ and run.jl gave them:
 - the launch sequence of one finite-difference RHS: the sensor (solver.jl:424), the split and
   the reconstruction of each direction (solver.jl:133-188), the viscous fluxes and div
   (solver.jl:429) with U = 0 and dt = 1, so U ends holding J times the flux divergence, the RHS;
-- prim2c, c2Prim and the ghost fill of one process for boundary.jl's own boundary set.
+- prim2c, c2Prim and the ghost fill of one process for boundary.jl's own boundary set, the
+  RK3 stage loop of time_step, its local time step and its filtering pass.
 
 Every value is a Python float (binary64): the reference's algorithm in FP64, in its own
 operation order. Slow (one Python call per thread): grids of a few hundred cells.
@@ -209,6 +210,45 @@ def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int
             launch(k["c2Prim"], ext, U, Q)
             k["fillGhost"](Q, U, 0, 0)
     return U.a, Q.a
+
+
+def prim2c(module_path, P, Q: np.ndarray) -> np.ndarray:
+    """prim2c (utils.jl:33-54) at every cell."""
+    k = kernels(module_path, P)
+    U = JArray(np.zeros((5, *Q.shape[1:])))
+    launch(k["prim2c"], (int(P.nx) + 2 * NG, int(P.ny) + 2 * NG, int(P.nz) + 2 * NG), U, JArray(Q.astype(np.float64)))
+    return U.a
+
+
+def local_dt(module_path, P, Q: np.ndarray, metrics, J) -> np.ndarray:
+    """compute_dt (utils.jl:73-99) with LTS_CFL = P.lts_cfl: the per-cell time step at the
+    interior (zero elsewhere)."""
+    k = kernels(module_path, P)
+    k["LTS_CFL"] = float(P.lts_cfl)
+    m, S, Jj = _metric_arrays(metrics, J)
+    dt = JArray(np.zeros(Q.shape[1:]))
+    ext = (int(P.nx) + 2 * NG, int(P.ny) + 2 * NG, int(P.nz) + 2 * NG)
+    launch(k["compute_dt"], ext, dt, JArray(Q.astype(np.float64)), Jj, *S)
+    return dt.a
+
+
+def filter_pass(module_path, P, U: np.ndarray, Q: np.ndarray) -> np.ndarray:
+    """One filtering pass of time_step (solver.jl:446-470) over U: per direction, Un = U, then
+    the pressure sensor pre_d and the shock-capturing filter_d (P.filter 2) or the linear
+    linearFilter_d (P.filter 1) with filtering_s0 = P.filter_s0, filtering_rth = P.filter_rth."""
+    k = kernels(module_path, P)
+    ext = (int(P.nx) + 2 * NG, int(P.ny) + 2 * NG, int(P.nz) + 2 * NG)
+    Uj, Qj = JArray(U.astype(np.float64).copy()), JArray(Q.astype(np.float64))
+    sc = JArray(np.zeros(Q.shape[1:]))
+    s0, rth = float(P.filter_s0), float(P.filter_rth)
+    for d in "xyz":
+        Un = JArray(Uj.a.copy())
+        if int(P.filter) == 2:
+            launch(k["pre_" + d], ext, Qj, sc, rth)
+            launch(k["filter_" + d], ext, Uj, Un, sc, s0)
+        else:
+            launch(k["linearFilter_" + d], ext, Uj, Un, s0)
+    return Uj.a
 
 
 SPLITS = ("fluxSplit_SW", "fluxSplit_LF", "fluxSplit_VL", "fluxSplit_AUSM")

@@ -7,7 +7,8 @@ Julia kernels translated mechanically into Python (oracle/ref_jl/jl2py.py) and r
 - three viscous cases made here the same way (curvilinear random states, Sutherland viscosity
   large enough for the viscous terms to matter), whose inputs are stored too;
 and, for the cases with boundary.jl's own boundary set, the reference's prim2c, c2Prim with
-the ghost fill, and two SSP-RK3 steps (the stage loop of solver.jl).
+the ghost fill, and two SSP-RK3 steps (the stage loop of solver.jl); for the viscous cases its
+local time step and one pass of each filter.
 The file also records SHA-256 digests of the translated Julia files and of the generated
 module. Needs the reference tree (read only):
 
@@ -29,6 +30,7 @@ ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
 from flame3d_mhd_gb300.abi import BC_PERIODIC, make_params  # noqa: E402
+from flame3d_mhd_gb300.cases import params_copy  # noqa: E402
 from oracle import np_oracle as npo  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 from oracle.ref_jl import jl2py, runtime  # noqa: E402
@@ -106,6 +108,11 @@ def main() -> None:
         report[name] = r
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, Q, m, J, name))
+        # the local time step (utils.jl:73-99) and the two filters (solver.jl:446-470)
+        U = runtime.prim2c(module, P, Q)
+        out[f"{name}__local_dt"] = runtime.local_dt(module, P, Q, m, J)
+        for filt, label in ((1, "linear"), (2, "shock")):
+            out[f"{name}__U_filter_{label}"] = runtime.filter_pass(module, params_copy(P, filter=filt), U, Q)
     np.savez_compressed(HERE / "jl_reference_rhs.npz", **out)
     for name, r in report.items():
         print(name, "max |rhs|", float(np.abs(r[I]).max()))

@@ -74,6 +74,23 @@ def test_oracle_state_ghosts_and_steps_equal_the_translated_reference(name):
     assert np.array_equal(Us, d[f"{name}__U_rk3"]) and np.array_equal(Qs, d[f"{name}__Q_rk3"])
 
 
+@pytest.mark.parametrize("name", [n for n in _cases()[1] if f"{n}__local_dt" in _cases()[0].files])
+def test_oracle_local_dt_and_filters_equal_the_translated_reference(name):
+    """compute_dt (utils.jl:73-99) and one pass of the linear and of the shock-capturing filter
+    (solver.jl:446-470, utils.jl:102-315): bit for bit."""
+    from flame3d_mhd_gb300.cases import params_copy
+    d, _ = _cases()
+    meta, Q, m, J = _inputs(d, name)
+    P = make_params(*meta["n"], **meta["params"])
+    assert np.array_equal(orc.local_dt(P, Q, list(m), J), d[f"{name}__local_dt"])
+    U = orc.prim2c(P, Q)
+    for filt, label in ((1, "linear"), (2, "shock")):
+        Uf, Un = U.copy(), np.zeros_like(U)
+        orc.filter_pass(params_copy(P, filter=filt), Uf, Un, Q)
+        ref = d[f"{name}__U_filter_{label}"]
+        assert not np.array_equal(ref, U) and np.array_equal(Uf, ref), label
+
+
 def test_fixture_covers_the_forms():
     d, names = _cases()
     forms = set()
