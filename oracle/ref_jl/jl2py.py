@@ -177,8 +177,64 @@ def _literal_powers(s: str) -> str:
         s = s[:start] + f"_p{m.group(1)}({s[start:end]})" + s[m.end():]
 
 
+def _ranges_in_brackets(s: str) -> str:
+    """Inside [...] subscripts: `a:b` -> `_r(a, b)` and a bare `:` -> `_all` (Julia slices)."""
+    out, i = [], 0
+    while i < len(s):
+        ch = s[i]
+        if ch == "[" and i > 0 and (s[i - 1].isalnum() or s[i - 1] in "_]" or ord(s[i - 1]) > 127):
+            depth, j = 0, i
+            while j < len(s):
+                if s[j] in "([{":
+                    depth += 1
+                elif s[j] in ")]}":
+                    depth -= 1
+                    if depth == 0:
+                        break
+                j += 1
+            inner = _ranges_in_brackets(s[i + 1:j])
+            parts, cur, d = [], "", 0
+            for c in inner:
+                if c in "([{":
+                    d += 1
+                elif c in ")]}":
+                    d -= 1
+                if c == "," and d == 0:
+                    parts.append(cur)
+                    cur = ""
+                else:
+                    cur += c
+            parts.append(cur)
+            conv = []
+            for part in parts:
+                t, d, colon = part, 0, None
+                for k, c in enumerate(t):
+                    if c in "([{":
+                        d += 1
+                    elif c in ")]}":
+                        d -= 1
+                    elif c == ":" and d == 0:
+                        colon = k
+                        break
+                if colon is None:
+                    conv.append(t)
+                elif not t.strip() or t.strip() == ":":
+                    conv.append("_all")
+                else:
+                    conv.append(f"_r({t[:colon].strip()}, {t[colon + 1:].strip()})")
+            out.append("[" + ", ".join(c.strip() for c in conv) + "]")
+            i = j + 1
+            continue
+        out.append(ch)
+        i += 1
+    return "".join(out)
+
+
 def expr(s: str) -> str:
     s = s.replace("CUDA.eps(Float32)", "_eps32()")
+    s = re.sub(r"\bzeros\(\s*Float(32|64)\s*,", "_zeros(", s)
+    if ":" in s and "[" in s:
+        s = _ranges_in_brackets(s)
     s = re.sub(r"MMatrix\{\s*([^,}]+)\s*,\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1, \2)", s)
     s = re.sub(r"MVector\{\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1)", s)
     s = re.sub(r"(\d+\.\d*|\.\d+|\d+)f(-?\d+)", r"\1e\2", s)          # Float32 literals
@@ -301,11 +357,85 @@ def translate(src: str) -> str:
     return "\n".join(fixed) + "\n"
 
 
+def translate_script(src: str, first: int, last: int) -> str:
+    """Python of the top-level statements of lines first..last (1-based) of a Julia script:
+    function definitions, assignments, `@.` broadcasts (-> _bset(lhs, rhs), elementwise on whole
+    arrays, the same operations per element), loops `for k ∈ a:b, j ∈ c:d, ...` (nested, the
+    first variable outermost) and ifs."""
+    lines = src.splitlines()[first - 1:last]
+    out: list[str] = []
+    stack: list[int] = []  # indentation levels opened by each block
+    depth = lambda: sum(stack)
+    last_expr = None
+    in_fun = []
+    for raw in logical_lines("\n".join(lines)):
+        s = _strip_macros(raw)
+        if s != "end":
+            last_expr = None
+        if s == "end":
+            n = stack.pop()
+            if in_fun and len(stack) == in_fun[-1]:
+                if last_expr is not None:
+                    out[last_expr] = "    " * (depth() + 1) + "return " + out[last_expr].strip()
+                in_fun.pop()
+            last_expr = None
+            continue
+        pad = "    " * depth()
+        m = re.match(r"function\s+(\w+)\s*\((.*)\)\s*$", s)
+        if m:
+            out.append(pad + f"def {m.group(1)}({_strip_annot(m.group(2))}):")
+            in_fun.append(len(stack))
+            stack.append(1)
+            continue
+        m = re.match(r"for\s+(.*)$", s)
+        if m:
+            specs = [t.strip() for t in re.split(r",(?![^()\[\]]*[)\]])", m.group(1))]
+            for k, spec in enumerate(specs):
+                v, rng = re.split(r"\s*(?:∈|=|\bin\b)\s*", spec, maxsplit=1)
+                a, b = rng.split(":", 1)
+                out.append("    " * (depth() + k) + f"for {v} in range({expr(a)}, ({expr(b)}) + 1):")
+            stack.append(len(specs))
+            continue
+        m = re.match(r"if\s+(.*)$", s)
+        if m:
+            out.append(pad + f"if {expr(m.group(1))}:")
+            stack.append(1)
+            continue
+        if s.startswith("return"):
+            rest = s[len("return"):].strip()
+            out.append(pad + ("return" if not rest else f"return {expr(rest)}"))
+            continue
+        m = re.match(r"@\.\s*(.+?)\s*=(?!=)\s*(.+)$", s)
+        if m:
+            out.append(pad + f"_bset({expr(m.group(1))}, {expr(m.group(2))})")
+            continue
+        m = re.match(r"([^=<>!]+?)\s*=(?!=)\s*(.+)$", s)
+        if m:
+            out.append(pad + f"{expr(_strip_annot(m.group(1)))} = {expr(m.group(2))}")
+            continue
+        out.append(pad + expr(s))
+        if in_fun and len(stack) == in_fun[-1] + 1:
+            last_expr = len(out) - 1
+    if stack:
+        raise ValueError(f"unterminated blocks: {stack}")
+    return "\n".join(out) + "\n"
+
+
+# the metric and Jacobian computation of parse_mesh.jl (its CD6 / CD2 stencils of the
+# coordinates, J and the J^-1-scaled metrics), without the file output that follows
+METRIC_LINES = (139, 248)
+
+
 def translate_tree(root: Path) -> str:
     parts = ["# Generated by oracle/ref_jl/jl2py.py from the reference's Julia kernels; do not edit.\n"]
     for name in FILES:
         parts.append(f"# ---- {name}\n")
         parts.append(translate((root / name).read_text()))
+    a, b = METRIC_LINES
+    parts.append(f"# ---- parse_mesh.jl:{a}-{b}, as the body of _metrics()\n")
+    body = translate_script((root / "parse_mesh.jl").read_text(), a, b)
+    parts.append("def _metrics(x, y, z):\n" + "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) +
+                 "    return (dξdx, dξdy, dξdz, dηdx, dηdy, dηdz, dζdx, dζdy, dζdz), J\n")
     return "\n".join(parts)
 
 

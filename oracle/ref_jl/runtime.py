@@ -13,7 +13,8 @@ and run.jl gave them:
   the reconstruction of each direction (solver.jl:133-188), the viscous fluxes and div
   (solver.jl:429) with U = 0 and dt = 1, so U ends holding J times the flux divergence, the RHS;
 - prim2c, c2Prim and the ghost fill of one process for boundary.jl's own boundary set, the
-  RK3 stage loop of time_step, its local time step and its filtering pass.
+  RK3 stage loop of time_step, its local time step and its filtering pass;
+- the metrics and J of parse_mesh.jl (a script, translated as the body of one function).
 
 Every value is a Python float (binary64): the reference's algorithm in FP64, in its own
 operation order. Slow (one Python call per thread): grids of a few hundred cells.
@@ -30,27 +31,65 @@ import numpy as np
 NG = 4
 
 
+class _Range:
+    """Julia's a:b in a subscript (inclusive, 1-based)."""
+
+    __slots__ = ("lo", "hi")
+
+    def __init__(self, lo, hi):
+        self.lo, self.hi = lo, hi
+
+
+_ALL = _Range(None, None)
+
+
+def _py_index(x):
+    if isinstance(x, _Range):
+        return slice(None if x.lo is None else x.lo - 1, x.hi)
+    return x - 1
+
+
 class JArray:
-    """A[i, j, k, n] (1-based, Julia's order) over a numpy array stored [n, k, j, i]."""
+    """A[i, j, k, n] (1-based, Julia's order) over a numpy array stored [n, k, j, i]; a:b and :
+    subscripts give JArray views; arithmetic on whole arrays is elementwise (Julia's @.)."""
 
     __slots__ = ("a",)
 
     def __init__(self, a: np.ndarray):
         self.a = a
 
+    def _key(self, idx):
+        idx = idx if isinstance(idx, tuple) else (idx,)
+        return tuple(_py_index(x) for x in reversed(idx)), any(isinstance(x, _Range) for x in idx)
+
     def __getitem__(self, idx):
-        if not isinstance(idx, tuple):
-            return float(self.a[idx - 1])
-        return float(self.a[tuple(x - 1 for x in reversed(idx))])
+        key, sliced = self._key(idx)
+        return JArray(self.a[key]) if sliced else float(self.a[key])
 
     def __setitem__(self, idx, v):
-        if not isinstance(idx, tuple):
-            self.a[idx - 1] = v
-        else:
-            self.a[tuple(x - 1 for x in reversed(idx))] = v
+        key, _ = self._key(idx)
+        self.a[key] = v.a if isinstance(v, JArray) else v
 
     def _fill(self, v):
         self.a[...] = v
+
+    # elementwise arithmetic (the fused broadcasts of @. evaluate the same operations per element)
+    def _o(self, x):
+        return x.a if isinstance(x, JArray) else x
+
+    def __add__(self, x): return self.a + self._o(x)
+    def __radd__(self, x): return self._o(x) + self.a
+    def __sub__(self, x): return self.a - self._o(x)
+    def __rsub__(self, x): return self._o(x) - self.a
+    def __mul__(self, x): return self.a * self._o(x)
+    def __rmul__(self, x): return self._o(x) * self.a
+    def __truediv__(self, x): return self.a / self._o(x)
+    def __rtruediv__(self, x): return self._o(x) / self.a
+    def __neg__(self): return -self.a
+
+
+def _bset(lhs, v):
+    lhs.a[...] = v.a if isinstance(v, JArray) else v
 
 
 _thread = SimpleNamespace(x=1, y=1, z=1)
@@ -85,6 +124,8 @@ HELPERS = dict(
     ifelse=lambda c, a, b: a if c else b, zero=lambda a: 0.0,
     _eps32=lambda: 2.0 ** -23, _mat=_mat, _f32=float, _f64=float,
     _p2=lambda x: x * x, _p3=lambda x: x * x * x,  # Julia's literal powers (Base.literal_pow)
+    _r=_Range, _all=_ALL, _bset=_bset,
+    _zeros=lambda *dims: JArray(np.zeros(tuple(reversed(dims)))),
 )
 
 
@@ -102,6 +143,8 @@ def kernels(module_path: Path | str, P) -> dict:
         "hybrid_ϕ1": float(P.phi1), "hybrid_ϕ2": float(P.phi2), "hybrid_ϕ3": float(P.phi3),
         "Linear": JArray(np.array([u * lp + c * (1.0 - lp) for u, c in zip(up7, cd6)])),
         "LES_smag": False, "LES_wale": False,
+        "Nx": int(P.nx), "Ny": int(P.ny), "Nz": int(P.nz),
+        "Nx_tot": int(P.nx) + 2 * NG, "Ny_tot": int(P.ny) + 2 * NG, "Nz_tot": int(P.nz) + 2 * NG,
     })
     # Python reads identifiers NFKC-normalised (the ϕ of hybrid_ϕ1 becomes φ): so must the names
     g = {unicodedata.normalize("NFKC", name): v for name, v in g.items()}
@@ -210,6 +253,14 @@ def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int
             launch(k["c2Prim"], ext, U, Q)
             k["fillGhost"](Q, U, 0, 0)
     return U.a, Q.a
+
+
+def metrics(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray):
+    """parse_mesh.jl:139-248 on the coordinates with ghosts: the nine J^-1-scaled metrics
+    (dξ/dx, dξ/dy, dξ/dz, dη/dx, ..., dζ/dz) and J, each (Nz_tot, Ny_tot, Nx_tot)."""
+    k = kernels(module_path, P)
+    m, J = k["_metrics"](*(JArray(np.asarray(c, dtype=np.float64)) for c in (x, y, z)))
+    return np.stack([a.a for a in m]), J.a
 
 
 def prim2c(module_path, P, Q: np.ndarray) -> np.ndarray:

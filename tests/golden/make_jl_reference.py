@@ -8,7 +8,9 @@ Julia kernels translated mechanically into Python (oracle/ref_jl/jl2py.py) and r
   large enough for the viscous terms to matter), whose inputs are stored too;
 and, for the cases with boundary.jl's own boundary set, the reference's prim2c, c2Prim with
 the ghost fill, and two SSP-RK3 steps (the stage loop of solver.jl); for the viscous cases its
-local time step and one pass of each filter.
+local time step and one pass of each filter; for every case a SHA-256 of the metrics and J of
+parse_mesh.jl:139-248 from the coordinates (the arrays themselves are those stored with the
+inputs).
 The file also records SHA-256 digests of the translated Julia files and of the generated
 module. Needs the reference tree (read only):
 
@@ -31,7 +33,6 @@ sys.path.insert(0, str(ROOT))
 
 from flame3d_mhd_gb300.abi import BC_PERIODIC, make_params  # noqa: E402
 from flame3d_mhd_gb300.cases import params_copy  # noqa: E402
-from oracle import np_oracle as npo  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 from oracle.ref_jl import jl2py, runtime  # noqa: E402
 
@@ -48,6 +49,14 @@ VISCOUS = {
         character=1, viscous=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0), seed=37, spikes=4),
 }
 RK3_DT, RK3_STEPS = 2e-4, 2
+
+
+def metrics_digest(m, J) -> str:
+    """SHA-256 of the nine metrics and J as little-endian binary64."""
+    h = hashlib.sha256()
+    for a in (*m, J):
+        h.update(np.ascontiguousarray(a, dtype="<f8").tobytes())
+    return h.hexdigest()
 
 
 def _golden():
@@ -88,6 +97,8 @@ def main() -> None:
         P = make_params(*meta["n"], **meta["params"])
         r = runtime.rhs(module, P, d["Q"], d["metrics"], d["J"])
         out[f"{f.stem}__rhs"] = r
+        mr, Jr = runtime.metrics(module, P, d["x"], d["y"], d["z"])  # parse_mesh.jl:139-248
+        out[f"{f.stem}__metrics_sha256"] = np.array(metrics_digest(mr, Jr))
         report[f.stem] = r
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, d["Q"], d["metrics"], d["J"], f.stem))
@@ -99,11 +110,12 @@ def main() -> None:
         Q = g.initial(P, n, spec["seed"], spec["spikes"], False, x, y, z)
         U = orc.prim2c(P, Q)
         orc.fill_ghosts(P, Q, U)
-        m, J = npo.metrics(x, y, z)
-        m = np.stack(m)
+        m, J = runtime.metrics(module, P, x, y, z)  # the reference's own metrics (parse_mesh.jl:139-248)
         r = runtime.rhs(module, P, Q, m, J)
         meta = dict(n=list(n), params=params)
         out.update({f"{name}__Q": Q, f"{name}__metrics": m, f"{name}__J": J, f"{name}__rhs": r,
+                    f"{name}__x": x, f"{name}__y": y, f"{name}__z": z,
+                    f"{name}__metrics_sha256": np.array(metrics_digest(m, J)),
                     f"{name}__meta": np.array(json.dumps(meta))})
         report[name] = r
         if runtime.is_reference_bcs(P):

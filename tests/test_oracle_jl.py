@@ -91,6 +91,29 @@ def test_oracle_local_dt_and_filters_equal_the_translated_reference(name):
         assert not np.array_equal(ref, U) and np.array_equal(Uf, ref), label
 
 
+def _digest(m, J):
+    import hashlib
+    h = hashlib.sha256()
+    for a in (*m, J):
+        h.update(np.ascontiguousarray(a, dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name", _cases()[1])
+def test_oracle_metrics_equal_the_translated_reference(name):
+    """The nine J^-1-scaled metrics and J of parse_mesh.jl:139-248 (CD6 inside, one-sided CD2
+    in the outer three layers): bit for bit."""
+    d, _ = _cases()
+    meta = _inputs(d, name)[0]
+    P = make_params(*meta["n"], **meta["params"])
+    src = d if f"{name}__x" in d.files else np.load(ROOT / "tests" / "golden" / f"{name}.npz", allow_pickle=True)
+    pre = f"{name}__" if src is d else ""
+    m, J = orc.metrics(P, src[pre + "x"], src[pre + "y"], src[pre + "z"])
+    assert _digest(m, J) == str(d[f"{name}__metrics_sha256"])
+    # the metrics the RHS cases were computed from are these
+    assert _digest(src[pre + "metrics"], src[pre + "J"]) == str(d[f"{name}__metrics_sha256"])
+
+
 def test_fixture_covers_the_forms():
     d, names = _cases()
     forms = set()
