@@ -43,18 +43,24 @@ __global__ void k_face_geometry(const DevParams P, const double* __restrict__ X,
     const long long sa = DIR == 0 ? sy : 1;             // transverse a: y for x faces, else x
     const long long sb = DIR == 2 ? sy : sz;            // transverse b: z, except y for z faces
     const long long c = lin3(P, i, j, k);
-    auto corner_sum = [&](const double* A, int pa, int pb) {
-        double s = 0.0;
-        for (int side = 0; side < 2; side++) {
-            const long long o = c + side * sd;
-            s = __dadd_rn(s, A[o + pa * sa]);
-            s = __dadd_rn(s, A[o + pb * sb]);
-            s = __dadd_rn(s, A[o + pa * sa + pb * sb]);
-        }
-        return s;
-    };
+    // the cell at pa a + pb b from the face's left (side 0) or right (side 1) cell
+    auto at = [&](const double* A, int pa, int pb, int side) { return A[c + side * sd + pa * sa + pb * sb]; };
+    // 0.125 x the twelve centres summed left to right in the order of FVM.jl:16-21 (and the
+    // j, k kernels): (pa,0), (0,pb), (pa,pb), each on both sides, then (-pa,0), (0,-pb),
+    // (-pa,-pb) subtracted
     auto diag = [&](const double* A, int pa, int pb) {
-        return __dmul_rn(0.125, __dadd_rn(corner_sum(A, pa, pb), -corner_sum(A, -pa, -pb)));
+        double s = __dadd_rn(at(A, pa, 0, 0), at(A, pa, 0, 1));
+        s = __dadd_rn(s, at(A, 0, pb, 0));
+        s = __dadd_rn(s, at(A, 0, pb, 1));
+        s = __dadd_rn(s, at(A, pa, pb, 0));
+        s = __dadd_rn(s, at(A, pa, pb, 1));
+        s = __dsub_rn(s, at(A, -pa, 0, 0));
+        s = __dsub_rn(s, at(A, -pa, 0, 1));
+        s = __dsub_rn(s, at(A, 0, -pb, 0));
+        s = __dsub_rn(s, at(A, 0, -pb, 1));
+        s = __dsub_rn(s, at(A, -pa, -pb, 0));
+        s = __dsub_rn(s, at(A, -pa, -pb, 1));
+        return __dmul_rn(0.125, s);
     };
     const double dx1 = diag(X, 1, 1), dy1 = diag(Y, 1, 1), dz1 = diag(Z, 1, 1);
     const double dx2 = diag(X, -1, 1), dy2 = diag(Y, -1, 1), dz2 = diag(Z, -1, 1);

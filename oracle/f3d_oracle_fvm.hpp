@@ -141,20 +141,29 @@ void fvm_face_geometry(int d, const V4<const R>& X, const V4<const R>& Y, const 
     const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
     da[a] = 1;
     db[b] = 1;
-    auto corner_sum = [&](const V4<const R>& A, int sa, int sb) {
-        // the three cells at (+-a, 0), (0, +-b), (+-a, +-b) around the face, on both sides
-        R s = R(0);
-        for (int side = 0; side < 2; side++) {
-            const long oi = side ? di[0] : 0, oj = side ? di[1] : 0, ok = side ? di[2] : 0;
-            s += A(i + oi + sa * da[0], j + oj + sa * da[1], k + ok + sa * da[2]);
-            s += A(i + oi + sb * db[0], j + oj + sb * db[1], k + ok + sb * db[2]);
-            s += A(i + oi + sa * da[0] + sb * db[0], j + oj + sa * da[1] + sb * db[1], k + ok + sa * da[2] + sb * db[2]);
-        }
-        return s;
+    // the cell at (pa a + pb b) from the face's left cell (side 0) or right cell (side 1)
+    auto at = [&](const V4<const R>& A, int pa, int pb, int side) -> R {
+        return A(i + side * di[0] + pa * da[0] + pb * db[0], j + side * di[1] + pa * da[1] + pb * db[1],
+                 k + side * di[2] + pa * da[2] + pb * db[2]);
     };
-    // d1 = P(+a,+b) - P(-a,-b), d2 = P(-a,+b) - P(+a,-b), each corner the mean of 8 cells
-    auto diag = [&](const V4<const R>& A, int s1a, int s1b) {
-        return R(0.125) * (corner_sum(A, s1a, s1b) - corner_sum(A, -s1a, -s1b));
+    // d1 = P(+a,+b) - P(-a,-b), d2 = P(-a,+b) - P(+a,-b), each corner the mean of 8 cells: the
+    // twelve centres summed left to right in the kernels' order (FVM.jl:16-21, 251-256,
+    // 466-471): (sa,0), (0,sb), (sa,sb), each on both sides, then (-sa,0), (0,-sb), (-sa,-sb)
+    // subtracted
+    auto diag = [&](const V4<const R>& A, int sa, int sb) {
+        R s = at(A, sa, 0, 0);
+        s += at(A, sa, 0, 1);
+        s += at(A, 0, sb, 0);
+        s += at(A, 0, sb, 1);
+        s += at(A, sa, sb, 0);
+        s += at(A, sa, sb, 1);
+        s -= at(A, -sa, 0, 0);
+        s -= at(A, -sa, 0, 1);
+        s -= at(A, 0, -sb, 0);
+        s -= at(A, 0, -sb, 1);
+        s -= at(A, -sa, -sb, 0);
+        s -= at(A, -sa, -sb, 1);
+        return R(0.125) * s;
     };
     const R dx1 = diag(X, 1, 1), dy1 = diag(Y, 1, 1), dz1 = diag(Z, 1, 1);
     const R dx2 = diag(X, -1, 1), dy2 = diag(Y, -1, 1), dz2 = diag(Z, -1, 1);

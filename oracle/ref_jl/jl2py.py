@@ -3,19 +3,20 @@
 The reference's hot path is Julia (CUDA.jl kernels) and no Julia is available, so the oracle
 (oracle/f3d_oracle.hpp) is a restatement written by hand. To check that restatement against
 the reference's own source, this script translates the kernel files (split.jl, schemes.jl,
-viscous.jl, div.jl, utils.jl, boundary.jl) statement by statement, with fixed rules and no
-hand edits:
+viscous.jl, div.jl, utils.jl, boundary.jl, FVM.jl) statement by statement, with fixed rules
+and no hand edits:
 
 - comments dropped; a line ending in an operator, a comma or an open bracket continues;
   ';' separates statements;
-- `function f(args)` .. `end`, `if` / `elseif` / `else`, `for v = a:b` become Python blocks; a
-  bare expression ending a function body is returned, as Julia returns it;
+- `function f(args)` .. `end`, `if` / `elseif` / `else`, `for v = a:b` become Python blocks
+  (`begin` .. `end` adds none); a bare expression ending a function body is returned, as
+  Julia returns it;
 - `@inbounds`, `@fastmath`, `@inline` and type annotations (`x::Float32 = ...`) are dropped;
 - literals: `12f0` -> `12e0`, `1i32` -> `1`, implicit products `547V1` -> `547*V1`;
 - `x^2` / `x^3` -> `_p2(x)` / `_p3(x)` (products, as Julia's literal powers), other `^` -> `**`,
   `&&` / `||` / `!` -> `and` / `or` / `not`, `c ? a : b` -> `(a if c else b)`,
-  `x .= v` -> `x._fill(v)`, `MMatrix{n, m, ...}(undef)` / `MVector{n, ...}(undef)` -> 1-based
-  arrays, `@cuda <keywords> f(args)` -> `_cuda(f, args)` (a launch the runtime runs over the
+  `x .= v` -> `x._fill(v)`, `MMatrix{n, m, ...}(undef)` / `MVector{n, ...}(undef)` /
+  `SVector{...}(values)` -> 1-based arrays, `@cuda <keywords> f(args)` -> `_cuda(f, args)` (a launch the runtime runs over the
   grid), `CUDA.eps(Float32)` -> 2^-23, `÷` -> `//`, a character Julia allows in names and
   Python does not (the ∂ of ∂ξ∂x) -> `_u2202_`;
 - array indexing is left as written: the runtime (runtime.py) passes arrays that take
@@ -27,7 +28,11 @@ algorithm evaluated in FP64 in the reference's own operation order, the form the
 restates. The generated module is written next to the compiled reference program
 (oracle/_ref/, not tracked).
 
-    python -m oracle.ref_jl.jl2py <reference root> [out.py]
+`translate_tree(root, corrected=True)` first applies CORRECTIONS, two defects of FVM.jl
+repaired by exact text substitutions, each of which must match the stated number of times;
+everything else is translated as written.
+
+    python -m oracle.ref_jl.jl2py <reference root> [out.py] [--corrected]
 """
 from __future__ import annotations
 
@@ -35,7 +40,36 @@ import re
 import sys
 from pathlib import Path
 
-FILES = ("split.jl", "schemes.jl", "viscous.jl", "div.jl", "utils.jl", "boundary.jl")
+FILES = ("split.jl", "schemes.jl", "viscous.jl", "div.jl", "utils.jl", "boundary.jl", "FVM.jl")
+
+# (file, region from / to (text markers, None = file start / end), pattern, replacement,
+#  matches, why)
+CORRECTIONS = (
+    ("FVM.jl", None, "function Conser_reconstruct_i", r"\bv2 = -1\.0f0\*V3([LR])", r"v2c = -1.0f0*V3\1", 6,
+     "Eigen_reconstruct_i/j/k, WENO5 branch (FVM.jl:178, 198, 399, 414, 615, 630): the candidate v2 "
+     "reuses the name of the Roe-averaged kinetic energy v2 (FVM.jl:73, 310, 526), a local of the "
+     "enclosing function, so the loop body assigns that variable and the right-eigenvector row of "
+     "field 2 (rn5 = v2, FVM.jl:211, 426, 642) reads the candidate on WENO5 faces"),
+    ("FVM.jl", None, "function Conser_reconstruct_i", r"α2([LR])\*v2 \+", r"α2\1*v2c +", 6,
+     "the renamed candidate's uses (FVM.jl:181, 201, 401, 416, 617, 632)"),
+    ("FVM.jl", "function Conser_reconstruct_j", None, r"= U[LR]_final_\d#(flux_temp\[\d\] \* Area)", r"= \1", 10,
+     "Conser_reconstruct_j/k (FVM.jl:1037-1041, 1215-1219) store the reconstructed states, the "
+     "flux flux_temp[n] * Area commented out after them"),
+)
+
+
+def apply_corrections(name: str, src: str) -> str:
+    """src with every correction of file `name` applied; a count that differs raises."""
+    for f, a, b, pat, rep, count, _ in CORRECTIONS:
+        if f != name:
+            continue
+        i0 = src.index(a) if a else 0
+        i1 = src.index(b) if b else len(src)
+        region, n = re.subn(pat, rep, src[i0:i1])
+        if n != count:
+            raise ValueError(f"{name}: {pat!r} matched {n} times, expected {count}")
+        src = src[:i0] + region + src[i1:]
+    return src
 
 _OPEN = "([{"
 _CLOSE = ")]}"
@@ -237,6 +271,7 @@ def expr(s: str) -> str:
         s = _ranges_in_brackets(s)
     s = re.sub(r"MMatrix\{\s*([^,}]+)\s*,\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1, \2)", s)
     s = re.sub(r"MVector\{\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1)", s)
+    s = re.sub(r"SVector\{[^}]*\}\s*\(", "_vec(", s)
     s = re.sub(r"(\d+\.\d*|\.\d+|\d+)f(-?\d+)", r"\1e\2", s)          # Float32 literals
     s = re.sub(r"(?<![\w.])(\d+)i32\b", r"\1", s)                       # Int32 literals
     # implicit products: a numeric literal (possibly with exponent) followed by a name or '('
@@ -286,7 +321,7 @@ def translate(src: str) -> str:
     """Python source of every function of a Julia kernel file (top-level code is skipped)."""
     out: list[str] = []
     stack: list[str] = []
-    pad = lambda: "    " * len(stack)
+    pad = lambda: "    " * sum(k != "begin" for k in stack)  # begin .. end adds no indentation
     last_expr = None  # index in out of the function body's last statement if it is a bare expression
     for raw in logical_lines(src):
         s = _strip_macros(raw)
@@ -309,6 +344,9 @@ def translate(src: str) -> str:
             continue
         if re.match(r"function\b", s):
             raise ValueError(f"nested function: {s}")
+        if s == "begin":
+            stack.append("begin")
+            continue
         m = re.match(r"if\s+(.*)$", s)
         if m:
             out.append(pad() + f"if {expr(m.group(1))}:")
@@ -316,10 +354,10 @@ def translate(src: str) -> str:
             continue
         m = re.match(r"elseif\s+(.*)$", s)
         if m:
-            out.append("    " * (len(stack) - 1) + f"elif {expr(m.group(1))}:")
+            out.append(pad()[4:] + f"elif {expr(m.group(1))}:")
             continue
         if s == "else":
-            out.append("    " * (len(stack) - 1) + "else:")
+            out.append(pad()[4:] + "else:")
             continue
         m = re.match(r"for\s+(\w+)\s*(?:=|in)\s*(.+?)\s*:\s*(.+)$", s)
         if m:
@@ -426,11 +464,14 @@ def translate_script(src: str, first: int, last: int) -> str:
 METRIC_LINES = (139, 248)
 
 
-def translate_tree(root: Path) -> str:
+def translate_tree(root: Path, corrected: bool = False) -> str:
     parts = ["# Generated by oracle/ref_jl/jl2py.py from the reference's Julia kernels; do not edit.\n"]
+    if corrected:
+        parts.append("# With CORRECTIONS applied (FVM.jl).\n")
     for name in FILES:
+        src = (root / name).read_text()
         parts.append(f"# ---- {name}\n")
-        parts.append(translate((root / name).read_text()))
+        parts.append(translate(apply_corrections(name, src) if corrected else src))
     a, b = METRIC_LINES
     parts.append(f"# ---- parse_mesh.jl:{a}-{b}, as the body of _metrics()\n")
     body = translate_script((root / "parse_mesh.jl").read_text(), a, b)
@@ -441,10 +482,12 @@ def translate_tree(root: Path) -> str:
 
 def main(argv=None) -> None:
     argv = sys.argv[1:] if argv is None else argv
+    corrected = "--corrected" in argv
+    argv = [a for a in argv if a != "--corrected"]
     root = Path(argv[0])
     out = Path(argv[1]) if len(argv) > 1 else Path(__file__).resolve().parent.parent / "_ref" / "jl_kernels.py"
     out.parent.mkdir(parents=True, exist_ok=True)
-    out.write_text(translate_tree(root))
+    out.write_text(translate_tree(root, corrected))
     print(out)
 
 

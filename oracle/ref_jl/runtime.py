@@ -9,9 +9,10 @@ and run.jl gave them:
   zero, eps(Float32);
 - the global constants of run.jl:8-13, 57-77 (γ, Rg, Cp, C_s, T_s, Pr, Ncons, the hybrid
   thresholds, Linear, NG, Nxp, Nyp, Nzp) from an f3d_params;
-- the launch sequence of one finite-difference RHS: the sensor (solver.jl:424), the split and
-  the reconstruction of each direction (solver.jl:133-188), the viscous fluxes and div
-  (solver.jl:429) with U = 0 and dt = 1, so U ends holding J times the flux divergence, the RHS;
+- the launch sequence of one RHS: the sensor (solver.jl:424), the split and the
+  reconstruction of each direction (solver.jl:133-188) or, for the finite-volume schemes, the
+  face kernels of FVM.jl (solver.jl:21-31), the viscous fluxes and div (solver.jl:429) into a
+  zero accumulator with dt = 1, so it ends holding J times the flux divergence, the RHS;
 - prim2c, c2Prim and the ghost fill of one process for boundary.jl's own boundary set, the
   RK3 stage loop of time_step, its local time step and its filtering pass;
 - the metrics and J of parse_mesh.jl (a script, translated as the body of one function).
@@ -124,7 +125,7 @@ HELPERS = dict(
     ifelse=lambda c, a, b: a if c else b, zero=lambda a: 0.0,
     _eps32=lambda: 2.0 ** -23, _mat=_mat, _f32=float, _f64=float,
     _p2=lambda x: x * x, _p3=lambda x: x * x * x,  # Julia's literal powers (Base.literal_pow)
-    _r=_Range, _all=_ALL, _bset=_bset,
+    _r=_Range, _all=_ALL, _bset=_bset, _vec=lambda *v: JArray(np.array(v, dtype=np.float64)),
     _zeros=lambda *dims: JArray(np.zeros(tuple(reversed(dims)))),
 )
 
@@ -194,27 +195,45 @@ def state_and_ghosts(module_path, P, Q: np.ndarray):
     return U0, Q2.a, U.a
 
 
-def _advance(k, P, Qj, m, S, Jj, U, dt):
-    """The sensor, flowAdvance's finite-difference branch and div (U += dt J (...))."""
+def _advance(k, P, Qj, m, S, Jj, U, dt, xyz=None, Ustate=None):
+    """The sensor, flowAdvance (solver.jl:19-188) and div (U += dt J (...)). Finite-difference
+    schemes: split and reconstruction per direction. Finite-volume schemes (P.scheme 1:
+    Eigen_reconstruct_*, 2: Conser_reconstruct_*): the face kernels of solver.jl:21-31 on the
+    cell-centre coordinates xyz, reading Ustate (default U, the stage's state, which div then
+    updates, as in the reference)."""
     nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
     ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
     shape = Qj.a.shape[1:]
     phi = JArray(np.zeros(shape))
     launch(k["shockSensor"], ext, phi, Qj)
-    Fp, Fm = JArray(np.zeros((5, *shape))), JArray(np.zeros((5, *shape)))
     F = [JArray(np.zeros((5, nz, ny, nx + 1))), JArray(np.zeros((5, nz, ny + 1, nx))),
          JArray(np.zeros((5, nz + 1, ny, nx)))]
-    split = k[SPLITS[int(P.split_method)]]
-    for d, name in enumerate("xyz"):
-        launch(split, ext, Qj, Fp, Fm, S[d], m[3 * d], m[3 * d + 1], m[3 * d + 2])
-        if int(P.character):
-            launch(k["advect_" + name + "c"], ext, F[d], phi, S[d], Fp, Fm, Qj, m[3 * d], m[3 * d + 1], m[3 * d + 2])
-        else:
-            launch(k["advect_" + name], ext, F[d], phi, S[d], Fp, Fm, 5)
+    scheme = int(getattr(P, "scheme", 0))
+    if scheme:
+        name = "Eigen_reconstruct_" if scheme == 1 else "Conser_reconstruct_"
+        for d, suf in enumerate("ijk"):
+            launch(k[name + suf], ext, Qj, U if Ustate is None else Ustate, phi, S[d], F[d], *xyz)
+    else:
+        Fp, Fm = JArray(np.zeros((5, *shape))), JArray(np.zeros((5, *shape)))
+        split = k[SPLITS[int(P.split_method)]]
+        for d, name in enumerate("xyz"):
+            launch(split, ext, Qj, Fp, Fm, S[d], m[3 * d], m[3 * d + 1], m[3 * d + 2])
+            if int(P.character):
+                launch(k["advect_" + name + "c"], ext, F[d], phi, S[d], Fp, Fm, Qj, m[3 * d], m[3 * d + 1], m[3 * d + 2])
+            else:
+                launch(k["advect_" + name], ext, F[d], phi, S[d], Fp, Fm, 5)
     Fv = [JArray(np.zeros((4, nz + 4, ny + 4, nx + 4))) for _ in range(3)]
     if int(P.viscous):
         launch(k["viscousFlux"], ext, *Fv, Qj, *m, Jj)
     launch(k["div"], (nx, ny, nz), U, *F, *Fv, dt, Jj)
+
+
+def _coords(P, xyz):
+    if int(getattr(P, "scheme", 0)) == 0:
+        return None
+    if xyz is None:
+        raise ValueError("the finite-volume schemes need the cell-centre coordinates")
+    return [JArray(np.asarray(a, dtype=np.float64)) for a in xyz]
 
 
 def _metric_arrays(metrics, J):
@@ -224,7 +243,8 @@ def _metric_arrays(metrics, J):
     return m, S, JArray(J.astype(np.float64))
 
 
-def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int, Q0: np.ndarray | None = None):
+def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int, Q0: np.ndarray | None = None,
+              xyz=None):
     """nsteps SSP-RK3 steps of time_step's loop (solver.jl:416-444; no local time step, no
     filter) from the conserved state U0 and its ghost-filled primitive state Q0 (formed from U0
     as a stage forms it when not given), for boundary.jl's boundary set. Returns (U, Q)."""
@@ -234,6 +254,7 @@ def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int
     nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
     ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
     m, S, Jj = _metric_arrays(metrics, J)
+    xyz = _coords(P, xyz)
     U = JArray(U0.astype(np.float64).copy())
     if Q0 is None:
         Q = JArray(np.zeros((6, *U0.shape[1:])))
@@ -245,7 +266,7 @@ def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int
         for krk in (1, 2, 3):
             if krk == 1:
                 Un = JArray(U.a.copy())
-            _advance(k, P, Q, m, S, Jj, U, dt)
+            _advance(k, P, Q, m, S, Jj, U, dt, xyz)
             if krk == 2:
                 launch(k["linComb"], ext, U, Un, 5, 0.25, 0.75)
             elif krk == 3:
@@ -261,6 +282,28 @@ def metrics(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray):
     k = kernels(module_path, P)
     m, J = k["_metrics"](*(JArray(np.asarray(c, dtype=np.float64)) for c in (x, y, z)))
     return np.stack([a.a for a in m]), J.a
+
+
+def fvm_faces(module_path, P, Q: np.ndarray, metrics: np.ndarray, xyz):
+    """The finite-volume face fluxes of the three directions, each in the Fx / Fy / Fz shape,
+    as flowAdvance's finite-volume branch launches them (solver.jl:21-31): Eigen_reconstruct_*
+    (P.scheme 1) or Conser_reconstruct_* (2) of FVM.jl on the ghost-filled primitive state Q,
+    U = prim2c(Q) at every cell, the reference's sensor, the metric-row norms s1, s2, s3 and
+    the cell-centre coordinates xyz = (x, y, z)."""
+    k = kernels(module_path, P)
+    nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
+    ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
+    _, S, _ = _metric_arrays(metrics, np.zeros(1))
+    Qj = JArray(Q.astype(np.float64))
+    U, phi = JArray(np.zeros((5, *Q.shape[1:]))), JArray(np.zeros(Q.shape[1:]))
+    launch(k["prim2c"], ext, U, Qj)
+    launch(k["shockSensor"], ext, phi, Qj)
+    F = [JArray(np.zeros((5, nz, ny, nx + 1))), JArray(np.zeros((5, nz, ny + 1, nx))),
+         JArray(np.zeros((5, nz + 1, ny, nx)))]
+    name = "Eigen_reconstruct_" if int(P.scheme) == 1 else "Conser_reconstruct_"
+    for d, suf in enumerate("ijk"):
+        launch(k[name + suf], ext, Qj, U, phi, S[d], F[d], *_coords(P, xyz))
+    return [f.a for f in F]
 
 
 def prim2c(module_path, P, Q: np.ndarray) -> np.ndarray:
@@ -305,12 +348,19 @@ def filter_pass(module_path, P, U: np.ndarray, Q: np.ndarray) -> np.ndarray:
 SPLITS = ("fluxSplit_SW", "fluxSplit_LF", "fluxSplit_VL", "fluxSplit_AUSM")
 
 
-def rhs(module_path, P, Q: np.ndarray, metrics: np.ndarray, J: np.ndarray) -> np.ndarray:
-    """dU/dt at the interior (zero elsewhere) of the reference's finite-difference RHS from
-    the ghost-filled primitive state Q (6, Nt...), the nine J^-1-scaled metrics and J: the
-    advance of one stage with U = 0 and dt = 1."""
+def rhs(module_path, P, Q: np.ndarray, metrics: np.ndarray, J: np.ndarray, xyz=None) -> np.ndarray:
+    """dU/dt at the interior (zero elsewhere) of the reference's RHS from the ghost-filled
+    primitive state Q (6, Nt...), the nine J^-1-scaled metrics and J: the advance of one stage
+    into a zero accumulator with dt = 1. The finite-volume schemes reconstruct U = prim2c(Q)
+    (utils.jl:33-54, every cell) on the cell-centre coordinates xyz = (x, y, z)."""
     k = kernels(module_path, P)
     m, S, Jj = _metric_arrays(metrics, J)
+    Qj = JArray(Q.astype(np.float64))
+    xyz = _coords(P, xyz)
+    Ustate = None
+    if xyz is not None:
+        Ustate = JArray(np.zeros((5, *Q.shape[1:])))
+        launch(k["prim2c"], (int(P.nx) + 2 * NG, int(P.ny) + 2 * NG, int(P.nz) + 2 * NG), Ustate, Qj)
     U = JArray(np.zeros((5, *Q.shape[1:])))
-    _advance(k, P, JArray(Q.astype(np.float64)), m, S, Jj, U, 1.0)
+    _advance(k, P, Qj, m, S, Jj, U, 1.0, xyz, Ustate)
     return U.a

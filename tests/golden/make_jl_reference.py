@@ -10,9 +10,16 @@ and, for the cases with boundary.jl's own boundary set, the reference's prim2c, 
 the ghost fill, and two SSP-RK3 steps (the stage loop of solver.jl); for the viscous cases its
 local time step and one pass of each filter; for every case a SHA-256 of the metrics and J of
 parse_mesh.jl:139-248 from the coordinates (the arrays themselves are those stored with the
-inputs).
+inputs);
+- four finite-volume cases (FVM.jl, the reference's default scheme: Roe-characteristic and
+  component-wise reconstruction, inviscid and viscous; noise that grows along x and two
+  pressure spikes, so that faces of all four branches occur): the face fluxes of the three
+  directions, the RHS and, for boundary.jl's boundary set, two SSP-RK3 steps, from the
+  translation with jl2py.CORRECTIONS applied, and the face fluxes of the translation as
+  written (two defects of FVM.jl: the corrected and as-written translations differ on the
+  Roe-characteristic WENO5 faces and on the component-wise y and z faces only).
 The file also records SHA-256 digests of the translated Julia files and of the generated
-module. Needs the reference tree (read only):
+modules. Needs the reference tree (read only):
 
   python tests/golden/make_jl_reference.py --ref <reference tree>
 """
@@ -49,6 +56,31 @@ VISCOUS = {
         character=1, viscous=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0), seed=37, spikes=4),
 }
 RK3_DT, RK3_STEPS = 2e-4, 2
+FVM = {
+    "fvm_eigen_refbc": dict(n=(6, 5, 5), params=dict(scheme=1, viscous=0), seed=51),
+    "fvm_eigen_viscous_refbc": dict(n=(6, 5, 5), params=dict(scheme=1, viscous=1, c_s=1e-2, t_s=1.0), seed=52),
+    "fvm_cons_refbc": dict(n=(6, 5, 5), params=dict(scheme=2, viscous=0), seed=53),
+    "fvm_cons_viscous_periodic": dict(n=(6, 5, 5), params=dict(
+        scheme=2, viscous=1, c_s=1e-2, t_s=1.0, bc=[dict(kind=BC_PERIODIC)] * 6), seed=54),
+}
+FVM_COMMON = dict(phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0)
+
+
+def fvm_state(P, n, seed):
+    """Primitive state with uniform noise whose amplitude grows from 1e-3 to 0.1 along x about
+    (1, 0.2, 0.2, 0.2, 1/1.4) and two pressure spikes (x1.5 .. x4); T = p / (rho Rg)."""
+    s = (n[2] + 2 * NG, n[1] + 2 * NG, n[0] + 2 * NG)
+    rng = np.random.default_rng(seed)
+    amp = np.geomspace(1e-3, 0.1, s[2])[None, None, :]
+    Q = np.zeros((6, *s))
+    Q[0] = 1.0 + amp * rng.uniform(-1, 1, s)
+    Q[1:4] = 0.2 + amp * rng.uniform(-1, 1, (3, *s))
+    Q[4] = (1.0 + amp * rng.uniform(-1, 1, s)) / 1.4
+    for _ in range(2):
+        a, b, c = [int(rng.integers(NG, k - NG)) for k in s]
+        Q[4, a, b, c] *= float(rng.uniform(1.5, 4))
+    Q[5] = Q[4] / (Q[0] * P.rg)
+    return Q
 
 
 def metrics_digest(m, J) -> str:
@@ -81,11 +113,15 @@ def main() -> None:
     a = ap.parse_args()
     ref = Path(a.ref)
     module = ROOT / "oracle" / "_ref" / "jl_kernels.py"
+    corrected = ROOT / "oracle" / "_ref" / "jl_kernels_corrected.py"
     module.parent.mkdir(parents=True, exist_ok=True)
     module.write_text(jl2py.translate_tree(ref))
+    corrected.write_text(jl2py.translate_tree(ref, corrected=True))
     out = {"provenance": np.array(json.dumps({
         "translated": {f: hashlib.sha256((ref / f).read_bytes()).hexdigest() for f in jl2py.FILES},
         "module_sha256": hashlib.sha256(module.read_bytes()).hexdigest(),
+        "corrected_module_sha256": hashlib.sha256(corrected.read_bytes()).hexdigest(),
+        "corrections": [c[-1] for c in jl2py.CORRECTIONS],
         "semantics": "every value binary64; Julia's literal powers as products",
         "rk3": {"dt": RK3_DT, "steps": RK3_STEPS}}))}
     report = {}
@@ -125,6 +161,28 @@ def main() -> None:
         out[f"{name}__local_dt"] = runtime.local_dt(module, P, Q, m, J)
         for filt, label in ((1, "linear"), (2, "shock")):
             out[f"{name}__U_filter_{label}"] = runtime.filter_pass(module, params_copy(P, filter=filt), U, Q)
+    for name, spec in FVM.items():
+        n, params = spec["n"], {**FVM_COMMON, **spec["params"]}
+        P = make_params(*n, **params)
+        x, y, z = g.coords(n)
+        Q = fvm_state(P, n, spec["seed"])
+        U = orc.prim2c(P, Q)
+        orc.fill_ghosts(P, Q, U)
+        m, J = runtime.metrics(module, P, x, y, z)
+        xyz = (x, y, z)
+        out.update({f"{name}__Q": Q, f"{name}__x": x, f"{name}__y": y, f"{name}__z": z,
+                    f"{name}__metrics_sha256": np.array(metrics_digest(m, J)),
+                    f"{name}__meta": np.array(json.dumps(dict(n=list(n), params=params)))})
+        for d, (fc, fw) in enumerate(zip(runtime.fvm_faces(corrected, P, Q, m, xyz),
+                                         runtime.fvm_faces(module, P, Q, m, xyz))):
+            out[f"{name}__F{d}"], out[f"{name}__F{d}_as_written"] = fc, fw
+        r = runtime.rhs(corrected, P, Q, m, J, xyz)
+        out[f"{name}__rhs_fvm"] = r
+        report[name] = r
+        if runtime.is_reference_bcs(P):
+            Us, Qs = runtime.rk3_steps(corrected, P, runtime.prim2c(module, P, Q), m, J, RK3_DT, RK3_STEPS,
+                                       Q0=Q, xyz=xyz)
+            out[f"{name}__U_rk3_fvm"], out[f"{name}__Q_rk3_fvm"] = Us, Qs
     np.savez_compressed(HERE / "jl_reference_rhs.npz", **out)
     for name, r in report.items():
         print(name, "max |rhs|", float(np.abs(r[I]).max()))

@@ -135,6 +135,7 @@ def test_translation_reproduces_the_fixture_digest():
     for f, h in prov["translated"].items():
         assert hashlib.sha256((REF / f).read_bytes()).hexdigest() == h, f
     assert hashlib.sha256(jl2py.translate_tree(REF).encode()).hexdigest() == prov["module_sha256"]
+    assert hashlib.sha256(jl2py.translate_tree(REF, True).encode()).hexdigest() == prov["corrected_module_sha256"]
 
 
 # ---- the translation rules on small pieces of Julia
@@ -189,3 +190,79 @@ def test_rule_blocks_and_implicit_return():
     assert ns["f"](1, 2) == 2
     assert ns["g"](JArray(np.array([0.1, 0.2])), 2) == pytest.approx(0.6)  # 1-based A[m]
     assert ns["g"](JArray(np.array([1.0, 1.0])), 2) == 1.0
+
+
+# ---- the finite-volume scheme (FVM.jl), from the translation with jl2py.CORRECTIONS applied
+def _fvm_cases():
+    d = np.load(FIX, allow_pickle=True)
+    return sorted({k.split("__")[0] for k in d.files if k.endswith("__rhs_fvm")})
+
+
+def _fvm_inputs(d, name):
+    meta = json.loads(str(d[f"{name}__meta"]))
+    P = make_params(*meta["n"], **meta["params"])
+    x, y, z = (d[f"{name}__{a}"] for a in "xyz")
+    m, J = orc.metrics(P, x, y, z)
+    assert _digest(m, J) == str(d[f"{name}__metrics_sha256"])  # the reference's metrics
+    return P, d[f"{name}__Q"], m, J, (x, y, z)
+
+
+@pytest.mark.parametrize("name", _fvm_cases())
+def test_oracle_fvm_faces_rhs_and_steps_equal_the_corrected_translation(name):
+    """Face fluxes of the three directions, the RHS and (boundary.jl's boundary set) two SSP-RK3
+    steps of the finite-volume scheme: bit for bit."""
+    d = np.load(FIX, allow_pickle=True)
+    P, Q, m, J, (x, y, z) = _fvm_inputs(d, name)
+    eigen = int(P.scheme) == 1
+    phi, U = orc.sensor(P, Q), orc.prim2c(P, Q)
+    for dd in range(3):
+        S = orc.metric_norm(P, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2])
+        F = orc.fvm_face_flux(P, dd, eigen, phi, S, Q, U, x, y, z)
+        assert np.array_equal(F, d[f"{name}__F{dd}"]), (dd, float(np.abs(F - d[f"{name}__F{dd}"]).max()))
+    orc.set_coordinates(x, y, z)
+    try:
+        r = orc.rhs(P, Q, list(m), J)
+        assert np.abs(r[I]).max() > 0 and np.array_equal(r[I], d[f"{name}__rhs_fvm"][I])
+        if f"{name}__U_rk3_fvm" in d.files:
+            rk = json.loads(str(d["provenance"]))["rk3"]
+            Us, Un, Qs = U.copy(), np.zeros_like(U), Q.copy()
+            orc.rk3(P, rk["steps"], rk["dt"], Us, Un, Qs, list(m), J)
+            assert np.array_equal(Us, d[f"{name}__U_rk3_fvm"]) and np.array_equal(Qs, d[f"{name}__Q_rk3_fvm"])
+    finally:
+        orc.set_coordinates(None)
+
+
+def test_fvm_cases_cover_the_branches_and_forms():
+    d = np.load(FIX, allow_pickle=True)
+    forms, seen = set(), {1: set(), 2: set()}
+    for name in _fvm_cases():
+        P, Q, m, J, xyz = _fvm_inputs(d, name)
+        forms.add((int(P.scheme), int(P.viscous)))
+        orc.set_coordinates(*xyz)
+        try:
+            _, br = orc.rhs(P, Q, list(m), J, with_branches=True)
+        finally:
+            orc.set_coordinates(None)
+        seen[int(P.scheme)] |= set(np.unique(np.concatenate([b.ravel() for b in br])).tolist())
+    assert forms == {(1, 0), (1, 1), (2, 0), (2, 1)}
+    assert seen[1] == seen[2] == {0, 1, 2, 3}  # linear, WENO7, WENO5, minmod faces
+
+
+def test_fvm_defects_change_only_the_faces_they_reach():
+    """The as-written translation differs from the corrected one exactly where the two defects
+    of FVM.jl act: the WENO5 faces of the Roe-characteristic reconstruction (the overwritten
+    kinetic energy) and the y and z faces of the component-wise one (states stored as fluxes)."""
+    d = np.load(FIX, allow_pickle=True)
+    for name in _fvm_cases():
+        P, Q, m, J, (x, y, z) = _fvm_inputs(d, name)
+        eigen = int(P.scheme) == 1
+        phi, U = orc.sensor(P, Q), orc.prim2c(P, Q)
+        for dd in range(3):
+            Fc, Fw = d[f"{name}__F{dd}"], d[f"{name}__F{dd}_as_written"]
+            differs = np.any(Fc != Fw, axis=0)
+            if eigen:
+                S = orc.metric_norm(P, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2])
+                _, br = orc.fvm_face_flux(P, dd, True, phi, S, Q, U, x, y, z, with_branch=True)
+                assert np.array_equal(differs, br == 2), (name, dd)
+            else:
+                assert differs.all() if dd else not differs.any(), (name, dd)
