@@ -20,6 +20,7 @@
 // that runs here, its Python coefficient script (Utils/FDMcoeffs.py), pins the UP7 and CD6
 // face coefficients (tests/golden/fdm_coeffs.json).
 #pragma once
+#include <type_traits>
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
@@ -896,14 +897,18 @@ namespace f3do {
 // ---------------------------------------------------------------------------------
 // Workspace and the composed RHS / RK3 stage (solver.jl:416-444 with flowAdvance).
 // The finite-volume schemes (params.scheme) reconstruct U: the stage's state, or prim2c(Q)
-// for a bare RHS; they need the cell-centre coordinates (set_coordinates).
+// for a bare RHS; they need the cell-centre coordinates (set_coordinates). Their face geometry
+// is computed in G: R, except for long double, whose solver (the rounding yardstick) takes
+// the FP64 geometry and so the FP64 side of every |nz| = |ny| tie of the tangent basis.
 template <class R, class W> struct Solver {
+    using G = typename std::conditional<std::is_same<R, long double>::value, double, R>::type;
     f3d_params P;
     Grid g;
     const R* m[9];
     const R* J;
-    const R *xs = nullptr, *ys = nullptr, *zs = nullptr;
-    std::vector<R> S[3], phi, Fp, Fm, F[3], Fv[3], Uq, xyz[3], dtl, sc;
+    const G *xs = nullptr, *ys = nullptr, *zs = nullptr;
+    std::vector<R> S[3], phi, Fp, Fm, F[3], Fv[3], Uq, dtl, sc;
+    std::vector<G> xyz[3];
     long tt = 0;  // steps done (the filter runs after every filter_interval-th)
     std::vector<int8_t> branch[3];
     bool record_branch = false;
@@ -929,7 +934,7 @@ template <class R, class W> struct Solver {
         Fm.assign(nc * 5, R(0));
     }
 
-    void set_coordinates(const R* x, const R* y, const R* z) {
+    void set_coordinates(const G* x, const G* y, const G* z) {
         xs = x;
         ys = y;
         zs = z;
@@ -945,7 +950,7 @@ template <class R, class W> struct Solver {
                 U = Uq.data();
             }
             for (int d = 0; d < 3; d++)
-                fvm_face_flux<R>(P, d, P.scheme == F3D_SCHEME_FVM_EIGEN, phi.data(), S[d].data(), Q, U, xs, ys, zs,
+                fvm_face_flux<R, G>(P, d, P.scheme == F3D_SCHEME_FVM_EIGEN, phi.data(), S[d].data(), Q, U, xs, ys, zs,
                                  F[d].data(), record_branch ? branch[d].data() : nullptr);
             if (P.viscous) viscous<R>(P, Q, m, J, Fv[0].data(), Fv[1].data(), Fv[2].data());
             return;

@@ -177,9 +177,12 @@ void fvm_face_geometry(int d, const V4<const R>& X, const V4<const R>& Y, const 
     nz = nz / area;
 }
 
-template <class R>
+// G: the type the face geometry is computed in (R by default; double with R = long double
+// gives the extended-precision yardstick the FP64 normals, and so the same side of every
+// |nz| = |ny| tie of the characteristic tangent basis).
+template <class R, class G = R>
 void fvm_face_flux(const f3d_params& P, int d, bool eigen, const R* phip, const R* Sp, const R* Qp, const R* Up,
-                   const R* xp, const R* yp, const R* zp, R* Fp_out, int8_t* branch_out) {
+                   const G* xp, const G* yp, const G* zp, R* Fp_out, int8_t* branch_out) {
     Grid g(P);
     Consts<R> C(P);
     const long NG = g.ng;
@@ -187,7 +190,7 @@ void fvm_face_flux(const f3d_params& P, int d, bool eigen, const R* phip, const 
     const long st = g.stride(d);
     const long fx = g.nx + (d == 0), fy = g.ny + (d == 1), fz = g.nz + (d == 2);
     const size_t nf = (size_t)fx * fy * fz;
-    V4<const R> X{xp, g.nxt, g.nyt, g.nzt}, Y{yp, g.nxt, g.nyt, g.nzt}, Z{zp, g.nxt, g.nyt, g.nzt};
+    V4<const G> X{xp, g.nxt, g.nyt, g.nzt}, Y{yp, g.nxt, g.nyt, g.nzt}, Z{zp, g.nxt, g.nyt, g.nzt};
     const R gm = C.gamma - R(1);
 #pragma omp parallel for schedule(static)
     for (long kf = 1; kf <= fz; kf++)
@@ -198,8 +201,9 @@ void fvm_face_flux(const f3d_params& P, int d, bool eigen, const R* phip, const 
                 const long cL = (i - 1) + g.nxt * ((j - 1) + g.nyt * (k - 1));
                 auto at = [&](const R* a, long off, int n) -> R { return a[cL + off * st + (size_t)n * nc]; };
                 const size_t fo = (ifc - 1) + fx * ((jf - 1) + fy * (kf - 1));
-                R nx, ny, nz, area;
-                fvm_face_geometry<R>(d, X, Y, Z, i, j, k, nx, ny, nz, area);
+                G gnx, gny, gnz, garea;
+                fvm_face_geometry<G>(d, X, Y, Z, i, j, k, gnx, gny, gnz, garea);
+                const R nx = R(gnx), ny = R(gny), nz = R(gnz), area = R(garea);
                 R phimax = at(phip, -2, 0);
                 for (long o = -1; o <= 3; o++) phimax = jmax(phimax, at(phip, o, 0));
                 const int br = face_branch(C, phimax);

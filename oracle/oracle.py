@@ -72,6 +72,15 @@ def fvm_face_flux(P, d, eigen, phi, S, Q, U, x, y, z, with_branch=False):
     return (F, br) if with_branch else F
 
 
+def fvm_face_flux_ld(P, d, eigen, phi, S, Q, U, x, y, z):
+    """fvm_face_flux evaluated in long double (the yardstick for FP64 rounding)."""
+    F = np.zeros((5, *face_shape(P, d)))
+    xs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z)]
+    lib().orcld_fvm_face_flux(C.byref(P), C.c_int(d), C.c_int(int(eigen)), _p(phi), _p(S), _p(Q), _p(U),
+                              _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(F))
+    return F
+
+
 _profiles: dict = {}
 
 

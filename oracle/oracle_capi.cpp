@@ -178,6 +178,23 @@ void orcld_rhs(const f3d_params* P, const double* Q, const double* const m[9], c
     }
 }
 
+// Finite-volume face fluxes of one direction in long double from FP64 inputs (rounded back),
+// on the FP64 face geometry.
+void orcld_fvm_face_flux(const f3d_params* P, int dir, int eigen, const double* phi, const double* S,
+                         const double* Q, const double* U, const double* x, const double* y, const double* z,
+                         double* F) {
+    Grid g(*P);
+    const size_t nc = g.ncell();
+    using L = long double;
+    std::vector<L> phil(phi, phi + nc), Sl(S, S + nc), Ql(Q, Q + nc * 6), Ul(U, U + nc * 5);
+    const size_t nf = (size_t)(g.nx + (dir == 0)) * (g.ny + (dir == 1)) * (g.nz + (dir == 2));
+    std::vector<L> Fl(nf * 5, L(0));
+    // the face geometry in FP64 (the FP64 normals), the rest in long double
+    fvm_face_flux<L, double>(*P, dir, eigen != 0, phil.data(), Sl.data(), Ql.data(), Ul.data(), x, y, z, Fl.data(),
+                             nullptr);
+    for (size_t i = 0; i < nf * 5; i++) F[i] = (double)Fl[i];
+}
+
 // ---- the reference's own precision: Float32 state, Float64 WENO7 alphas -------------
 // nsteps SSP-RK3 steps in long double from FP64 inputs (the yardstick for the rounding of
 // FP64 trajectories); U, Un, Q updated in place (rounded back to FP64).
