@@ -40,6 +40,11 @@ struct Dual {
         double s = std::sqrt(a.v);
         return Dual(s, a.d / (2.0 * s));
     }
+    // a^e for a constant exponent e
+    friend Dual pow(const Dual& a, const Dual& e) {
+        const double r = std::pow(a.v, e.v);
+        return Dual(r, e.v * std::pow(a.v, e.v - 1.0) * a.d);
+    }
 };
 
 // Operation counters (single-threaded use: the counting entry point runs on one thread).
@@ -76,6 +81,7 @@ struct Counted {
     friend Counted abs(const Counted& a) { tick(OPC_CMP); return Counted(std::fabs(a.v)); }
     friend Counted sqrt(const Counted& a) { tick(OPC_SQRT); return Counted(std::sqrt(a.v)); }
     friend Counted cbrt(const Counted& a) { tick(OPC_SQRT); return Counted(std::cbrt(a.v)); }
+    friend Counted pow(const Counted& a, const Counted& e) { tick(OPC_SQRT); return Counted(std::pow(a.v, e.v)); }
 };
 
 }  // namespace f3do

@@ -35,6 +35,7 @@ namespace f3do {
 using std::abs;
 using std::sqrt;
 using std::cbrt;
+using std::pow;
 
 // NaN-propagating max/min like Julia's max/min on floats.
 template <class T> inline T jmax(const T& a, const T& b) {
@@ -714,12 +715,14 @@ void viscous(const f3d_params& P, const R* Qp, const R* const m[9], const R* Jp,
                     const R s12 = R(0.5) * (dudy + dvdx), s13 = R(0.5) * (dudz + dwdx), s23 = R(0.5) * (dvdz + dwdy);
                     const R sii = dudx * dudx + dvdy * dvdy + dwdz * dwdz;
                     const R sij = s12 * s12 + s13 * s13 + s23 * s23;
-                    const R J13 = cbrt(Jac);  // Jac^(1/3)
+                    // Jac^(1/3f0), S^5 and Sd^2.5f0 through pow, (C/Jac^(1/3))^2 and Sd^3 as
+                    // Julia's literal powers (products), in the reference's grouping
+                    const R J13 = pow(Jac, R(1) / R(3));
                     R mut;
                     if (P.les == F3D_LES_SMAGORINSKY) {  // viscous.jl:66-78
                         const R Smag = sqrt(R(2) * (sii + R(2) * sij));
                         const R cd = R(0.1) / J13;
-                        mut = jmin(rho * cd * cd * Smag, R(2) * mu);
+                        mut = jmin(rho * (cd * cd) * Smag, R(2) * mu);
                     } else {  // WALE, viscous.jl:79-101
                         const R S = sqrt(sii + R(2) * sij);
                         R d11 = dudx * dudx + dudy * dvdx + dudz * dwdx;
@@ -733,9 +736,9 @@ void viscous(const f3d_params& P, const R* Qp, const R* const m[9], const R* Jp,
                         const R d13 = R(0.5) * (dudx * dwdx + dvdx * dwdy + dwdx * dwdz + dudz * dudx + dvdz * dudy + dwdz * dudz);
                         const R d23 = R(0.5) * (dudy * dwdx + dvdy * dwdy + dwdy * dwdz + dudz * dvdx + dvdz * dvdy + dwdz * dvdz);
                         const R Sd = sqrt(d11 * d11 + d22 * d22 + d33 * d33 + R(2) * (d12 * d12 + d13 * d13 + d23 * d23));
-                        const R D = Sd * Sd * Sd / (S * S * S * S * S + Sd * Sd * sqrt(Sd));  // Sd^3/(S^5 + Sd^2.5)
+                        const R D = Sd * Sd * Sd / (pow(S, R(5)) + pow(Sd, R(2.5)));  // Sd^3/(S^5 + Sd^2.5)
                         const R cd = R(0.325) / J13;
-                        mut = jmin(rho * cd * cd * D, R(2) * mu);
+                        mut = jmin(rho * (cd * cd) * D, R(2) * mu);
                     }
                     mu = mu + mut;
                     lam = lam + C.cp * mut / R(0.9);

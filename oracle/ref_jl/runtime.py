@@ -7,8 +7,8 @@ and run.jl gave them:
 - the thread index of a launch (one thread at a time: blockIdx = blockDim = 1,
   threadIdx = (i, j, k)) and Julia's max / min (a NaN wins), sqrt (NaN below 0), ifelse,
   zero, eps(Float32);
-- the global constants of run.jl:8-13, 57-77 (γ, Rg, Cp, C_s, T_s, Pr, Ncons, the hybrid
-  thresholds, Linear, NG, Nxp, Nyp, Nzp) from an f3d_params;
+- the global constants of run.jl:4-13, 57-77 (LES_smag, LES_wale, γ, Rg, Cp, C_s, T_s, Pr, Ncons,
+  the hybrid thresholds, Linear, NG, Nxp, Nyp, Nzp) from an f3d_params;
 - the launch sequence of one RHS: the sensor (solver.jl:424), the split and the
   reconstruction of each direction (solver.jl:133-188) or, for the finite-volume schemes, the
   face kernels of FVM.jl (solver.jl:21-31), the viscous fluxes and div (solver.jl:429) into a
@@ -65,7 +65,7 @@ class JArray:
 
     def __getitem__(self, idx):
         key, sliced = self._key(idx)
-        return JArray(self.a[key]) if sliced else float(self.a[key])
+        return JArray(self.a[key]) if sliced else self.a[key]  # a NumPy scalar: IEEE 0/0 = NaN, as Julia
 
     def __setitem__(self, idx, v):
         key, _ = self._key(idx)
@@ -112,7 +112,7 @@ def _jmin(*v):
 
 
 def _sqrt(x):
-    return math.sqrt(x) if x >= 0 else float("nan")
+    return np.float64(math.sqrt(x)) if x >= 0 else np.float64("nan")
 
 
 def _mat(r, c=None):
@@ -143,7 +143,7 @@ def kernels(module_path: Path | str, P) -> dict:
         "Ncons": 5, "Nprim": 6, "NG": NG, "Nxp": int(P.nx), "Nyp": int(P.ny), "Nzp": int(P.nz),
         "hybrid_ϕ1": float(P.phi1), "hybrid_ϕ2": float(P.phi2), "hybrid_ϕ3": float(P.phi3),
         "Linear": JArray(np.array([u * lp + c * (1.0 - lp) for u, c in zip(up7, cd6)])),
-        "LES_smag": False, "LES_wale": False,
+        "LES_smag": int(getattr(P, "les", 0)) == 1, "LES_wale": int(getattr(P, "les", 0)) == 2,
         "Nx": int(P.nx), "Ny": int(P.ny), "Nz": int(P.nz),
         "Nx_tot": int(P.nx) + 2 * NG, "Ny_tot": int(P.ny) + 2 * NG, "Nz_tot": int(P.nz) + 2 * NG,
     })
@@ -157,13 +157,15 @@ def kernels(module_path: Path | str, P) -> dict:
 
 
 def launch(fn, ext, *args):
-    """Every thread (i, j, k) of a grid covering ext = (X, Y, Z), one after the other."""
+    """Every thread (i, j, k) of a grid covering ext = (X, Y, Z), one after the other (IEEE
+    exceptions quiet: a division by zero gives inf or NaN, as on the GPU)."""
     X, Y, Z = ext
-    for k in range(1, Z + 1):
-        for j in range(1, Y + 1):
-            for i in range(1, X + 1):
-                _thread.x, _thread.y, _thread.z = i, j, k
-                fn(*args)
+    with np.errstate(all="ignore"):
+        for k in range(1, Z + 1):
+            for j in range(1, Y + 1):
+                for i in range(1, X + 1):
+                    _thread.x, _thread.y, _thread.z = i, j, k
+                    fn(*args)
 
 
 def is_reference_bcs(P) -> bool:

@@ -4,8 +4,9 @@ Julia kernels translated mechanically into Python (oracle/ref_jl/jl2py.py) and r
 - the inputs of the golden fixtures (test_oracle.py::test_golden_fixtures: four splits,
   characteristic and component-wise, hybrid and WENO5-everywhere, periodic, reference and
   mixed boundary rules; inviscid), and
-- three viscous cases made here the same way (curvilinear random states, Sutherland viscosity
-  large enough for the viscous terms to matter), whose inputs are stored too;
+- five viscous cases made here the same way (curvilinear random states, Sutherland viscosity
+  large enough for the viscous terms to matter; two with the LES closures, Smagorinsky and
+  WALE), whose inputs are stored too;
 and, for the cases with boundary.jl's own boundary set, the reference's prim2c, c2Prim with
 the ghost fill, and two SSP-RK3 steps (the stage loop of solver.jl); for the viscous cases its
 local time step and one pass of each filter; for every case a SHA-256 of the metrics and J of
@@ -54,6 +55,12 @@ VISCOUS = {
         seed=36, spikes=4),
     "curvi_viscous_char_sw_refbc": dict(n=(6, 5, 5), params=dict(
         character=1, viscous=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0), seed=37, spikes=4),
+    # the LES closures of viscous.jl:66-106 (run.jl:4-5 LES_smag / LES_wale)
+    "curvi_les_smagorinsky_char_sw_refbc": dict(n=(6, 5, 5), params=dict(
+        character=1, viscous=1, les=1, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0), seed=61, spikes=4),
+    "curvi_les_wale_comp_ausm_periodic": dict(n=(6, 6, 5), params=dict(
+        character=0, split_method=3, viscous=1, les=2, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0,
+        bc=[dict(kind=BC_PERIODIC)] * 6), seed=62, spikes=4),
 }
 RK3_DT, RK3_STEPS = 2e-4, 2
 FVM = {
@@ -122,7 +129,7 @@ def main() -> None:
         "module_sha256": hashlib.sha256(module.read_bytes()).hexdigest(),
         "corrected_module_sha256": hashlib.sha256(corrected.read_bytes()).hexdigest(),
         "corrections": [c[-1] for c in jl2py.CORRECTIONS],
-        "semantics": "every value binary64; Julia's literal powers as products",
+        "semantics": "every value binary64; Julia's literal powers x^2, x^3 as products, other powers by C pow",
         "rk3": {"dt": RK3_DT, "steps": RK3_STEPS}}))}
     report = {}
     for f in sorted(HERE.glob("*.npz")):

@@ -2,9 +2,10 @@
 (oracle/ref_jl/jl2py.py, run by oracle/ref_jl/runtime.py; CPU only).
 
 tests/golden/jl_reference_rhs.npz holds the reference's finite-difference RHS, so computed
-(tests/golden/make_jl_reference.py), on the golden fixtures' inputs and on three viscous
-cases, and for the cases with boundary.jl's own boundary set its prim2c, c2Prim with the
-ghost fill and two SSP-RK3 steps. The FP64 oracle must equal all of it bit for bit: the same
+(tests/golden/make_jl_reference.py), on the golden fixtures' inputs and on five viscous
+cases (two with the LES closures), and for the cases with boundary.jl's own boundary set its
+prim2c, c2Prim with the ghost fill and two SSP-RK3 steps; and its finite-volume faces, RHS
+and steps. The FP64 oracle must equal all of it bit for bit: the same
 statements in the same order, in binary64 (the oracle is built without FMA contraction). With F3D_REFERENCE naming the reference tree,
 the translation is regenerated and must reproduce the digest recorded with the fixture.
 """
@@ -119,9 +120,10 @@ def test_fixture_covers_the_forms():
     forms = set()
     for name in names:
         p = _inputs(d, name)[0]["params"]
-        forms.add((p.get("split_method", 0), p.get("character", 1), p.get("viscous", 0)))
-    assert {s for s, _, _ in forms} == {0, 1, 2, 3}  # SW, LF, VL, AUSM
-    assert {c for _, c, _ in forms} == {0, 1} and {v for _, _, v in forms} == {0, 1}
+        forms.add((p.get("split_method", 0), p.get("character", 1), p.get("viscous", 0), p.get("les", 0)))
+    assert {f[0] for f in forms} == {0, 1, 2, 3}  # SW, LF, VL, AUSM
+    assert {f[1] for f in forms} == {0, 1} and {f[2] for f in forms} == {0, 1}
+    assert {f[3] for f in forms} == {0, 1, 2}  # laminar, Smagorinsky, WALE
 
 
 REF = Path(os.environ.get("F3D_REFERENCE", "")) if os.environ.get("F3D_REFERENCE") else None
