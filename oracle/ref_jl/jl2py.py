@@ -28,11 +28,18 @@ algorithm evaluated in FP64 in the reference's own operation order, the form the
 restates. The generated module is written next to the compiled reference program
 (oracle/_ref/, not tracked).
 
+`translate_tree(root, typed=True)` keeps Julia's element types instead, for an evaluation of
+the reference's own precision in NumPy scalars: `12f0` -> `_f32(12e0)` (Float32), `1e-20` /
+`0.5` -> `_f64(...)` (Float64), integer literals left as they are (Python ints take the
+other operand's type, as Julia's Int does), a local declared `x::Float32` / `x::Float64`
+converted at every assignment to it (`x op= e` included), `MMatrix` / `MVector` temporaries of
+their element type. The runtime then supplies Float32 arrays and run.jl's Float32 constants.
+
 `translate_tree(root, corrected=True)` first applies CORRECTIONS, two defects of FVM.jl
 repaired by exact text substitutions, each of which must match the stated number of times;
 everything else is translated as written.
 
-    python -m oracle.ref_jl.jl2py <reference root> [out.py] [--corrected]
+    python -m oracle.ref_jl.jl2py <reference root> [out.py] [--corrected] [--typed]
 """
 from __future__ import annotations
 
@@ -264,14 +271,28 @@ def _ranges_in_brackets(s: str) -> str:
     return "".join(out)
 
 
-def expr(s: str) -> str:
+def _typed_literal(m) -> str:
+    num, f32 = m.group(1), m.group(2)
+    if f32 is not None:
+        return f"_f32({num}e{f32})"
+    return f"_f64({num})" if re.search(r"[.eE]", num) else num
+
+
+def expr(s: str, typed: bool = False) -> str:
     s = s.replace("CUDA.eps(Float32)", "_eps32()")
     s = re.sub(r"\bzeros\(\s*Float(32|64)\s*,", "_zeros(", s)
     if ":" in s and "[" in s:
         s = _ranges_in_brackets(s)
+    if typed:  # temporaries of the stated element type
+        s = re.sub(r"MMatrix\{\s*([^,}]+)\s*,\s*([^,}]+)\s*,\s*Float(32|64)[^}]*\}\s*\(\s*undef\s*\)",
+                   r"_mat(\1, \2, \3)", s)
+        s = re.sub(r"MVector\{\s*([^,}]+)\s*,\s*Float(32|64)[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1, None, \2)", s)
     s = re.sub(r"MMatrix\{\s*([^,}]+)\s*,\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1, \2)", s)
     s = re.sub(r"MVector\{\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1)", s)
     s = re.sub(r"SVector\{[^}]*\}\s*\(", "_vec(", s)
+    if typed:  # Float32 literals (12f0) -> _f32(12e0), Float64 ones (1e-20, 0.5) -> _f64(...)
+        s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][-+]?\d+)?|\.\d+(?:[eE][-+]?\d+)?|\d+(?:[eE][-+]?\d+)?)"
+                   r"(?:f(-?\d+))?(?![\w.])", _typed_literal, s)
     s = re.sub(r"(\d+\.\d*|\.\d+|\d+)f(-?\d+)", r"\1e\2", s)          # Float32 literals
     s = re.sub(r"(?<![\w.])(\d+)i32\b", r"\1", s)                       # Int32 literals
     # implicit products: a numeric literal (possibly with exponent) followed by a name or '('
@@ -317,10 +338,17 @@ def _strip_annot(lhs: str) -> str:
     return re.sub(r"::\s*\w+(\{[^}]*\})?", "", lhs).strip()
 
 
-def translate(src: str) -> str:
-    """Python source of every function of a Julia kernel file (top-level code is skipped)."""
+_ANNOT = re.compile(r"^\s*([^\W\d]\w*)\s*::\s*Float(32|64)\s*$")
+
+
+def translate(src: str, typed: bool = False) -> str:
+    """Python source of every function of a Julia kernel file (top-level code is skipped).
+    typed: Julia's element types kept (literals, `x::Float32` locals converting on every
+    assignment, temporaries) for an evaluation in Float32 / Float64 NumPy scalars."""
+    expr_ = (lambda e: expr(e, True)) if typed else expr
     out: list[str] = []
     stack: list[str] = []
+    types: dict[str, str] = {}  # the declared Float32 / Float64 locals of the current function
     pad = lambda: "    " * sum(k != "begin" for k in stack)  # begin .. end adds no indentation
     last_expr = None  # index in out of the function body's last statement if it is a bare expression
     for raw in logical_lines(src):
@@ -332,6 +360,7 @@ def translate(src: str) -> str:
             if m:
                 out.append(f"def {m.group(1)}({_strip_annot(m.group(2))}):")
                 stack.append("function")
+                types = {}
             continue
         if s == "end":
             stack.pop()
@@ -349,38 +378,49 @@ def translate(src: str) -> str:
             continue
         m = re.match(r"if\s+(.*)$", s)
         if m:
-            out.append(pad() + f"if {expr(m.group(1))}:")
+            out.append(pad() + f"if {expr_(m.group(1))}:")
             stack.append("if")
             continue
         m = re.match(r"elseif\s+(.*)$", s)
         if m:
-            out.append(pad()[4:] + f"elif {expr(m.group(1))}:")
+            out.append(pad()[4:] + f"elif {expr_(m.group(1))}:")
             continue
         if s == "else":
             out.append(pad()[4:] + "else:")
             continue
         m = re.match(r"for\s+(\w+)\s*(?:=|in)\s*(.+?)\s*:\s*(.+)$", s)
         if m:
-            out.append(pad() + f"for {m.group(1)} in range({expr(m.group(2))}, ({expr(m.group(3))}) + 1):")
+            out.append(pad() + f"for {m.group(1)} in range({expr_(m.group(2))}, ({expr_(m.group(3))}) + 1):")
             stack.append("for")
             continue
         if s == "return" or s.startswith("return "):
             rest = s[len("return"):].strip()
-            out.append(pad() + ("return" if not rest else f"return {expr(rest)}"))
+            out.append(pad() + ("return" if not rest else f"return {expr_(rest)}"))
             continue
         m = re.match(r"(.+?)\s*\.=\s*(.+)$", s)
         if m:
-            out.append(pad() + f"{expr(m.group(1))}._fill({expr(m.group(2))})")
+            out.append(pad() + f"{expr_(m.group(1))}._fill({expr_(m.group(2))})")
             continue
         m = re.match(r"(.+?)\s*(\+=|-=|\*=|/=)\s*(.+)$", s)
         if m:
-            out.append(pad() + f"{expr(_strip_annot(m.group(1)))} {m.group(2)} {expr(m.group(3))}")
+            lhs = expr_(_strip_annot(m.group(1)))
+            if typed and lhs in types:  # x op= e assigns x op e converted to x's declared type
+                out.append(pad() + f"{lhs} = _f{types[lhs]}({lhs} {m.group(2)[0]} ({expr_(m.group(3))}))")
+            else:
+                out.append(pad() + f"{lhs} {m.group(2)} {expr_(m.group(3))}")
             continue
         m = re.match(r"([^=<>!]+?)\s*=(?!=)\s*(.+)$", s)
         if m:
-            out.append(pad() + f"{expr(_strip_annot(m.group(1)))} = {expr(m.group(2))}")
+            a = _ANNOT.match(m.group(1))
+            lhs = expr_(_strip_annot(m.group(1)))
+            if typed and a:
+                types[lhs] = a.group(2)
+            if typed and lhs in types:
+                out.append(pad() + f"{lhs} = _f{types[lhs]}({expr_(m.group(2))})")
+            else:
+                out.append(pad() + f"{lhs} = {expr_(m.group(2))}")
             continue
-        out.append(pad() + expr(s))
+        out.append(pad() + expr_(s))
         if len(stack) == 1:
             last_expr = len(out) - 1
     if stack:
@@ -464,14 +504,16 @@ def translate_script(src: str, first: int, last: int) -> str:
 METRIC_LINES = (139, 248)
 
 
-def translate_tree(root: Path, corrected: bool = False) -> str:
+def translate_tree(root: Path, corrected: bool = False, typed: bool = False) -> str:
     parts = ["# Generated by oracle/ref_jl/jl2py.py from the reference's Julia kernels; do not edit.\n"]
     if corrected:
         parts.append("# With CORRECTIONS applied (FVM.jl).\n")
+    if typed:
+        parts.append("# Typed: Julia's Float32 / Float64 literals, locals and temporaries kept.\n")
     for name in FILES:
         src = (root / name).read_text()
         parts.append(f"# ---- {name}\n")
-        parts.append(translate(apply_corrections(name, src) if corrected else src))
+        parts.append(translate(apply_corrections(name, src) if corrected else src, typed))
     a, b = METRIC_LINES
     parts.append(f"# ---- parse_mesh.jl:{a}-{b}, as the body of _metrics()\n")
     body = translate_script((root / "parse_mesh.jl").read_text(), a, b)
@@ -482,12 +524,12 @@ def translate_tree(root: Path, corrected: bool = False) -> str:
 
 def main(argv=None) -> None:
     argv = sys.argv[1:] if argv is None else argv
-    corrected = "--corrected" in argv
-    argv = [a for a in argv if a != "--corrected"]
+    corrected, typed = "--corrected" in argv, "--typed" in argv
+    argv = [a for a in argv if a not in ("--corrected", "--typed")]
     root = Path(argv[0])
     out = Path(argv[1]) if len(argv) > 1 else Path(__file__).resolve().parent.parent / "_ref" / "jl_kernels.py"
     out.parent.mkdir(parents=True, exist_ok=True)
-    out.write_text(translate_tree(root, corrected))
+    out.write_text(translate_tree(root, corrected, typed))
     print(out)
 
 

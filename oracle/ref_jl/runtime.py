@@ -119,6 +119,30 @@ def _mat(r, c=None):
     return JArray(np.zeros(r if c is None else (c, r)))
 
 
+def _tjmax(*v):
+    """Julia's max on typed values: NaN wins, the result in the promoted type."""
+    for x in v:
+        if x != x:
+            return np.result_type(*v).type(x)
+    return np.result_type(*v).type(max(v))
+
+
+def _tjmin(*v):
+    for x in v:
+        if x != x:
+            return np.result_type(*v).type(x)
+    return np.result_type(*v).type(min(v))
+
+
+def _tsqrt(x):
+    """sqrt in the argument's precision (an Int gives Float64); NaN below 0, as on the GPU."""
+    return np.sqrt(x if isinstance(x, np.floating) else np.float64(x))
+
+
+def _tmat(r, c=None, bits=64):
+    return JArray(np.zeros(r if c is None else (c, r), dtype=np.float32 if bits == 32 else np.float64))
+
+
 HELPERS = dict(
     blockIdx=lambda: _one, blockDim=lambda: _one, threadIdx=lambda: _thread,
     max=_jmax, min=_jmin, sqrt=_sqrt, abs=abs,
@@ -130,19 +154,28 @@ HELPERS = dict(
 )
 
 
-def kernels(module_path: Path | str, P) -> dict:
-    """The translated kernels with the run.jl constants of the parameter set P."""
+def kernels(module_path: Path | str, P, typed: bool = False) -> dict:
+    """The translated kernels with the run.jl constants of the parameter set P. typed: for a
+    module translated with Julia's types (jl2py typed), the constants in run.jl's types
+    (Float32, computed in Float32 where run.jl computes them) and type-preserving helpers."""
     g = dict(HELPERS)
-    gamma, rg = float(P.gamma), float(P.rg)
+    f = np.float32 if typed else float
+    gamma, rg = f(P.gamma), f(P.rg)
     up7 = [-3 / 420, 25 / 420, -101 / 420, 319 / 420, 214 / 420, -38 / 420, 4 / 420]
     cd6 = [0.0, 1 / 60, -2 / 15, 37 / 60, 37 / 60, -2 / 15, 1 / 60]
-    lp = float(P.linear_phi)
+    lp = f(P.linear_phi)
+    if typed:  # SVector{7, Float32}(Float64 quotients); Linear = UP7 * Linear_ϕ + CD6 * (1 - Linear_ϕ)
+        linear = (np.array(up7).astype(np.float32) * lp + np.array(cd6).astype(np.float32) * (np.float32(1) - lp))
+        g.update(_f32=np.float32, _f64=np.float64, _eps32=lambda: np.float32(2.0 ** -23), _mat=_tmat,
+                 max=_tjmax, min=_tjmin, sqrt=_tsqrt, zero=lambda a: type(a)(0) if isinstance(a, np.generic) else 0)
+    else:
+        linear = np.array([u * lp + c * (1.0 - lp) for u, c in zip(up7, cd6)])
     g.update({
-        "γ": gamma, "Rg": rg, "Cp": float(P.cp) if P.cp else rg * gamma / (gamma - 1),
-        "C_s": float(P.c_s), "T_s": float(P.t_s), "Pr": float(P.pr),
+        "γ": gamma, "Rg": rg, "Cp": f(P.cp) if P.cp else rg * gamma / (gamma - 1),
+        "C_s": f(P.c_s), "T_s": f(P.t_s), "Pr": f(P.pr),
         "Ncons": 5, "Nprim": 6, "NG": NG, "Nxp": int(P.nx), "Nyp": int(P.ny), "Nzp": int(P.nz),
-        "hybrid_ϕ1": float(P.phi1), "hybrid_ϕ2": float(P.phi2), "hybrid_ϕ3": float(P.phi3),
-        "Linear": JArray(np.array([u * lp + c * (1.0 - lp) for u, c in zip(up7, cd6)])),
+        "hybrid_ϕ1": f(P.phi1), "hybrid_ϕ2": f(P.phi2), "hybrid_ϕ3": f(P.phi3),
+        "Linear": JArray(linear),
         "LES_smag": int(getattr(P, "les", 0)) == 1, "LES_wale": int(getattr(P, "les", 0)) == 2,
         "Nx": int(P.nx), "Ny": int(P.ny), "Nz": int(P.nz),
         "Nx_tot": int(P.nx) + 2 * NG, "Ny_tot": int(P.ny) + 2 * NG, "Nz_tot": int(P.nz) + 2 * NG,
@@ -177,21 +210,23 @@ def is_reference_bcs(P) -> bool:
         (float(b.rho), float(b.u), float(b.v), float(b.w), float(b.p)) == (1.0, 0.5, 0.0, 0.0, 1.0 / 1.4) for b in fs)
 
 
-def state_and_ghosts(module_path, P, Q: np.ndarray):
+def state_and_ghosts(module_path, P, Q: np.ndarray, typed: bool = False):
     """U = prim2c(Q) at every cell (utils.jl:33-54); then, as a stage does
     (solver.jl:438-443), Q = c2Prim(U) at the interior (utils.jl:2-30) and the ghost fill of one
     process (boundary.jl's fillGhost: fill_x, fill_y, fill_z; the periodic exchange of mpi.jl on
     one process only copies layers that fill_y and fill_z overwrite afterwards). Returns
-    (U from prim2c, Q after c2Prim and the fill, U after the fill)."""
+    (U from prim2c, Q after c2Prim and the fill, U after the fill). typed: Float32 arrays and a
+    module translated with Julia's types."""
     if not is_reference_bcs(P):
         raise ValueError("boundary.jl hard-codes one boundary set; these parameters have another")
-    k = kernels(module_path, P)
+    k = kernels(module_path, P, typed)
+    dtype = np.float32 if typed else np.float64
     nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
     ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
-    U = JArray(np.zeros((5, *Q.shape[1:])))
-    launch(k["prim2c"], ext, U, JArray(Q.astype(np.float64)))
+    U = JArray(np.zeros((5, *Q.shape[1:]), dtype))
+    launch(k["prim2c"], ext, U, JArray(Q.astype(dtype)))
     U0 = U.a.copy()
-    Q2 = JArray(np.zeros(Q.shape))
+    Q2 = JArray(np.zeros(Q.shape, dtype))
     launch(k["c2Prim"], ext, U, Q2)
     k["fillGhost"](Q2, U, 0, 0)  # rank (0, 0) of one process
     return U0, Q2.a, U.a
@@ -205,18 +240,18 @@ def _advance(k, P, Qj, m, S, Jj, U, dt, xyz=None, Ustate=None):
     updates, as in the reference)."""
     nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
     ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
-    shape = Qj.a.shape[1:]
-    phi = JArray(np.zeros(shape))
+    shape, dt_ = Qj.a.shape[1:], Qj.a.dtype  # intermediates in the state's element type
+    phi = JArray(np.zeros(shape, dt_))
     launch(k["shockSensor"], ext, phi, Qj)
-    F = [JArray(np.zeros((5, nz, ny, nx + 1))), JArray(np.zeros((5, nz, ny + 1, nx))),
-         JArray(np.zeros((5, nz + 1, ny, nx)))]
+    F = [JArray(np.zeros((5, nz, ny, nx + 1), dt_)), JArray(np.zeros((5, nz, ny + 1, nx), dt_)),
+         JArray(np.zeros((5, nz + 1, ny, nx), dt_))]
     scheme = int(getattr(P, "scheme", 0))
     if scheme:
         name = "Eigen_reconstruct_" if scheme == 1 else "Conser_reconstruct_"
         for d, suf in enumerate("ijk"):
             launch(k[name + suf], ext, Qj, U if Ustate is None else Ustate, phi, S[d], F[d], *xyz)
     else:
-        Fp, Fm = JArray(np.zeros((5, *shape))), JArray(np.zeros((5, *shape)))
+        Fp, Fm = JArray(np.zeros((5, *shape), dt_)), JArray(np.zeros((5, *shape), dt_))
         split = k[SPLITS[int(P.split_method)]]
         for d, name in enumerate("xyz"):
             launch(split, ext, Qj, Fp, Fm, S[d], m[3 * d], m[3 * d + 1], m[3 * d + 2])
@@ -224,7 +259,7 @@ def _advance(k, P, Qj, m, S, Jj, U, dt, xyz=None, Ustate=None):
                 launch(k["advect_" + name + "c"], ext, F[d], phi, S[d], Fp, Fm, Qj, m[3 * d], m[3 * d + 1], m[3 * d + 2])
             else:
                 launch(k["advect_" + name], ext, F[d], phi, S[d], Fp, Fm, 5)
-    Fv = [JArray(np.zeros((4, nz + 4, ny + 4, nx + 4))) for _ in range(3)]
+    Fv = [JArray(np.zeros((4, nz + 4, ny + 4, nx + 4), dt_)) for _ in range(3)]
     if int(P.viscous):
         launch(k["viscousFlux"], ext, *Fv, Qj, *m, Jj)
     launch(k["div"], (nx, ny, nz), U, *F, *Fv, dt, Jj)
@@ -238,41 +273,47 @@ def _coords(P, xyz):
     return [JArray(np.asarray(a, dtype=np.float64)) for a in xyz]
 
 
-def _metric_arrays(metrics, J):
-    m = [JArray(metrics[n].astype(np.float64)) for n in range(9)]
-    # solver.jl:286-288: s = sqrt(a^2 + b^2 + c^2) of each metric row
-    S = [JArray(np.sqrt(metrics[3 * d] ** 2 + metrics[3 * d + 1] ** 2 + metrics[3 * d + 2] ** 2)) for d in range(3)]
-    return m, S, JArray(J.astype(np.float64))
+def _metric_arrays(metrics, J, dtype=np.float64):
+    m = [JArray(metrics[n].astype(dtype)) for n in range(9)]
+    # solver.jl:286-288: s = sqrt(a^2 + b^2 + c^2) of each metric row, in the arrays' type
+    S = [JArray(np.sqrt(m[3 * d].a ** 2 + m[3 * d + 1].a ** 2 + m[3 * d + 2].a ** 2)) for d in range(3)]
+    return m, S, JArray(J.astype(dtype))
 
 
 def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int, Q0: np.ndarray | None = None,
-              xyz=None):
+              xyz=None, typed: bool = False):
     """nsteps SSP-RK3 steps of time_step's loop (solver.jl:416-444; no local time step, no
     filter) from the conserved state U0 and its ghost-filled primitive state Q0 (formed from U0
-    as a stage forms it when not given), for boundary.jl's boundary set. Returns (U, Q)."""
+    as a stage forms it when not given), for boundary.jl's boundary set; xyz: the cell-centre
+    coordinates (x, y, z) for the finite-volume schemes; typed: Float32 arrays, dt and linComb
+    weights (0.25f0, 0.75f0, 2/3f0, 1/3f0) and a module translated with Julia's types.
+    Returns (U, Q)."""
     if not is_reference_bcs(P):
         raise ValueError("boundary.jl hard-codes one boundary set; these parameters have another")
-    k = kernels(module_path, P)
+    k = kernels(module_path, P, typed)
+    dtype = np.float32 if typed else np.float64
+    f = np.float32 if typed else float
     nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
     ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
-    m, S, Jj = _metric_arrays(metrics, J)
+    m, S, Jj = _metric_arrays(metrics, J, dtype)
     xyz = _coords(P, xyz)
-    U = JArray(U0.astype(np.float64).copy())
+    U = JArray(U0.astype(dtype).copy())
+    dt = f(dt)
     if Q0 is None:
-        Q = JArray(np.zeros((6, *U0.shape[1:])))
+        Q = JArray(np.zeros((6, *U0.shape[1:]), dtype))
         launch(k["c2Prim"], ext, U, Q)
         k["fillGhost"](Q, U, 0, 0)
     else:
-        Q = JArray(Q0.astype(np.float64).copy())
+        Q = JArray(Q0.astype(dtype).copy())
     for _ in range(nsteps):
         for krk in (1, 2, 3):
             if krk == 1:
                 Un = JArray(U.a.copy())
             _advance(k, P, Q, m, S, Jj, U, dt, xyz)
             if krk == 2:
-                launch(k["linComb"], ext, U, Un, 5, 0.25, 0.75)
+                launch(k["linComb"], ext, U, Un, 5, f(0.25), f(0.75))
             elif krk == 3:
-                launch(k["linComb"], ext, U, Un, 5, 2 / 3, 1 / 3)
+                launch(k["linComb"], ext, U, Un, 5, f(2) / f(3), f(1) / f(3))
             launch(k["c2Prim"], ext, U, Q)
             k["fillGhost"](Q, U, 0, 0)
     return U.a, Q.a
@@ -350,19 +391,21 @@ def filter_pass(module_path, P, U: np.ndarray, Q: np.ndarray) -> np.ndarray:
 SPLITS = ("fluxSplit_SW", "fluxSplit_LF", "fluxSplit_VL", "fluxSplit_AUSM")
 
 
-def rhs(module_path, P, Q: np.ndarray, metrics: np.ndarray, J: np.ndarray, xyz=None) -> np.ndarray:
+def rhs(module_path, P, Q: np.ndarray, metrics: np.ndarray, J: np.ndarray, xyz=None, typed: bool = False) -> np.ndarray:
     """dU/dt at the interior (zero elsewhere) of the reference's RHS from the ghost-filled
     primitive state Q (6, Nt...), the nine J^-1-scaled metrics and J: the advance of one stage
     into a zero accumulator with dt = 1. The finite-volume schemes reconstruct U = prim2c(Q)
-    (utils.jl:33-54, every cell) on the cell-centre coordinates xyz = (x, y, z)."""
-    k = kernels(module_path, P)
-    m, S, Jj = _metric_arrays(metrics, J)
-    Qj = JArray(Q.astype(np.float64))
+    (utils.jl:33-54, every cell) on the cell-centre coordinates xyz = (x, y, z). typed: a module
+    translated with Julia's types, on Float32 arrays (the reference's CuArray{Float32})."""
+    k = kernels(module_path, P, typed)
+    dtype = np.float32 if typed else np.float64
+    m, S, Jj = _metric_arrays(metrics, J, dtype)
+    Qj = JArray(Q.astype(dtype))
     xyz = _coords(P, xyz)
     Ustate = None
     if xyz is not None:
         Ustate = JArray(np.zeros((5, *Q.shape[1:])))
         launch(k["prim2c"], (int(P.nx) + 2 * NG, int(P.ny) + 2 * NG, int(P.nz) + 2 * NG), Ustate, Qj)
-    U = JArray(np.zeros((5, *Q.shape[1:])))
-    _advance(k, P, Qj, m, S, Jj, U, 1.0, xyz, Ustate)
+    U = JArray(np.zeros((5, *Q.shape[1:]), dtype))
+    _advance(k, P, Qj, m, S, Jj, U, np.float32(1) if typed else 1.0, xyz, Ustate)
     return U.a

@@ -18,7 +18,12 @@ inputs);
   directions, the RHS and, for boundary.jl's boundary set, two SSP-RK3 steps, from the
   translation with jl2py.CORRECTIONS applied, and the face fluxes of the translation as
   written (two defects of FVM.jl: the corrected and as-written translations differ on the
-  Roe-characteristic WENO5 faces and on the component-wise y and z faces only).
+  Roe-characteristic WENO5 faces and on the component-wise y and z faces only);
+- the reference's Float32 arithmetic: the translation with Julia's types kept (jl2py typed:
+  Float32 arrays, f0 literals and ::Float32 locals, the Float64 WENO7 epsilon and what it
+  promotes) on the finite-difference cases' inputs rounded to Float32, as SHA-256 digests of
+  the RHS and, for boundary.jl's boundary set, of prim2c, c2Prim with the ghost fill and two
+  SSP-RK3 steps (Float32 dt and weights), all little-endian binary32.
 The file also records SHA-256 digests of the translated Julia files and of the generated
 modules. Needs the reference tree (read only):
 
@@ -98,6 +103,25 @@ def metrics_digest(m, J) -> str:
     return h.hexdigest()
 
 
+def f32_digest(*arrays) -> str:
+    """SHA-256 of the arrays as little-endian binary32, in order."""
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype="<f4").tobytes())
+    return h.hexdigest()
+
+
+def _ref32(typed, P, Q, m, J, name):
+    """The Float32 digests of one finite-difference case (no LES: the Float32 form has none)."""
+    Q32, m32, J32 = (np.asarray(a, dtype=np.float32) for a in (Q, m, J))
+    out = {f"{name}__rhs32_sha256": np.array(f32_digest(runtime.rhs(typed, P, Q32, m32, J32, typed=True)))}
+    if runtime.is_reference_bcs(P):
+        U0, Qf, Uf = runtime.state_and_ghosts(typed, P, Q32, typed=True)
+        U, Qs = runtime.rk3_steps(typed, P, U0, m32, J32, RK3_DT, RK3_STEPS, Q0=Q32, typed=True)
+        out[f"{name}__state32_sha256"] = np.array(f32_digest(U0, Qf, Uf, U, Qs))
+    return out
+
+
 def _golden():
     spec = importlib.util.spec_from_file_location("make_golden", HERE / "make_golden.py")
     mod = importlib.util.module_from_spec(spec)
@@ -121,13 +145,16 @@ def main() -> None:
     ref = Path(a.ref)
     module = ROOT / "oracle" / "_ref" / "jl_kernels.py"
     corrected = ROOT / "oracle" / "_ref" / "jl_kernels_corrected.py"
+    typed = ROOT / "oracle" / "_ref" / "jl_kernels_typed.py"
     module.parent.mkdir(parents=True, exist_ok=True)
     module.write_text(jl2py.translate_tree(ref))
     corrected.write_text(jl2py.translate_tree(ref, corrected=True))
+    typed.write_text(jl2py.translate_tree(ref, typed=True))
     out = {"provenance": np.array(json.dumps({
         "translated": {f: hashlib.sha256((ref / f).read_bytes()).hexdigest() for f in jl2py.FILES},
         "module_sha256": hashlib.sha256(module.read_bytes()).hexdigest(),
         "corrected_module_sha256": hashlib.sha256(corrected.read_bytes()).hexdigest(),
+        "typed_module_sha256": hashlib.sha256(typed.read_bytes()).hexdigest(),
         "corrections": [c[-1] for c in jl2py.CORRECTIONS],
         "semantics": "every value binary64; Julia's literal powers x^2, x^3 as products, other powers by C pow",
         "rk3": {"dt": RK3_DT, "steps": RK3_STEPS}}))}
@@ -145,6 +172,7 @@ def main() -> None:
         report[f.stem] = r
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, d["Q"], d["metrics"], d["J"], f.stem))
+        out.update(_ref32(typed, P, d["Q"], d["metrics"], d["J"], f.stem))
     g = _golden()
     for name, spec in VISCOUS.items():
         n, params = spec["n"], dict(spec["params"])
@@ -163,6 +191,8 @@ def main() -> None:
         report[name] = r
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, Q, m, J, name))
+        if not params.get("les", 0):
+            out.update(_ref32(typed, P, Q, m, J, name))
         # the local time step (utils.jl:73-99) and the two filters (solver.jl:446-470)
         U = runtime.prim2c(module, P, Q)
         out[f"{name}__local_dt"] = runtime.local_dt(module, P, Q, m, J)

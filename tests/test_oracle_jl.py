@@ -138,6 +138,38 @@ def test_translation_reproduces_the_fixture_digest():
         assert hashlib.sha256((REF / f).read_bytes()).hexdigest() == h, f
     assert hashlib.sha256(jl2py.translate_tree(REF).encode()).hexdigest() == prov["module_sha256"]
     assert hashlib.sha256(jl2py.translate_tree(REF, True).encode()).hexdigest() == prov["corrected_module_sha256"]
+    assert hashlib.sha256(jl2py.translate_tree(REF, typed=True).encode()).hexdigest() == prov["typed_module_sha256"]
+
+
+# ---- the reference's Float32 arithmetic (the REF32 form), from the typed translation
+def _f32_digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype="<f4").tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name", [n for n in _cases()[1] if f"{n}__rhs32_sha256" in _cases()[0].files])
+def test_oracle_float32_form_equals_the_typed_translation(name):
+    """The oracle's Float32 restatement (the reference's own precision: Float32 arrays and
+    arithmetic, WENO7 alphas in Float64 through WENOϵ1::Float64) against the reference's kernels
+    evaluated with Julia's types: the RHS and, for boundary.jl's boundary set, prim2c, c2Prim
+    with the ghost fill and two SSP-RK3 steps, bit for bit."""
+    d, _ = _cases()
+    meta, Q, m, J = _inputs(d, name)
+    P = make_params(*meta["n"], **meta["params"])
+    Q32, J32 = np.asarray(Q, dtype=np.float32), np.asarray(J, dtype=np.float32)
+    m32 = [np.ascontiguousarray(a, dtype=np.float32) for a in m]
+    assert _f32_digest(orc.rhs32(P, Q32, m32, J32)) == str(d[f"{name}__rhs32_sha256"])
+    if f"{name}__state32_sha256" in d.files:
+        rk = json.loads(str(d["provenance"]))["rk3"]
+        U0 = orc.prim2c32(P, Q32)
+        Qf, Uf = orc.c2prim32(P, U0), U0.copy()
+        orc.fill_ghosts32(P, Qf, Uf)
+        Us, Un, Qs = U0.copy(), np.zeros_like(U0), Q32.copy()
+        orc.rk3_32(P, rk["steps"], np.float32(rk["dt"]), Us, Un, Qs, m32, J32)
+        assert _f32_digest(U0, Qf, Uf, Us, Qs) == str(d[f"{name}__state32_sha256"])
 
 
 # ---- the translation rules on small pieces of Julia
@@ -268,3 +300,26 @@ def test_fvm_defects_change_only_the_faces_they_reach():
                 assert np.array_equal(differs, br == 2), (name, dd)
             else:
                 assert differs.all() if dd else not differs.any(), (name, dd)
+
+
+def test_rule_typed_literals_and_locals():
+    """Julia's types kept: Float32 literals, Float64 literals, typed locals converting on every
+    assignment (x op= e included), typed temporaries."""
+    assert jl2py.expr("1/12f0 + WENOϵ1*1e-20 - 2x + 0.5", typed=True) == "1/_f32(12e0) + WENOϵ1*_f64(1e-20) - 2*x + _f64(0.5)"
+    assert jl2py.expr("MMatrix{5, 5, Float32, 25}(undef)", typed=True) == "_mat(5, 5, 32)"
+    py = _py_typed = jl2py.translate("""
+    function g(A, n)
+        s::Float32 = 0.f0
+        t = 0.f0
+        for m = 1:n
+            s += A[m] * 0.1
+            t += A[m] * 0.1
+        end
+        return s, t
+    end
+    """, typed=True)
+    assert "s = _f32(s + (A[m] * _f64(0.1)))" in py and "t += A[m] * _f64(0.1)" in py
+    ns = {"_f32": np.float32, "_f64": np.float64}
+    exec(py, ns)
+    s_, t_ = ns["g"](JArray(np.array([1.0, 2.0], dtype=np.float32)), 2)
+    assert type(s_) is np.float32 and type(t_) is np.float64  # t is Float64 after t += Float64, as in Julia
