@@ -280,6 +280,8 @@ def _typed_literal(m) -> str:
 
 def expr(s: str, typed: bool = False) -> str:
     s = s.replace("CUDA.eps(Float32)", "_eps32()")
+    if typed:
+        s = re.sub(r"\bzeros\(\s*Float(32|64)\s*,", r"_zerosT(\1,", s)
     s = re.sub(r"\bzeros\(\s*Float(32|64)\s*,", "_zeros(", s)
     if ":" in s and "[" in s:
         s = _ranges_in_brackets(s)
@@ -290,6 +292,8 @@ def expr(s: str, typed: bool = False) -> str:
     s = re.sub(r"MMatrix\{\s*([^,}]+)\s*,\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1, \2)", s)
     s = re.sub(r"MVector\{\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1)", s)
     s = re.sub(r"SVector\{[^}]*\}\s*\(", "_vec(", s)
+    if typed:  # Int / Int is a Float64 quotient (1/60 -> _f64(1/60))
+        s = re.sub(r"(?<![\w.])(\d+)\s*/\s*(\d+)(?![\w.])", r"_f64(\1/\2)", s)
     if typed:  # Float32 literals (12f0) -> _f32(12e0), Float64 ones (1e-20, 0.5) -> _f64(...)
         s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][-+]?\d+)?|\.\d+(?:[eE][-+]?\d+)?|\d+(?:[eE][-+]?\d+)?)"
                    r"(?:f(-?\d+))?(?![\w.])", _typed_literal, s)
@@ -337,6 +341,8 @@ def _strip_macros(s: str) -> str:
 def _strip_annot(lhs: str) -> str:
     return re.sub(r"::\s*\w+(\{[^}]*\})?", "", lhs).strip()
 
+
+_expr = expr  # for translate_script, whose local name expr selects the typed form
 
 _ANNOT = re.compile(r"^\s*([^\W\d]\w*)\s*::\s*Float(32|64)\s*$")
 
@@ -435,11 +441,12 @@ def translate(src: str, typed: bool = False) -> str:
     return "\n".join(fixed) + "\n"
 
 
-def translate_script(src: str, first: int, last: int) -> str:
+def translate_script(src: str, first: int, last: int, typed: bool = False) -> str:
     """Python of the top-level statements of lines first..last (1-based) of a Julia script:
     function definitions, assignments, `@.` broadcasts (-> _bset(lhs, rhs), elementwise on whole
     arrays, the same operations per element), loops `for k ∈ a:b, j ∈ c:d, ...` (nested, the
-    first variable outermost) and ifs."""
+    first variable outermost) and ifs. typed: Julia's element types kept, as translate()."""
+    expr = (lambda e: _expr(e, True)) if typed else _expr
     lines = src.splitlines()[first - 1:last]
     out: list[str] = []
     stack: list[int] = []  # indentation levels opened by each block
@@ -516,7 +523,7 @@ def translate_tree(root: Path, corrected: bool = False, typed: bool = False) -> 
         parts.append(translate(apply_corrections(name, src) if corrected else src, typed))
     a, b = METRIC_LINES
     parts.append(f"# ---- parse_mesh.jl:{a}-{b}, as the body of _metrics()\n")
-    body = translate_script((root / "parse_mesh.jl").read_text(), a, b)
+    body = translate_script((root / "parse_mesh.jl").read_text(), a, b, typed)
     parts.append("def _metrics(x, y, z):\n" + "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) +
                  "    return (dξdx, dξdy, dξdz, dηdx, dηdy, dηdz, dζdx, dζdy, dζdz), J\n")
     return "\n".join(parts)

@@ -167,6 +167,8 @@ def kernels(module_path: Path | str, P, typed: bool = False) -> dict:
     if typed:  # SVector{7, Float32}(Float64 quotients); Linear = UP7 * Linear_ϕ + CD6 * (1 - Linear_ϕ)
         linear = (np.array(up7).astype(np.float32) * lp + np.array(cd6).astype(np.float32) * (np.float32(1) - lp))
         g.update(_f32=np.float32, _f64=np.float64, _eps32=lambda: np.float32(2.0 ** -23), _mat=_tmat,
+                 _zerosT=lambda bits, *dims: JArray(np.zeros(tuple(reversed(dims)),
+                                                             np.float32 if bits == 32 else np.float64)),
                  max=_tjmax, min=_tjmin, sqrt=_tsqrt, zero=lambda a: type(a)(0) if isinstance(a, np.generic) else 0)
     else:
         linear = np.array([u * lp + c * (1.0 - lp) for u, c in zip(up7, cd6)])
@@ -319,11 +321,14 @@ def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int
     return U.a, Q.a
 
 
-def metrics(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray):
+def metrics(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray, typed: bool = False):
     """parse_mesh.jl:139-248 on the coordinates with ghosts: the nine J^-1-scaled metrics
-    (dξ/dx, dξ/dy, dξ/dz, dη/dx, ..., dζ/dz) and J, each (Nz_tot, Ny_tot, Nx_tot)."""
-    k = kernels(module_path, P)
-    m, J = k["_metrics"](*(JArray(np.asarray(c, dtype=np.float64)) for c in (x, y, z)))
+    (dξ/dx, dξ/dy, dξ/dz, dη/dx, ..., dζ/dz) and J, each (Nz_tot, Ny_tot, Nx_tot). typed: the
+    script's own precision (Float32 coordinates and arrays, Float64 coefficients) from a module
+    translated with Julia's types."""
+    k = kernels(module_path, P, typed)
+    dtype = np.float32 if typed else np.float64
+    m, J = k["_metrics"](*(JArray(np.asarray(c, dtype=dtype)) for c in (x, y, z)))
     return np.stack([a.a for a in m]), J.a
 
 

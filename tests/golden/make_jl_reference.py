@@ -23,7 +23,8 @@ inputs);
   Float32 arrays, f0 literals and ::Float32 locals, the Float64 WENO7 epsilon and what it
   promotes) on the finite-difference cases' inputs rounded to Float32, as SHA-256 digests of
   the RHS and, for boundary.jl's boundary set, of prim2c, c2Prim with the ghost fill and two
-  SSP-RK3 steps (Float32 dt and weights), all little-endian binary32.
+  SSP-RK3 steps (Float32 dt and weights), and of parse_mesh.jl:139-248 on the coordinates
+  rounded to Float32 (its Float32 arrays and Float64 coefficients), all little-endian binary32.
 The file also records SHA-256 digests of the translated Julia files and of the generated
 modules. Needs the reference tree (read only):
 
@@ -111,10 +112,12 @@ def f32_digest(*arrays) -> str:
     return h.hexdigest()
 
 
-def _ref32(typed, P, Q, m, J, name):
+def _ref32(typed, P, Q, m, J, name, xyz):
     """The Float32 digests of one finite-difference case (no LES: the Float32 form has none)."""
     Q32, m32, J32 = (np.asarray(a, dtype=np.float32) for a in (Q, m, J))
-    out = {f"{name}__rhs32_sha256": np.array(f32_digest(runtime.rhs(typed, P, Q32, m32, J32, typed=True)))}
+    out = {f"{name}__rhs32_sha256": np.array(f32_digest(runtime.rhs(typed, P, Q32, m32, J32, typed=True))),
+           f"{name}__metrics32_sha256": np.array(f32_digest(*runtime.metrics(
+               typed, P, *(np.asarray(a, dtype=np.float32) for a in xyz), typed=True)))}
     if runtime.is_reference_bcs(P):
         U0, Qf, Uf = runtime.state_and_ghosts(typed, P, Q32, typed=True)
         U, Qs = runtime.rk3_steps(typed, P, U0, m32, J32, RK3_DT, RK3_STEPS, Q0=Q32, typed=True)
@@ -172,7 +175,7 @@ def main() -> None:
         report[f.stem] = r
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, d["Q"], d["metrics"], d["J"], f.stem))
-        out.update(_ref32(typed, P, d["Q"], d["metrics"], d["J"], f.stem))
+        out.update(_ref32(typed, P, d["Q"], d["metrics"], d["J"], f.stem, (d["x"], d["y"], d["z"])))
     g = _golden()
     for name, spec in VISCOUS.items():
         n, params = spec["n"], dict(spec["params"])
@@ -192,7 +195,7 @@ def main() -> None:
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, Q, m, J, name))
         if not params.get("les", 0):
-            out.update(_ref32(typed, P, Q, m, J, name))
+            out.update(_ref32(typed, P, Q, m, J, name, (x, y, z)))
         # the local time step (utils.jl:73-99) and the two filters (solver.jl:446-470)
         U = runtime.prim2c(module, P, Q)
         out[f"{name}__local_dt"] = runtime.local_dt(module, P, Q, m, J)
