@@ -321,7 +321,7 @@ def expr(s: str, typed: bool = False) -> str:
 
 
 def _strip_macros(s: str) -> str:
-    s = re.sub(r"@(inbounds|fastmath|inline)\s+", "", s).strip()
+    s = re.sub(r"@(inbounds|fastmath|inline|view)\s+", "", s).strip()  # a view reads what the slice does
     # a kernel launch of a host function: @cuda <keyword = value ...> f(args) -> _cuda(f, args)
     m = re.match(r"@cuda\s+(.*)$", s)
     if m:
@@ -509,6 +509,10 @@ def translate_script(src: str, first: int, last: int, typed: bool = False) -> st
 # the metric and Jacobian computation of parse_mesh.jl (its CD6 / CD2 stencils of the
 # coordinates, J and the J^-1-scaled metrics), without the file output that follows
 METRIC_LINES = (139, 248)
+# the same computation in SCU-benchmark/readfort.jl (Float32 coefficients): its CD6 / CD2
+# functions and the body of computeMetrics before its file output
+READFORT = "SCU-benchmark/readfort.jl"
+READFORT_LINES = ((104, 117), (120, 208))
 
 
 def translate_tree(root: Path, corrected: bool = False, typed: bool = False) -> str:
@@ -525,6 +529,12 @@ def translate_tree(root: Path, corrected: bool = False, typed: bool = False) -> 
     parts.append(f"# ---- parse_mesh.jl:{a}-{b}, as the body of _metrics()\n")
     body = translate_script((root / "parse_mesh.jl").read_text(), a, b, typed)
     parts.append("def _metrics(x, y, z):\n" + "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) +
+                 "    return (dξdx, dξdy, dξdz, dηdx, dηdy, dηdz, dζdx, dζdy, dζdz), J\n")
+    rf = (root / READFORT).read_text()
+    parts.append(f"# ---- {READFORT}:" + ", ".join(f"{a}-{b}" for a, b in READFORT_LINES) +
+                 ", as the body of _metrics_readfort()\n")
+    body = "".join(translate_script(rf, a, b, typed) for a, b in READFORT_LINES)
+    parts.append("def _metrics_readfort(x, y, z):\n" + "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) +
                  "    return (dξdx, dξdy, dξdz, dηdx, dηdy, dηdz, dζdx, dζdy, dζdz), J\n")
     return "\n".join(parts)
 

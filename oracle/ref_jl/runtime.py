@@ -321,14 +321,17 @@ def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int
     return U.a, Q.a
 
 
-def metrics(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray, typed: bool = False):
-    """parse_mesh.jl:139-248 on the coordinates with ghosts: the nine J^-1-scaled metrics
-    (dξ/dx, dξ/dy, dξ/dz, dη/dx, ..., dζ/dz) and J, each (Nz_tot, Ny_tot, Nx_tot). typed: the
-    script's own precision (Float32 coordinates and arrays, Float64 coefficients) from a module
-    translated with Julia's types."""
+def metrics(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray, typed: bool = False,
+            source: str = "parse_mesh"):
+    """parse_mesh.jl:139-248 (source "readfort": SCU-benchmark/readfort.jl:104-208) on the
+    coordinates with ghosts: the nine J^-1-scaled metrics (dξ/dx, dξ/dy, dξ/dz, dη/dx, ...,
+    dζ/dz) and J, each (Nz_tot, Ny_tot, Nx_tot). typed: the script's own precision (Float32
+    coordinates and arrays; parse_mesh.jl's Float64 coefficients, readfort.jl's Float32 ones)
+    from a module translated with Julia's types."""
     k = kernels(module_path, P, typed)
     dtype = np.float32 if typed else np.float64
-    m, J = k["_metrics"](*(JArray(np.asarray(c, dtype=dtype)) for c in (x, y, z)))
+    fn = k["_metrics" if source == "parse_mesh" else "_metrics_readfort"]
+    m, J = fn(*(JArray(np.asarray(c, dtype=dtype)) for c in (x, y, z)))
     return np.stack([a.a for a in m]), J.a
 
 

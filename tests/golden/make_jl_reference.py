@@ -23,8 +23,9 @@ inputs);
   Float32 arrays, f0 literals and ::Float32 locals, the Float64 WENO7 epsilon and what it
   promotes) on the finite-difference cases' inputs rounded to Float32, as SHA-256 digests of
   the RHS and, for boundary.jl's boundary set, of prim2c, c2Prim with the ghost fill and two
-  SSP-RK3 steps (Float32 dt and weights), and of parse_mesh.jl:139-248 on the coordinates
-  rounded to Float32 (its Float32 arrays and Float64 coefficients), all little-endian binary32.
+  SSP-RK3 steps (Float32 dt and weights), and of the metrics of parse_mesh.jl:139-248 (Float32
+  arrays, Float64 coefficients) and of SCU-benchmark/readfort.jl:104-208 (Float32 coefficients)
+  on the coordinates rounded to Float32, all little-endian binary32.
 The file also records SHA-256 digests of the translated Julia files and of the generated
 modules. Needs the reference tree (read only):
 
@@ -117,7 +118,9 @@ def _ref32(typed, P, Q, m, J, name, xyz):
     Q32, m32, J32 = (np.asarray(a, dtype=np.float32) for a in (Q, m, J))
     out = {f"{name}__rhs32_sha256": np.array(f32_digest(runtime.rhs(typed, P, Q32, m32, J32, typed=True))),
            f"{name}__metrics32_sha256": np.array(f32_digest(*runtime.metrics(
-               typed, P, *(np.asarray(a, dtype=np.float32) for a in xyz), typed=True)))}
+               typed, P, *(np.asarray(a, dtype=np.float32) for a in xyz), typed=True))),
+           f"{name}__metrics32_readfort_sha256": np.array(f32_digest(*runtime.metrics(
+               typed, P, *(np.asarray(a, dtype=np.float32) for a in xyz), typed=True, source="readfort")))}
     if runtime.is_reference_bcs(P):
         U0, Qf, Uf = runtime.state_and_ghosts(typed, P, Q32, typed=True)
         U, Qs = runtime.rk3_steps(typed, P, U0, m32, J32, RK3_DT, RK3_STEPS, Q0=Q32, typed=True)
@@ -154,7 +157,8 @@ def main() -> None:
     corrected.write_text(jl2py.translate_tree(ref, corrected=True))
     typed.write_text(jl2py.translate_tree(ref, typed=True))
     out = {"provenance": np.array(json.dumps({
-        "translated": {f: hashlib.sha256((ref / f).read_bytes()).hexdigest() for f in jl2py.FILES},
+        "translated": {f: hashlib.sha256((ref / f).read_bytes()).hexdigest()
+                       for f in (*jl2py.FILES, "parse_mesh.jl", jl2py.READFORT)},
         "module_sha256": hashlib.sha256(module.read_bytes()).hexdigest(),
         "corrected_module_sha256": hashlib.sha256(corrected.read_bytes()).hexdigest(),
         "typed_module_sha256": hashlib.sha256(typed.read_bytes()).hexdigest(),

@@ -174,10 +174,10 @@ def test_oracle_float32_form_equals_the_typed_translation(name):
 
 @pytest.mark.parametrize("name", [n for n in _cases()[1] if f"{n}__metrics32_sha256" in _cases()[0].files])
 def test_float32_set_up_metrics_equal_the_typed_translation(name):
-    """meshgen.metrics_f32 with parse_mesh.jl's coefficients (the host set-up of the Float32
-    form; the device's f3d_compute_metrics_f32 equals it bit for bit) against parse_mesh.jl:
-    139-248 evaluated in its own types: Float32 coordinates and arrays, Float64 CD6 / CD2
-    coefficients (1/60, 0.5, ...), bit for bit."""
+    """meshgen.metrics_f32 (the host set-up of the Float32 form; the device's
+    f3d_compute_metrics_f32 equals it bit for bit) against parse_mesh.jl:139-248 and
+    readfort.jl:104-208 evaluated in their own types: Float32 coordinates and arrays, Float64
+    (parse_mesh.jl: 1/60, 0.5, ...) or Float32 (readfort.jl) CD6 / CD2 coefficients, bit for bit."""
     from flame3d_mhd_gb300 import meshgen
     d, _ = _cases()
     src = d if f"{name}__x" in d.files else np.load(ROOT / "tests" / "golden" / f"{name}.npz", allow_pickle=True)
@@ -185,6 +185,9 @@ def test_float32_set_up_metrics_equal_the_typed_translation(name):
     x, y, z = (np.asarray(src[pre + a], dtype=np.float32) for a in "xyz")
     m, J = meshgen.metrics_f32(x, y, z, coefficients="parse_mesh")
     assert _f32_digest(*m, J) == str(d[f"{name}__metrics32_sha256"])
+    # readfort.jl:104-208, the same stencils with Float32 coefficients (1/60f0, 0.5f0, ...)
+    m, J = meshgen.metrics_f32(x, y, z, coefficients="readfort")
+    assert _f32_digest(*m, J) == str(d[f"{name}__metrics32_readfort_sha256"])
 
 
 # ---- the translation rules on small pieces of Julia
