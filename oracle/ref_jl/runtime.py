@@ -15,10 +15,14 @@ and run.jl gave them:
   zero accumulator with dt = 1, so it ends holding J times the flux divergence, the RHS;
 - prim2c, c2Prim and the ghost fill of one process for boundary.jl's own boundary set, the
   RK3 stage loop of time_step, its local time step and its filtering pass;
-- the metrics and J of parse_mesh.jl (a script, translated as the body of one function).
+- the metrics and J of parse_mesh.jl and of SCU-benchmark/readfort.jl (scripts, each
+  translated as the body of one function).
 
-Every value is a Python float (binary64): the reference's algorithm in FP64, in its own
-operation order. Slow (one Python call per thread): grids of a few hundred cells.
+Every value is a binary64 NumPy scalar (IEEE: 0/0 is NaN, as in Julia): the reference's
+algorithm in FP64, in its own operation order. With typed=True (a module translated with
+Julia's types) the arrays are Float32, run.jl's constants Float32 and the helpers keep and
+promote types as Julia does: the reference's own precision. Slow (one Python call per
+thread): grids of a few hundred cells.
 """
 from __future__ import annotations
 

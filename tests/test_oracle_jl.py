@@ -325,7 +325,7 @@ def test_rule_typed_literals_and_locals():
     assignment (x op= e included), typed temporaries."""
     assert jl2py.expr("1/12f0 + WENOϵ1*1e-20 - 2x + 0.5", typed=True) == "1/_f32(12e0) + WENOϵ1*_f64(1e-20) - 2*x + _f64(0.5)"
     assert jl2py.expr("MMatrix{5, 5, Float32, 25}(undef)", typed=True) == "_mat(5, 5, 32)"
-    py = _py_typed = jl2py.translate("""
+    py = jl2py.translate("""
     function g(A, n)
         s::Float32 = 0.f0
         t = 0.f0
