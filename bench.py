@@ -139,8 +139,10 @@ def reduce_max(x: float, device=None) -> float:
 
 
 def cpu_sample(target_s: float = 12.0, max_steps: int = 8) -> dict:
-    """The oracle (C++ restatement of the reference algorithm, OpenMP on every host core) on
-    the same workload: one untimed step, then whole RK3 steps until about target_s."""
+    """The oracle (C++ restatement of the reference algorithm, OpenMP on every host core; its
+    RHS and RK3 steps equal the reference's kernels translated into Python bit for bit on the
+    fixture cases) on the same workload: one untimed step, then whole RK3 steps until about
+    target_s."""
     import numpy as np
 
     from flame3d_mhd_gb300 import cases
@@ -236,7 +238,8 @@ def run_reference(args):
                    "parallelism": "openmp", "threads": threads},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} SSP-RK3 steps of the full workload after {max(args.warmup, 1)} "
-                                   f"untimed; C++ restatement of the reference formulas (Julia absent)"},
+                                   f"untimed; C++ restatement of the reference formulas (Julia absent), equal bit "
+                                   f"for bit to the reference's kernels translated into Python on the fixture cases"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
