@@ -43,8 +43,8 @@ int validate_params(const f3d_params& p, std::string& why) {
     if (p.character != 0 && p.character != 1) { why = "character must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.viscous != 0 && p.viscous != 1) { why = "viscous must be 0 or 1"; return F3D_ERR_ARG; }
     if (p.precision < F3D_PREC_FP64 || p.precision > F3D_PREC_REF32) { why = "unknown precision"; return F3D_ERR_ARG; }
-    if (p.precision == F3D_PREC_REF32 && (p.lts || p.filter || p.les)) {
-        why = "the Float32 reference form has no local time stepping, filters or LES";
+    if (p.precision == F3D_PREC_REF32 && (p.lts || p.filter)) {
+        why = "the Float32 reference form has no local time stepping or filters";
         return F3D_ERR_UNSUPPORTED;
     }
     if (p.scheme < F3D_SCHEME_FDM || p.scheme > F3D_SCHEME_FVM_CONS) { why = "unknown scheme"; return F3D_ERR_ARG; }

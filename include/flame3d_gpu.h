@@ -278,10 +278,10 @@ int f3d_debug_round_f32(const double* in, float* out, long long n, f3d_stream st
  * f3d_rk3_stage and f3d_rk3_steps on Float32 arrays of the same shapes: the reference's
  * CuArray{Float32} U, Un, Q, metrics and J (solver.jl:238-337) pass unchanged. The
  * computation follows the reference's Float32 operations (c2Prim clamps at eps(Float32),
- * Float32 splitting, sensor, UP7/WENO5 and viscous fluxes, WENO7 weights in FP64, Float32
- * RK update); FP64 entries and these refuse each other's contexts (F3D_ERR_ARG). No
- * inflow-profile faces, local time stepping, filters, LES, adjoint or finite-volume
- * scheme in this form (F3D_ERR_UNSUPPORTED at f3d_create). */
+ * Float32 splitting, sensor, UP7/WENO5 and viscous fluxes (with either LES model),
+ * WENO7 weights in FP64, Float32 RK update); FP64 entries and these refuse each other's
+ * contexts (F3D_ERR_ARG). No inflow-profile faces, local time stepping, filters, adjoint
+ * or finite-volume scheme in this form (F3D_ERR_UNSUPPORTED at f3d_create). */
 int f3d_set_metrics_f32(f3d_ctx* ctx, const float* const metrics[9], const float* jac, f3d_stream stream);
 /* The Float32 metrics and J the reference's set-up writes to metrics.h5, from Float32
  * coordinates with ghosts (Nxt,Nyt,Nzt): the CD6 / one-sided CD2 differences with Float32

@@ -114,7 +114,7 @@ def f32_digest(*arrays) -> str:
 
 
 def _ref32(typed, P, Q, m, J, name, xyz):
-    """The Float32 digests of one finite-difference case (no LES: the Float32 form has none)."""
+    """The Float32 digests of one finite-difference case."""
     Q32, m32, J32 = (np.asarray(a, dtype=np.float32) for a in (Q, m, J))
     out = {f"{name}__rhs32_sha256": np.array(f32_digest(runtime.rhs(typed, P, Q32, m32, J32, typed=True))),
            f"{name}__metrics32_sha256": np.array(f32_digest(*runtime.metrics(
@@ -198,8 +198,7 @@ def main() -> None:
         report[name] = r
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, Q, m, J, name))
-        if not params.get("les", 0):
-            out.update(_ref32(typed, P, Q, m, J, name, (x, y, z)))
+        out.update(_ref32(typed, P, Q, m, J, name, (x, y, z)))
         # the local time step (utils.jl:73-99) and the two filters (solver.jl:446-470)
         U = runtime.prim2c(module, P, Q)
         out[f"{name}__local_dt"] = runtime.local_dt(module, P, Q, m, J)

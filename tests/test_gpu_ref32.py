@@ -108,10 +108,11 @@ def test_pointwise_bitwise(gpu_lib):
         s.close()
 
 
-@pytest.mark.parametrize("bcs,character,viscous", [("periodic", 1, 0), ("periodic", 0, 0), ("walls", 1, 1),
-                                                   ("mixed", 0, 1)])
-def test_rhs_against_the_reference_arithmetic(gpu_lib, bcs, character, viscous):
-    P, P64, (m, J, Q, U), (m32, J32, Q32, U32), s, keep = _case(bcs, character=character, viscous=viscous)
+@pytest.mark.parametrize("bcs,character,viscous,les", [("periodic", 1, 0, 0), ("periodic", 0, 0, 0), ("walls", 1, 1, 0),
+                                                       ("mixed", 0, 1, 0), ("walls", 1, 1, 1), ("mixed", 0, 1, 2)])
+def test_rhs_against_the_reference_arithmetic(gpu_lib, bcs, character, viscous, les):
+    """les: Smagorinsky (1) or WALE (2) eddy viscosity in the Float32 viscous fluxes."""
+    P, P64, (m, J, Q, U), (m32, J32, Q32, U32), s, keep = _case(bcs, character=character, viscous=viscous, les=les)
     r = host(s.rhs(dev(Q32))).astype(np.float64)
     r32 = orc.rhs32(P, Q32, m32, J32).astype(np.float64)
     Q64 = Q32.astype(np.float64)
@@ -123,6 +124,9 @@ def test_rhs_against_the_reference_arithmetic(gpu_lib, bcs, character, viscous):
     print(msg)
     assert gpu_orc <= max(2e-6, 2.0 * orc_ld), msg
     assert gpu_ld <= 1.5 * orc_ld + 2e-6, msg
+    if les:  # the eddy viscosity moves the answer far beyond the bars above (2e-4 .. 4e-4)
+        r0 = orc.rhs32(params_copy(P, les=0), Q32, m32, J32).astype(np.float64)
+        assert max(float(np.abs(r32[n][I[1:]] - r0[n][I[1:]]).max() / scale[n]) for n in range(5)) > 2e-5
     s.close()
 
 
@@ -170,7 +174,7 @@ def test_ref32_entry_errors(gpu_lib):
     s64.close()
     with pytest.raises(TypeError):
         s.rhs(dev(Q32.astype(np.float64)))
-    for kw in (dict(lts=1, lts_cfl=0.5), dict(les=1)):
+    for kw in (dict(lts=1, lts_cfl=0.5), dict(filter=1)):
         with pytest.raises(F3DError) as e:
             Flame3D(params_copy(P, **kw))
         assert e.value.code == F3D_ERR_UNSUPPORTED
