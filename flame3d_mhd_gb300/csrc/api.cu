@@ -459,8 +459,9 @@ int run_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double*
     last.combine = stage != 1;
     last.ca = stage == 2 ? 0.25 : 2.0 / 3.0;  // utils.jl:57-70 via solver.jl:433-435
     last.cb = stage == 2 ? 0.75 : 1.0 / 3.0;
-    if (ctx->params.lts) {  // compute_dt before flowAdvance (solver.jl:419-420), div_LTS after
-        F3D_CUDA(ctx, launch_local_dt(ctx->dp, Q, ctx->m, ctx->J, ctx->params.lts_cfl, ctx->dtl, st));
+    if (ctx->params.lts) {  // compute_dt at the first stage only (solver.jl:418-421), div_LTS in all
+        if (stage == 1)
+            F3D_CUDA(ctx, launch_local_dt(ctx->dp, Q, ctx->m, ctx->J, ctx->params.lts_cfl, ctx->dtl, st));
         last.dtl = ctx->dtl;
     }
     int rc = run_rhs(ctx, Q, ctx->acc, last, st, fill_current);

@@ -198,7 +198,9 @@ int f3d_rhs(f3d_ctx* ctx, const double* Q, double* dUdt, f3d_stream stream);
 
 /* One SSP-RK3 stage (stage = 1,2,3) exactly as solver.jl:416-444: stage 1 copies U to
  * Un; U += dt L(Q); stage 2: U = U/4 + 3Un/4; stage 3: U = 2U/3 + Un/3; then
- * Q = c2Prim(U) and the ghost fill of Q and U. Q must be ghost-filled on entry. */
+ * Q = c2Prim(U) and the ghost fill of Q and U. Q must be ghost-filled on entry. With
+ * params.lts, stage 1 computes the local time steps from its Q and stages 2 and 3 of the
+ * same context use them (compute_dt at KRK == 1 only, solver.jl:418-421). */
 int f3d_rk3_stage(f3d_ctx* ctx, int stage, double dt, double* U, double* Un, double* Q,
                   f3d_stream stream);
 

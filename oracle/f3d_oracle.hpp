@@ -977,7 +977,10 @@ template <class R, class W> struct Solver {
     void rk3_stage(int stage, R dt, R* U, R* Un, R* Q) {
         const size_t n5 = g.ncell() * 5;
         if (stage == 1) std::memcpy(Un, U, n5 * sizeof(R));
-        if (P.lts) {  // solver.jl:419-420: compute_dt before flowAdvance
+        // solver.jl:418-421: compute_dt inside `if KRK == 1`, before flowAdvance; stages 2
+        // and 3 take the first stage's steps (a lone later stage on a fresh solver computes
+        // them from its own Q, having no first stage)
+        if (P.lts && (stage == 1 || dtl.empty())) {
             dtl.assign(g.ncell(), R(0));
             compute_dt<R>(P, Q, J, S[0].data(), S[1].data(), S[2].data(), dtl.data());
         }

@@ -238,12 +238,13 @@ def state_and_ghosts(module_path, P, Q: np.ndarray, typed: bool = False):
     return U0, Q2.a, U.a
 
 
-def _advance(k, P, Qj, m, S, Jj, U, dt, xyz=None, Ustate=None):
+def _advance(k, P, Qj, m, S, Jj, U, dt, xyz=None, Ustate=None, lts_dt=None):
     """The sensor, flowAdvance (solver.jl:19-188) and div (U += dt J (...)). Finite-difference
     schemes: split and reconstruction per direction. Finite-volume schemes (P.scheme 1:
     Eigen_reconstruct_*, 2: Conser_reconstruct_*): the face kernels of solver.jl:21-31 on the
     cell-centre coordinates xyz, reading Ustate (default U, the stage's state, which div then
-    updates, as in the reference)."""
+    updates, as in the reference). lts_dt: the per-cell time steps of compute_dt, applied by
+    div_LTS (solver.jl:425-426) in place of div with the global dt."""
     nx, ny, nz = int(P.nx), int(P.ny), int(P.nz)
     ext = (nx + 2 * NG, ny + 2 * NG, nz + 2 * NG)
     shape, dt_ = Qj.a.shape[1:], Qj.a.dtype  # intermediates in the state's element type
@@ -268,7 +269,10 @@ def _advance(k, P, Qj, m, S, Jj, U, dt, xyz=None, Ustate=None):
     Fv = [JArray(np.zeros((4, nz + 4, ny + 4, nx + 4), dt_)) for _ in range(3)]
     if int(P.viscous):
         launch(k["viscousFlux"], ext, *Fv, Qj, *m, Jj)
-    launch(k["div"], (nx, ny, nz), U, *F, *Fv, dt, Jj)
+    if lts_dt is None:
+        launch(k["div"], (nx, ny, nz), U, *F, *Fv, dt, Jj)
+    else:
+        launch(k["div_LTS"], (nx, ny, nz), U, *F, *Fv, lts_dt, Jj)
 
 
 def _coords(P, xyz):
@@ -288,9 +292,11 @@ def _metric_arrays(metrics, J, dtype=np.float64):
 
 def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int, Q0: np.ndarray | None = None,
               xyz=None, typed: bool = False):
-    """nsteps SSP-RK3 steps of time_step's loop (solver.jl:416-444; no local time step, no
-    filter) from the conserved state U0 and its ghost-filled primitive state Q0 (formed from U0
-    as a stage forms it when not given), for boundary.jl's boundary set; xyz: the cell-centre
+    """nsteps SSP-RK3 steps of time_step's loop (solver.jl:410-470) from the conserved state U0
+    and its ghost-filled primitive state Q0 (formed from U0 as a stage forms it when not
+    given), for boundary.jl's boundary set: with P.lts, compute_dt before the first stage of
+    each step and div_LTS in every stage; with P.filter, after every P.filter_interval-th step
+    the filtering pass of solver.jl:446-470 (step counter from 1); xyz: the cell-centre
     coordinates (x, y, z) for the finite-volume schemes; typed: Float32 arrays, dt and linComb
     weights (0.25f0, 0.75f0, 2/3f0, 1/3f0) and a module translated with Julia's types.
     Returns (U, Q)."""
@@ -311,17 +317,25 @@ def rk3_steps(module_path, P, U0: np.ndarray, metrics, J, dt: float, nsteps: int
         k["fillGhost"](Q, U, 0, 0)
     else:
         Q = JArray(Q0.astype(dtype).copy())
-    for _ in range(nsteps):
+    lts = bool(int(P.lts))
+    if lts:
+        k["LTS_CFL"] = f(P.lts_cfl)
+        lts_dt = JArray(np.zeros(U0.shape[1:], dtype))
+    for tt in range(1, nsteps + 1):
         for krk in (1, 2, 3):
             if krk == 1:
                 Un = JArray(U.a.copy())
-            _advance(k, P, Q, m, S, Jj, U, dt, xyz)
+                if lts:
+                    launch(k["compute_dt"], ext, lts_dt, Q, Jj, *S)
+            _advance(k, P, Q, m, S, Jj, U, dt, xyz, lts_dt=lts_dt if lts else None)
             if krk == 2:
                 launch(k["linComb"], ext, U, Un, 5, f(0.25), f(0.75))
             elif krk == 3:
                 launch(k["linComb"], ext, U, Un, 5, f(2) / f(3), f(1) / f(3))
             launch(k["c2Prim"], ext, U, Q)
             k["fillGhost"](Q, U, 0, 0)
+        if int(P.filter) and tt % int(P.filter_interval) == 0:
+            _filter(k, P, U, Q, f)
     return U.a, Q.a
 
 
@@ -381,15 +395,14 @@ def local_dt(module_path, P, Q: np.ndarray, metrics, J) -> np.ndarray:
     return dt.a
 
 
-def filter_pass(module_path, P, U: np.ndarray, Q: np.ndarray) -> np.ndarray:
-    """One filtering pass of time_step (solver.jl:446-470) over U: per direction, Un = U, then
-    the pressure sensor pre_d and the shock-capturing filter_d (P.filter 2) or the linear
-    linearFilter_d (P.filter 1) with filtering_s0 = P.filter_s0, filtering_rth = P.filter_rth."""
-    k = kernels(module_path, P)
+def _filter(k, P, Uj, Qj, f=float):
+    """The filtering pass of time_step (solver.jl:446-470) over Uj in place: per direction,
+    Un = U, then the pressure sensor pre_d and the shock-capturing filter_d (P.filter 2) or the
+    linear linearFilter_d (P.filter 1) with filtering_s0 = P.filter_s0, filtering_rth =
+    P.filter_rth."""
     ext = (int(P.nx) + 2 * NG, int(P.ny) + 2 * NG, int(P.nz) + 2 * NG)
-    Uj, Qj = JArray(U.astype(np.float64).copy()), JArray(Q.astype(np.float64))
-    sc = JArray(np.zeros(Q.shape[1:]))
-    s0, rth = float(P.filter_s0), float(P.filter_rth)
+    sc = JArray(np.zeros(Qj.a.shape[1:], Qj.a.dtype))
+    s0, rth = f(P.filter_s0), f(P.filter_rth)
     for d in "xyz":
         Un = JArray(Uj.a.copy())
         if int(P.filter) == 2:
@@ -397,6 +410,12 @@ def filter_pass(module_path, P, U: np.ndarray, Q: np.ndarray) -> np.ndarray:
             launch(k["filter_" + d], ext, Uj, Un, sc, s0)
         else:
             launch(k["linearFilter_" + d], ext, Uj, Un, s0)
+
+
+def filter_pass(module_path, P, U: np.ndarray, Q: np.ndarray) -> np.ndarray:
+    """One filtering pass of time_step (solver.jl:446-470) over a copy of U (_filter)."""
+    Uj, Qj = JArray(U.astype(np.float64).copy()), JArray(Q.astype(np.float64))
+    _filter(kernels(module_path, P), P, Uj, Qj)
     return Uj.a
 
 
