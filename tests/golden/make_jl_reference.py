@@ -9,7 +9,9 @@ Julia kernels translated mechanically into Python (oracle/ref_jl/jl2py.py) and r
   WALE), whose inputs are stored too;
 and, for the cases with boundary.jl's own boundary set, the reference's prim2c, c2Prim with
 the ghost fill, and two SSP-RK3 steps (the stage loop of solver.jl); for the viscous cases its
-local time step and one pass of each filter; for every case a SHA-256 of the metrics and J of
+local time step and one pass of each filter, and for those with boundary.jl's boundary set
+two steps of the whole time_step loop (solver.jl:410-470) with local time stepping and/or
+either filter (STEP_VARIANTS), as SHA-256 digests of U and Q; for every case a SHA-256 of the metrics and J of
 parse_mesh.jl:139-248 from the coordinates (the arrays themselves are those stored with the
 inputs);
 - four finite-volume cases (FVM.jl, the reference's default scheme: Roe-characteristic and
@@ -70,6 +72,14 @@ VISCOUS = {
         bc=[dict(kind=BC_PERIODIC)] * 6), seed=62, spikes=4),
 }
 RK3_DT, RK3_STEPS = 2e-4, 2
+# the time_step loop's options: compute_dt at the first stage and div_LTS, the filters after
+# every filtering_interval-th step
+STEP_VARIANTS = {
+    "lts": dict(lts=1, lts_cfl=0.3),
+    "filter_linear": dict(filter=1, filter_interval=2, filter_s0=0.5),
+    "filter_shock": dict(filter=2, filter_interval=1, filter_rth=1e-5, filter_s0=1.0),
+    "lts_filter_shock": dict(lts=1, lts_cfl=0.3, filter=2, filter_interval=2, filter_rth=1e-5, filter_s0=1.0),
+}
 FVM = {
     "fvm_eigen_refbc": dict(n=(6, 5, 5), params=dict(scheme=1, viscous=0), seed=51),
     "fvm_eigen_viscous_refbc": dict(n=(6, 5, 5), params=dict(scheme=1, viscous=1, c_s=1e-2, t_s=1.0), seed=52),
@@ -103,6 +113,24 @@ def metrics_digest(m, J) -> str:
     for a in (*m, J):
         h.update(np.ascontiguousarray(a, dtype="<f8").tobytes())
     return h.hexdigest()
+
+
+def f64_digest(*arrays) -> str:
+    """SHA-256 of the arrays as little-endian binary64, in order."""
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+def _step_variants(module, P, Q, m, J, name):
+    """RK3_STEPS steps of the time_step loop per STEP_VARIANTS entry from U = prim2c(Q)."""
+    U0 = runtime.prim2c(module, P, Q)
+    out = {}
+    for label, kw in STEP_VARIANTS.items():
+        U, Qs = runtime.rk3_steps(module, params_copy(P, **kw), U0, m, J, RK3_DT, RK3_STEPS, Q0=Q)
+        out[f"{name}__steps_{label}_sha256"] = np.array(f64_digest(U, Qs))
+    return out
 
 
 def f32_digest(*arrays) -> str:
@@ -164,7 +192,7 @@ def main() -> None:
         "typed_module_sha256": hashlib.sha256(typed.read_bytes()).hexdigest(),
         "corrections": [c[-1] for c in jl2py.CORRECTIONS],
         "semantics": "every value binary64; Julia's literal powers x^2, x^3 as products, other powers by C pow",
-        "rk3": {"dt": RK3_DT, "steps": RK3_STEPS}}))}
+        "rk3": {"dt": RK3_DT, "steps": RK3_STEPS}, "step_variants": STEP_VARIANTS}))}
     report = {}
     for f in sorted(HERE.glob("*.npz")):
         d = np.load(f, allow_pickle=True)
@@ -198,6 +226,7 @@ def main() -> None:
         report[name] = r
         if runtime.is_reference_bcs(P):
             out.update(_state_steps(module, P, Q, m, J, name))
+            out.update(_step_variants(module, P, Q, m, J, name))
         out.update(_ref32(typed, P, Q, m, J, name, (x, y, z)))
         # the local time step (utils.jl:73-99) and the two filters (solver.jl:446-470)
         U = runtime.prim2c(module, P, Q)

@@ -92,6 +92,32 @@ def test_oracle_local_dt_and_filters_equal_the_translated_reference(name):
         assert not np.array_equal(ref, U) and np.array_equal(Uf, ref), label
 
 
+def _f64_digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name", [n for n in _cases()[1] if f"{n}__steps_lts_sha256" in _cases()[0].files])
+def test_oracle_time_step_loop_equals_the_translated_reference(name):
+    """Two steps of the whole time_step loop (solver.jl:410-470) with local time stepping
+    (compute_dt at the first stage of each step, div_LTS in every stage) and with either filter
+    after every filtering_interval-th step, alone and together: U and Q bit for bit."""
+    from flame3d_mhd_gb300.cases import params_copy
+    d, _ = _cases()
+    meta, Q, m, J = _inputs(d, name)
+    P = make_params(*meta["n"], **meta["params"])
+    prov = json.loads(str(d["provenance"]))
+    rk = prov["rk3"]
+    U0 = orc.prim2c(P, Q)
+    for label, kw in prov["step_variants"].items():
+        U, Un, Qs = U0.copy(), np.zeros_like(U0), np.array(Q, dtype=np.float64)
+        orc.rk3(params_copy(P, **kw), rk["steps"], rk["dt"], U, Un, Qs, list(m), J)
+        assert _f64_digest(U, Qs) == str(d[f"{name}__steps_{label}_sha256"]), label
+
+
 def _digest(m, J):
     import hashlib
     h = hashlib.sha256()
