@@ -123,12 +123,13 @@ def f64_digest(*arrays) -> str:
     return h.hexdigest()
 
 
-def _step_variants(module, P, Q, m, J, name):
-    """RK3_STEPS steps of the time_step loop per STEP_VARIANTS entry from U = prim2c(Q)."""
+def _step_variants(module, P, Q, m, J, name, xyz=None):
+    """RK3_STEPS steps of the time_step loop per STEP_VARIANTS entry from U = prim2c(Q) (xyz:
+    the cell-centre coordinates of a finite-volume case)."""
     U0 = runtime.prim2c(module, P, Q)
     out = {}
     for label, kw in STEP_VARIANTS.items():
-        U, Qs = runtime.rk3_steps(module, params_copy(P, **kw), U0, m, J, RK3_DT, RK3_STEPS, Q0=Q)
+        U, Qs = runtime.rk3_steps(module, params_copy(P, **kw), U0, m, J, RK3_DT, RK3_STEPS, Q0=Q, xyz=xyz)
         out[f"{name}__steps_{label}_sha256"] = np.array(f64_digest(U, Qs))
     return out
 
@@ -255,6 +256,7 @@ def main() -> None:
             Us, Qs = runtime.rk3_steps(corrected, P, runtime.prim2c(module, P, Q), m, J, RK3_DT, RK3_STEPS,
                                        Q0=Q, xyz=xyz)
             out[f"{name}__U_rk3_fvm"], out[f"{name}__Q_rk3_fvm"] = Us, Qs
+            out.update(_step_variants(corrected, P, Q, m, J, name, xyz))
     np.savez_compressed(HERE / "jl_reference_rhs.npz", **out)
     for name, r in report.items():
         print(name, "max |rhs|", float(np.abs(r[I]).max()))

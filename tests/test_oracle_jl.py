@@ -310,6 +310,26 @@ def test_oracle_fvm_faces_rhs_and_steps_equal_the_corrected_translation(name):
         orc.set_coordinates(None)
 
 
+@pytest.mark.parametrize("name", [n for n in _fvm_cases() if f"{n}__steps_lts_sha256" in np.load(FIX).files])
+def test_oracle_fvm_time_step_loop_equals_the_corrected_translation(name):
+    """Two steps of the time_step loop on the finite-volume scheme with local time stepping
+    and/or either filter: U and Q bit for bit."""
+    from flame3d_mhd_gb300.cases import params_copy
+    d = np.load(FIX, allow_pickle=True)
+    P, Q, m, J, (x, y, z) = _fvm_inputs(d, name)
+    prov = json.loads(str(d["provenance"]))
+    rk = prov["rk3"]
+    U0 = orc.prim2c(P, Q)
+    orc.set_coordinates(x, y, z)
+    try:
+        for label, kw in prov["step_variants"].items():
+            U, Un, Qs = U0.copy(), np.zeros_like(U0), np.array(Q, dtype=np.float64)
+            orc.rk3(params_copy(P, **kw), rk["steps"], rk["dt"], U, Un, Qs, list(m), J)
+            assert _f64_digest(U, Qs) == str(d[f"{name}__steps_{label}_sha256"]), label
+    finally:
+        orc.set_coordinates(None)
+
+
 def test_fvm_cases_cover_the_branches_and_forms():
     d = np.load(FIX, allow_pickle=True)
     forms, seen = set(), {1: set(), 2: set()}
