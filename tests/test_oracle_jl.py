@@ -387,3 +387,14 @@ def test_rule_typed_literals_and_locals():
     exec(py, ns)
     s_, t_ = ns["g"](JArray(np.array([1.0, 2.0], dtype=np.float32)), 2)
     assert type(s_) is np.float32 and type(t_) is np.float64  # t is Float64 after t += Float64, as in Julia
+
+
+def test_rule_corrections_are_exact():
+    """A correction applies only with its stated number of matches: a changed reference
+    source fails loudly rather than being patched in part."""
+    src = "function Eigen_reconstruct_i()\n    v2 = -1.0f0*V3L + 1\n    x = α2L*v2 + 1\nend\n" \
+          "function Conser_reconstruct_i()\nend\nfunction Conser_reconstruct_j()\n" \
+          "    Fy[1] = UR_final_1#flux_temp[1] * Area\nend\n"
+    with pytest.raises(ValueError, match="matched 1 times, expected 6"):
+        jl2py.apply_corrections("FVM.jl", src)
+    assert jl2py.apply_corrections("split.jl", src) == src  # other files untouched
