@@ -292,8 +292,9 @@ def expr(s: str, typed: bool = False) -> str:
     s = re.sub(r"MMatrix\{\s*([^,}]+)\s*,\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1, \2)", s)
     s = re.sub(r"MVector\{\s*([^,}]+)\s*,[^}]*\}\s*\(\s*undef\s*\)", r"_mat(\1)", s)
     s = re.sub(r"SVector\{[^}]*\}\s*\(", "_vec(", s)
-    if typed:  # Int / Int is a Float64 quotient (1/60 -> _f64(1/60))
-        s = re.sub(r"(?<![\w.])(\d+)\s*/\s*(\d+)(?![\w.])", r"_f64(\1/\2)", s)
+    if typed:  # Int / Int is a Float64 quotient (1/60 -> _f64(1/60)); a quotient that continues a
+        # product (a*3/4 is (a*3)/4) or is raised to a power (1/2^k) is left as it is
+        s = re.sub(r"(?<![\w.*/^])(?<![*/^] )(\d+)\s*/\s*(\d+)(?![\w.^])(?! *\^)", r"_f64(\1/\2)", s)
     if typed:  # Float32 literals (12f0) -> _f32(12e0), Float64 ones (1e-20, 0.5) -> _f64(...)
         s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][-+]?\d+)?|\.\d+(?:[eE][-+]?\d+)?|\d+(?:[eE][-+]?\d+)?)"
                    r"(?:f(-?\d+))?(?![\w.])", _typed_literal, s)

@@ -371,6 +371,10 @@ def test_rule_typed_literals_and_locals():
     assignment (x op= e included), typed temporaries."""
     assert jl2py.expr("1/12f0 + WENOϵ1*1e-20 - 2x + 0.5", typed=True) == "1/_f32(12e0) + WENOϵ1*_f64(1e-20) - 2*x + _f64(0.5)"
     assert jl2py.expr("MMatrix{5, 5, Float32, 25}(undef)", typed=True) == "_mat(5, 5, 32)"
+    # Int / Int is Float64, unless the quotient continues a product or is raised to a power
+    assert jl2py.expr("1/60*(f[7]-f[1])", typed=True) == "_f64(1/60)*(f[7]-f[1])"
+    assert jl2py.expr("a*3/4", typed=True) == "a*3/4"
+    assert jl2py.expr("1/2^k", typed=True) == "1/2**k"
     py = jl2py.translate("""
     function g(A, n)
         s::Float32 = 0.f0
