@@ -3,7 +3,8 @@
 The reference's hot path is Julia (CUDA.jl kernels) and no Julia is available, so the oracle
 (oracle/f3d_oracle.hpp) is a restatement written by hand. To check that restatement against
 the reference's own source, this script translates the kernel files (split.jl, schemes.jl,
-viscous.jl, div.jl, utils.jl, boundary.jl, FVM.jl) statement by statement, with fixed rules
+viscous.jl, div.jl, utils.jl, boundary.jl, FVM.jl) and the metric computations of two
+scripts (parse_mesh.jl, SCU-benchmark/readfort.jl) statement by statement, with fixed rules
 and no hand edits:
 
 - comments dropped; a line ending in an operator, a comma or an open bracket continues;
@@ -11,7 +12,8 @@ and no hand edits:
 - `function f(args)` .. `end`, `if` / `elseif` / `else`, `for v = a:b` become Python blocks
   (`begin` .. `end` adds none); a bare expression ending a function body is returned, as
   Julia returns it;
-- `@inbounds`, `@fastmath`, `@inline` and type annotations (`x::Float32 = ...`) are dropped;
+- `@inbounds`, `@fastmath`, `@inline`, `@view` and type annotations (`x::Float32 = ...`) are
+  dropped (a view reads what its slice reads);
 - literals: `12f0` -> `12e0`, `1i32` -> `1`, implicit products `547V1` -> `547*V1`;
 - `x^2` / `x^3` -> `_p2(x)` / `_p3(x)` (products, as Julia's literal powers), other `^` -> `**`,
   `&&` / `||` / `!` -> `and` / `or` / `not`, `c ? a : b` -> `(a if c else b)`,
@@ -20,9 +22,10 @@ and no hand edits:
   grid), `CUDA.eps(Float32)` -> 2^-23, `÷` -> `//`, a character Julia allows in names and
   Python does not (the ∂ of ∂ξ∂x) -> `_u2202_`;
 - array indexing is left as written: the runtime (runtime.py) passes arrays that take
-  Julia's 1-based, column-major subscripts.
+  Julia's 1-based, column-major subscripts; in the scripts, `a:b` and `:` subscripts become
+  slices, loops over several variables nest, `@.` broadcasts run elementwise.
 
-In this FP64 reading every value is a Python float (binary64); the reference's Float32
+In this FP64 reading every value is a binary64 scalar; the reference's Float32
 annotations and f0 literals select the element type only, so the result is the reference's
 algorithm evaluated in FP64 in the reference's own operation order, the form the FP64 oracle
 restates. The generated module is written next to the compiled reference program
@@ -30,8 +33,9 @@ restates. The generated module is written next to the compiled reference program
 
 `translate_tree(root, typed=True)` keeps Julia's element types instead, for an evaluation of
 the reference's own precision in NumPy scalars: `12f0` -> `_f32(12e0)` (Float32), `1e-20` /
-`0.5` -> `_f64(...)` (Float64), integer literals left as they are (Python ints take the
-other operand's type, as Julia's Int does), a local declared `x::Float32` / `x::Float64`
+`0.5` -> `_f64(...)` (Float64), an Int / Int quotient -> `_f64(a/b)`, other integer literals
+left as they are (Python ints take the other operand's type, as Julia's Int does), `zeros(
+Float32, ...)` -> Float32 arrays, a local declared `x::Float32` / `x::Float64`
 converted at every assignment to it (`x op= e` included), `MMatrix` / `MVector` temporaries of
 their element type. The runtime then supplies Float32 arrays and run.jl's Float32 constants.
 
