@@ -449,3 +449,60 @@ def test_random_configurations_against_the_translation(tmp_path, seed):
         Uo, Un, Qo = U.copy(), np.zeros_like(U), Q.copy()
         orc.rk3(P, 1, 1e-4, Uo, Un, Qo, list(m), J)
         assert np.array_equal(Us, Uo, equal_nan=True) and np.array_equal(Qs, Qo, equal_nan=True)
+
+
+@pytest.mark.skipif(REF is None or not (REF / "FVM.jl").exists(),
+                    reason="F3D_REFERENCE does not name the reference tree")
+@pytest.mark.parametrize("seed", range(4))
+def test_random_fvm_configurations_against_the_corrected_translation(tmp_path, seed):
+    """Random finite-volume configurations (reconstruction, viscosity, boundary set, noise
+    growing along x, pressure spikes): the face fluxes and the RHS equal the corrected
+    translation's bit for bit, and with the reference's boundary set so does one SSP-RK3 step,
+    plain, with local time stepping and with the shock-capturing filter."""
+    import importlib.util
+    from flame3d_mhd_gb300.abi import BC_PERIODIC
+    from flame3d_mhd_gb300.cases import params_copy
+    from oracle.ref_jl import runtime
+    mod = tmp_path / "jl_corrected.py"
+    mod.write_text(jl2py.translate_tree(REF, corrected=True))
+    spec = importlib.util.spec_from_file_location("make_golden", ROOT / "tests" / "golden" / "make_golden.py")
+    g = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(g)
+    rng = np.random.default_rng(2000 + seed)
+    n = tuple(int(v) for v in rng.integers(5, 8, 3))
+    kw = dict(scheme=1 + seed % 2, viscous=(seed // 2) % 2, phi1=0.02, phi2=0.1, phi3=0.4, rg=1.0, c_s=1e-2, t_s=1.0)
+    if seed == 3:
+        kw["bc"] = [dict(kind=BC_PERIODIC)] * 6
+    P = make_params(*n, **kw)
+    x, y, z = g.coords(n)
+    s = (n[2] + 2 * NG, n[1] + 2 * NG, n[0] + 2 * NG)
+    amp = np.geomspace(1e-3, 0.1, s[2])[None, None, :]
+    Q = np.zeros((6, *s))
+    Q[0] = 1.0 + amp * rng.uniform(-1, 1, s)
+    Q[1:4] = rng.uniform(-0.3, 0.3, (3, 1, 1, 1)) + amp * rng.uniform(-1, 1, (3, *s))
+    Q[4] = (1.0 + amp * rng.uniform(-1, 1, s)) / 1.4
+    for _ in range(2):
+        a, b, c = [int(rng.integers(NG, k - NG)) for k in s]
+        Q[4, a, b, c] *= float(rng.uniform(1.5, 6))
+    Q[5] = Q[4] / (Q[0] * P.rg)
+    U = orc.prim2c(P, Q)
+    orc.fill_ghosts(P, Q, U)
+    m, J = orc.metrics(P, x, y, z)
+    m = np.stack(m)
+    phi, Uq = orc.sensor(P, Q), orc.prim2c(P, Q)
+    for d, F in enumerate(runtime.fvm_faces(mod, P, Q, m, (x, y, z))):
+        S = orc.metric_norm(P, m[3 * d], m[3 * d + 1], m[3 * d + 2])
+        assert np.array_equal(F, orc.fvm_face_flux(P, d, int(P.scheme) == 1, phi, S, Q, Uq, x, y, z), equal_nan=True)
+    r = runtime.rhs(mod, P, Q, m, J, (x, y, z))
+    orc.set_coordinates(x, y, z)
+    try:
+        assert np.array_equal(r[I], orc.rhs(P, Q, list(m), J)[I], equal_nan=True)
+        if runtime.is_reference_bcs(P):
+            for v in ({}, dict(lts=1, lts_cfl=0.3), dict(filter=2, filter_interval=1, filter_rth=1e-5)):
+                Pv = params_copy(P, **v)
+                Us, Qs = runtime.rk3_steps(mod, Pv, U, m, J, 1e-4, 1, Q0=Q, xyz=(x, y, z))
+                Uo, Un, Qo = U.copy(), np.zeros_like(U), Q.copy()
+                orc.rk3(Pv, 1, 1e-4, Uo, Un, Qo, list(m), J)
+                assert np.array_equal(Us, Uo, equal_nan=True) and np.array_equal(Qs, Qo, equal_nan=True), v
+    finally:
+        orc.set_coordinates(None)
