@@ -97,7 +97,9 @@ typedef struct f3d_bc {
 } f3d_bc;
 
 typedef struct f3d_params {
-    int32_t nx, ny, nz;  /* interior cells per direction (Nxp, Nyp, Nzp; run.jl:84-86)   */
+    int32_t nx, ny, nz;  /* interior cells per direction (Nxp, Nyp, Nzp; run.jl:84-86),    */
+                         /* each >= 4 = NG (a periodic fill copies NG interior layers;   */
+                         /* smaller grids: F3D_ERR_ARG); a quasi-2D case uses 4 layers  */
     int32_t ng;          /* ghost layers; must be 4 (parse_mesh.jl:6)                    */
     double gamma;        /* run.jl:8                                                     */
     double rg;           /* run.jl:9                                                     */
