@@ -349,6 +349,30 @@ def _strip_annot(lhs: str) -> str:
 
 _expr = expr  # for translate_script, whose local name expr selects the typed form
 
+
+def _top_colon(s: str) -> int:
+    """Index of the first ':' outside brackets, or -1."""
+    d = 0
+    for i, ch in enumerate(s):
+        if ch in _OPEN:
+            d += 1
+        elif ch in _CLOSE:
+            d -= 1
+        elif ch == ":" and d == 0:
+            return i
+    return -1
+
+
+def _loops(spec: str, ex) -> list[tuple[str, str]]:
+    """`k in K_in, j = 1:n, i ∈ a:b` -> [(var, Python iterable), ...], the first outermost:
+    a:b is range(a, b + 1), anything else (a range variable) is iterated as it is."""
+    out = []
+    for part in (t.strip() for t in re.split(r",(?![^()\[\]]*[)\]])", spec)):
+        v, rng = re.split(r"\s*(?:∈|=|\bin\b)\s*", part, maxsplit=1)
+        c = _top_colon(rng)
+        out.append((v, f"range({ex(rng[:c].strip())}, ({ex(rng[c + 1:].strip())}) + 1)" if c >= 0 else ex(rng)))
+    return out
+
 _ANNOT = re.compile(r"^\s*([^\W\d]\w*)\s*::\s*Float(32|64)\s*$")
 
 
@@ -360,7 +384,9 @@ def translate(src: str, typed: bool = False) -> str:
     out: list[str] = []
     stack: list[str] = []
     types: dict[str, str] = {}  # the declared Float32 / Float64 locals of the current function
-    pad = lambda: "    " * sum(k != "begin" for k in stack)  # begin .. end adds no indentation
+    # indentation levels opened by each block: begin .. end none, a loop over n variables n
+    levels = lambda k: 0 if k == "begin" else (int(k[4:]) if k.startswith("for:") else 1)
+    pad = lambda: "    " * sum(levels(k) for k in stack)
     last_expr = None  # index in out of the function body's last statement if it is a bare expression
     for raw in logical_lines(src):
         s = _strip_macros(raw)
@@ -399,10 +425,13 @@ def translate(src: str, typed: bool = False) -> str:
         if s == "else":
             out.append(pad()[4:] + "else:")
             continue
-        m = re.match(r"for\s+(\w+)\s*(?:=|in)\s*(.+?)\s*:\s*(.+)$", s)
+        m = re.match(r"for\s+(.*)$", s)
         if m:
-            out.append(pad() + f"for {m.group(1)} in range({expr_(m.group(2))}, ({expr_(m.group(3))}) + 1):")
-            stack.append("for")
+            base = pad()
+            loops = _loops(m.group(1), expr_)
+            for k, (v, it) in enumerate(loops):
+                out.append(base + "    " * k + f"for {v} in {it}:")
+            stack.append(f"for:{len(loops)}")
             continue
         if s == "return" or s.startswith("return "):
             rest = s[len("return"):].strip()
@@ -426,10 +455,13 @@ def translate(src: str, typed: bool = False) -> str:
             lhs = expr_(_strip_annot(m.group(1)))
             if typed and a:
                 types[lhs] = a.group(2)
-            if typed and lhs in types:
-                out.append(pad() + f"{lhs} = _f{types[lhs]}({expr_(m.group(2))})")
+            rhs, c = m.group(2), _top_colon(m.group(2))
+            if c >= 0 and "?" not in rhs:  # a range a:b
+                out.append(pad() + f"{lhs} = range({expr_(rhs[:c].strip())}, ({expr_(rhs[c + 1:].strip())}) + 1)")
+            elif typed and lhs in types:
+                out.append(pad() + f"{lhs} = _f{types[lhs]}({expr_(rhs)})")
             else:
-                out.append(pad() + f"{lhs} = {expr_(m.group(2))}")
+                out.append(pad() + f"{lhs} = {expr_(rhs)}")
             continue
         out.append(pad() + expr_(s))
         if len(stack) == 1:
@@ -499,6 +531,10 @@ def translate_script(src: str, first: int, last: int, typed: bool = False) -> st
         if m:
             out.append(pad + f"_bset({expr(m.group(1))}, {expr(m.group(2))})")
             continue
+        m = re.match(r"(\w+)\s*\.([-+*/])=\s*(.+)$", s)  # x ./= e: elementwise x = x / e
+        if m:
+            out.append(pad + f"_bset({m.group(1)}, {m.group(1)} {m.group(2)} ({expr(m.group(3))}))")
+            continue
         m = re.match(r"([^=<>!]+?)\s*=(?!=)\s*(.+)$", s)
         if m:
             out.append(pad + f"{expr(_strip_annot(m.group(1)))} = {expr(m.group(2))}")
@@ -518,6 +554,17 @@ METRIC_LINES = (139, 248)
 # functions and the body of computeMetrics before its file output
 READFORT = "SCU-benchmark/readfort.jl"
 READFORT_LINES = ((104, 117), (120, 208))
+# the ghost coordinates: readfort.jl's generateXYZ after reading the file (point reflection,
+# edge completion, then ./= 1000) and solver.jl's extrapolation of the coordinates it reads
+READFORT_GHOST_LINES = (34, 99)
+EXTRAPOLATION = ("solver.jl", "function extrapolation(")
+
+
+def _function_text(src: str, head: str) -> str:
+    """The top-level function starting with `head`, through its closing `end` line."""
+    i = src.index(head)
+    j = src.index("\nend", i)
+    return src[i:j + 4] + "\n"
 
 
 def translate_tree(root: Path, corrected: bool = False, typed: bool = False) -> str:
@@ -541,6 +588,14 @@ def translate_tree(root: Path, corrected: bool = False, typed: bool = False) -> 
     body = "".join(translate_script(rf, a, b, typed) for a, b in READFORT_LINES)
     parts.append("def _metrics_readfort(x, y, z):\n" + "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) +
                  "    return (dξdx, dξdy, dξdz, dηdx, dηdy, dηdz, dζdx, dζdy, dζdz), J\n")
+    a, b = READFORT_GHOST_LINES
+    parts.append(f"# ---- {READFORT}:{a}-{b}, as the body of _ghosts_readfort()\n")
+    body = translate_script(rf, a, b, typed)
+    parts.append("def _ghosts_readfort(x, y, z):\n" + "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) +
+                 "    return x, y, z\n")
+    f, head = EXTRAPOLATION
+    parts.append(f"# ---- {f}: {head.rstrip('(')}\n")
+    parts.append(translate(_function_text((root / f).read_text(), head), typed))
     return "\n".join(parts)
 
 

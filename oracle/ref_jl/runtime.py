@@ -16,7 +16,8 @@ and run.jl gave them:
 - prim2c, c2Prim and the ghost fill of one process for boundary.jl's own boundary set, the
   RK3 stage loop of time_step, its local time step and its filtering pass;
 - the metrics and J of parse_mesh.jl and of SCU-benchmark/readfort.jl (scripts, each
-  translated as the body of one function).
+  translated as the body of one function), and the ghost coordinates of readfort.jl's
+  generateXYZ and of solver.jl's extrapolation.
 
 Every value is a binary64 NumPy scalar (IEEE: 0/0 is NaN, as in Julia): the reference's
 algorithm in FP64, in its own operation order. With typed=True (a module translated with
@@ -351,6 +352,23 @@ def metrics(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray, typed: 
     fn = k["_metrics" if source == "parse_mesh" else "_metrics_readfort"]
     m, J = fn(*(JArray(np.asarray(c, dtype=dtype)) for c in (x, y, z)))
     return np.stack([a.a for a in m]), J.a
+
+
+def ghost_coordinates(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarray, rule: str = "readfort",
+                      typed: bool = False):
+    """Ghost cell-centre coordinates from coordinates with the interior filled ((Nz_tot,
+    Ny_tot, Nx_tot) each): rule "readfort" runs SCU-benchmark/readfort.jl:34-99 (the
+    reflections and edge completions of generateXYZ, then ./= 1000), rule "solver" runs
+    solver.jl's extrapolation on one rank. typed: Float32 arrays (the reference's) and a
+    module translated with Julia's types."""
+    k = kernels(module_path, P, typed)
+    dtype = np.float32 if typed else np.float64
+    X, Y, Z = (JArray(np.array(a, dtype=dtype, copy=True)) for a in (x, y, z))
+    if rule == "readfort":
+        k["_ghosts_readfort"](X, Y, Z)
+    else:
+        k["extrapolation"](X, Y, Z, 0, 0, 0)
+    return X.a, Y.a, Z.a
 
 
 def fvm_faces(module_path, P, Q: np.ndarray, metrics: np.ndarray, xyz):

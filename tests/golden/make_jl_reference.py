@@ -27,7 +27,10 @@ inputs);
   the RHS and, for boundary.jl's boundary set, of prim2c, c2Prim with the ghost fill and two
   SSP-RK3 steps (Float32 dt and weights), and of the metrics of parse_mesh.jl:139-248 (Float32
   arrays, Float64 coefficients) and of SCU-benchmark/readfort.jl:104-208 (Float32 coefficients)
-  on the coordinates rounded to Float32, all little-endian binary32.
+  on the coordinates rounded to Float32, all little-endian binary32;
+- the ghost coordinates of readfort.jl's generateXYZ (:34-99, with ./= 1000) and of solver.jl's
+  extrapolation, in binary64 and in Float32, on one grid whose interior is stored
+  (ghosts__x/y/z), as SHA-256 digests.
 The file also records SHA-256 digests of the translated Julia files and of the generated
 modules. Needs the reference tree (read only):
 
@@ -157,6 +160,33 @@ def _ref32(typed, P, Q, m, J, name, xyz):
     return out
 
 
+def ghost_inputs():
+    """Interior coordinates in millimetres (zero ghosts) of a curved 7 x 6 x 5 grid."""
+    n = (7, 6, 5)
+    s = (n[2] + 2 * NG, n[1] + 2 * NG, n[0] + 2 * NG)
+    rng = np.random.default_rng(5)
+    kk, jj, ii = np.meshgrid(*[np.arange(v, dtype=float) for v in s], indexing="ij")
+    f = [ii + 0.1 * np.sin(jj), 1.3 * jj + 0.2 * np.cos(ii), 0.7 * kk + 0.05 * ii * jj / 40]
+    I3 = (slice(NG, -NG),) * 3
+    out = []
+    for a in f:
+        c = np.zeros(s)
+        c[I3] = ((a + rng.uniform(-0.01, 0.01, s)) * 1000.0)[I3]
+        out.append(c)
+    return n, out
+
+
+def _ghosts(module, typed):
+    n, xyz = ghost_inputs()
+    P = make_params(*n)
+    out = {"ghosts__x": xyz[0], "ghosts__y": xyz[1], "ghosts__z": xyz[2]}
+    for rule in ("readfort", "solver"):
+        for label, mod, t in (("64", module, False), ("32", typed, True)):
+            g = runtime.ghost_coordinates(mod, P, *xyz, rule=rule, typed=t)
+            out[f"ghosts__{rule}{label}_sha256"] = np.array((f32_digest if t else f64_digest)(*g))
+    return out
+
+
 def _golden():
     spec = importlib.util.spec_from_file_location("make_golden", HERE / "make_golden.py")
     mod = importlib.util.module_from_spec(spec)
@@ -257,6 +287,7 @@ def main() -> None:
                                        Q0=Q, xyz=xyz)
             out[f"{name}__U_rk3_fvm"], out[f"{name}__Q_rk3_fvm"] = Us, Qs
             out.update(_step_variants(corrected, P, Q, m, J, name, xyz))
+    out.update(_ghosts(module, typed))
     np.savez_compressed(HERE / "jl_reference_rhs.npz", **out)
     for name, r in report.items():
         print(name, "max |rhs|", float(np.abs(r[I]).max()))

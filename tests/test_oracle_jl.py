@@ -216,6 +216,27 @@ def test_float32_set_up_metrics_equal_the_typed_translation(name):
     assert _f32_digest(*m, J) == str(d[f"{name}__metrics32_readfort_sha256"])
 
 
+@pytest.mark.parametrize("rule", ["readfort", "solver"])
+def test_ghost_coordinates_equal_the_translated_reference(tmp_path, rule):
+    """grid.extend_ghosts (and, for readfort.jl, grid.mesh_from_ocfd reading a mesh file)
+    against readfort.jl's generateXYZ (:34-99: reflections, edge completions, ./= 1000) and
+    solver.jl's extrapolation, in binary64 and in Float32: bit for bit."""
+    from flame3d_mhd_gb300 import grid
+    d = np.load(FIX, allow_pickle=True)
+    xyz = [d["ghosts__x"], d["ghosts__y"], d["ghosts__z"]]
+    for dt, label, dig in ((np.float64, "64", _f64_digest), (np.float32, "32", _f32_digest)):
+        g = grid.extend_ghosts(*[a.astype(dt) for a in xyz], dtype=dt, rule=rule)
+        if rule == "readfort":
+            g = tuple(a / dt(1000) for a in g)
+        assert dig(*g) == str(d[f"ghosts__{rule}{label}_sha256"]), label
+    if rule == "readfort":  # the mesh file's Float64 planes read into Float32 arrays
+        nz, ny, nx = (v - 2 * NG for v in xyz[0].shape)
+        path = str(tmp_path / "OCFD3d-Mesh.dat")
+        grid.write_ocfd_mesh(path, *[a[NG:-NG, NG:-NG, NG:-NG] for a in xyz])
+        g = grid.mesh_from_ocfd(path, nx, ny, nz)
+        assert _f32_digest(*g) == str(d["ghosts__readfort32_sha256"])
+
+
 # ---- the translation rules on small pieces of Julia
 def _py(src):
     return jl2py.translate(src).strip()
@@ -391,6 +412,24 @@ def test_rule_typed_literals_and_locals():
     exec(py, ns)
     s_, t_ = ns["g"](JArray(np.array([1.0, 2.0], dtype=np.float32)), 2)
     assert type(s_) is np.float32 and type(t_) is np.float64  # t is Float64 after t += Float64, as in Julia
+
+
+def test_rule_loops_and_ranges():
+    """Loops over several variables and over named ranges, range assignments."""
+    py = jl2py.translate("""
+    function f(A)
+        I_in = 2 : 3
+        for k in I_in, j = 1:2
+            A[j, k] = j + 10k
+        end
+    end
+    """)
+    assert "I_in = range(2, (3) + 1)" in py and "for k in I_in:" in py and "for j in range(1, (2) + 1):" in py
+    ns = {}
+    exec(py, ns)
+    A = JArray(np.zeros((3, 2)))
+    ns["f"](A)
+    assert A.a.tolist() == [[0, 0], [21, 22], [31, 32]]
 
 
 def test_rule_corrections_are_exact():
