@@ -557,6 +557,9 @@ READFORT_LINES = ((104, 117), (120, 208))
 # the ghost coordinates: readfort.jl's generateXYZ after reading the file (point reflection,
 # edge completion, then ./= 1000) and solver.jl's extrapolation of the coordinates it reads
 READFORT_GHOST_LINES = (34, 99)
+# parse_mesh.jl's flat-plate coordinates: stretching_y, the mapping of every cell, then the
+# ghost reflections (its constants Lx, Ly, Lz, stretch_factor_y become parameters)
+FLAT_PLATE_LINES = ((38, 41), (46, 136))
 EXTRAPOLATION = ("solver.jl", "function extrapolation(")
 
 
@@ -593,6 +596,12 @@ def translate_tree(root: Path, corrected: bool = False, typed: bool = False) -> 
     body = translate_script(rf, a, b, typed)
     parts.append("def _ghosts_readfort(x, y, z):\n" + "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) +
                  "    return x, y, z\n")
+    pm = (root / "parse_mesh.jl").read_text()
+    parts.append("# ---- parse_mesh.jl:" + ", ".join(f"{a}-{b}" for a, b in FLAT_PLATE_LINES) +
+                 ", as the body of _flat_plate()\n")
+    body = "".join(translate_script(pm, a, b, typed) for a, b in FLAT_PLATE_LINES)
+    parts.append("def _flat_plate(x, y, z, Lx, Ly, Lz, stretch_factor_y):\n" +
+                 "".join("    " + l + "\n" if l else "\n" for l in body.splitlines()) + "    return x, y, z\n")
     f, head = EXTRAPOLATION
     parts.append(f"# ---- {f}: {head.rstrip('(')}\n")
     parts.append(translate(_function_text((root / f).read_text(), head), typed))

@@ -148,8 +148,15 @@ def _tmat(r, c=None, bits=64):
     return JArray(np.zeros(r if c is None else (c, r), dtype=np.float32 if bits == 32 else np.float64))
 
 
+def _sinh(x):
+    """sinh in binary64, rounded to the argument's type (for Float32: Julia's own Float32 sinh
+    may differ from this in the last bit)."""
+    r = np.float64(math.sinh(float(x)))
+    return r.astype(x.dtype) if isinstance(x, np.floating) else r
+
+
 HELPERS = dict(
-    blockIdx=lambda: _one, blockDim=lambda: _one, threadIdx=lambda: _thread,
+    blockIdx=lambda: _one, blockDim=lambda: _one, threadIdx=lambda: _thread, sinh=_sinh,
     max=_jmax, min=_jmin, sqrt=_sqrt, abs=abs,
     ifelse=lambda c, a, b: a if c else b, zero=lambda a: 0.0,
     _eps32=lambda: 2.0 ** -23, _mat=_mat, _f32=float, _f64=float,
@@ -368,6 +375,18 @@ def ghost_coordinates(module_path, P, x: np.ndarray, y: np.ndarray, z: np.ndarra
         k["_ghosts_readfort"](X, Y, Z)
     else:
         k["extrapolation"](X, Y, Z, 0, 0, 0)
+    return X.a, Y.a, Z.a
+
+
+def flat_plate(module_path, P, lx=2.0, ly=0.1, lz=0.1, factor=3.5, typed: bool = False):
+    """parse_mesh.jl's flat-plate coordinates (:38-136) for the grid of P: every cell mapped
+    (x = Lx xi, y = stretching_y(eta), z = Lz zeta), then the ghost layers reflected; its
+    Float32 constants Lx, Ly, Lz, stretch_factor_y from the arguments."""
+    k = kernels(module_path, P, typed)
+    f, dtype = (np.float32, np.float32) if typed else (float, np.float64)
+    shape = (int(P.nz) + 2 * NG, int(P.ny) + 2 * NG, int(P.nx) + 2 * NG)
+    X, Y, Z = (JArray(np.zeros(shape, dtype)) for _ in range(3))
+    k["_flat_plate"](X, Y, Z, f(lx), f(ly), f(lz), f(factor))
     return X.a, Y.a, Z.a
 
 

@@ -30,7 +30,8 @@ inputs);
   on the coordinates rounded to Float32, all little-endian binary32;
 - the ghost coordinates of readfort.jl's generateXYZ (:34-99, with ./= 1000) and of solver.jl's
   extrapolation, in binary64 and in Float32, on one grid whose interior is stored
-  (ghosts__x/y/z), as SHA-256 digests.
+  (ghosts__x/y/z), as SHA-256 digests; and parse_mesh.jl's flat-plate coordinates (:38-136) in
+  Float32 on a 9 x 7 x 5 grid (its sinh taken in binary64 and rounded to Float32).
 The file also records SHA-256 digests of the translated Julia files and of the generated
 modules. Needs the reference tree (read only):
 
@@ -288,6 +289,7 @@ def main() -> None:
             out[f"{name}__U_rk3_fvm"], out[f"{name}__Q_rk3_fvm"] = Us, Qs
             out.update(_step_variants(corrected, P, Q, m, J, name, xyz))
     out.update(_ghosts(module, typed))
+    out["flat_plate_9x7x5_sha256"] = np.array(f32_digest(*runtime.flat_plate(typed, make_params(9, 7, 5), typed=True)))
     np.savez_compressed(HERE / "jl_reference_rhs.npz", **out)
     for name, r in report.items():
         print(name, "max |rhs|", float(np.abs(r[I]).max()))

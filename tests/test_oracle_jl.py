@@ -237,6 +237,15 @@ def test_ghost_coordinates_equal_the_translated_reference(tmp_path, rule):
         assert _f32_digest(*g) == str(d["ghosts__readfort32_sha256"])
 
 
+def test_flat_plate_grid_equals_the_translated_reference():
+    """meshgen.flat_plate_grid against parse_mesh.jl:38-136 evaluated with its types (Float32
+    mapping of every cell, then the ghost reflections): bit for bit, with sinh taken in binary64
+    and rounded to Float32 on both sides (Julia's own Float32 sinh may differ in the last bit)."""
+    from flame3d_mhd_gb300 import meshgen
+    d = np.load(FIX, allow_pickle=True)
+    assert _f32_digest(*meshgen.flat_plate_grid(9, 7, 5)) == str(d["flat_plate_9x7x5_sha256"])
+
+
 # ---- the translation rules on small pieces of Julia
 def _py(src):
     return jl2py.translate(src).strip()
