@@ -196,6 +196,11 @@ def test_oracle_float32_form_equals_the_typed_translation(name):
         Us, Un, Qs = U0.copy(), np.zeros_like(U0), Q32.copy()
         orc.rk3_32(P, rk["steps"], np.float32(rk["dt"]), Us, Un, Qs, m32, J32)
         assert _f32_digest(U0, Qf, Uf, Us, Qs) == str(d[f"{name}__state32_sha256"])
+        from flame3d_mhd_gb300.cases import params_copy
+        for label, kw in json.loads(str(d["provenance"]))["step_variants"].items():  # LTS, filters
+            Us, Un, Qs = U0.copy(), np.zeros_like(U0), Q32.copy()
+            orc.rk3_32(params_copy(P, **kw), rk["steps"], np.float32(rk["dt"]), Us, Un, Qs, m32, J32)
+            assert _f32_digest(Us, Qs) == str(d[f"{name}__steps32_{label}_sha256"]), label
 
 
 @pytest.mark.parametrize("name", [n for n in _cases()[1] if f"{n}__metrics32_sha256" in _cases()[0].files])
